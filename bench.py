@@ -1,0 +1,322 @@
+#!/usr/bin/env python
+"""Benchmark of the trace-sampling hot path at Hilbert dimension 55296.
+
+Workload (one "step"): the single large radical pair (radical A = two 14N +
+five 1H, radical B = one 14N + four 1H; anisotropic hyperfine tensors, tilted
+0.05 mT field, J = 0.01 mT, axial D = -0.4 mT, kS = kT = 1/us), M = 512
+random-phase sample vectors, Krylov dimension 30, dt = 1 ns, propagated over
+a window of --window-ns (default 100 ns = 100 dt steps, about four Krylov
+builds per sample, the steady-state build/reuse ratio of the full 2 us run).
+A step is the whole hot path: device Hamiltonian build (general builder) +
+batched propagation + sample average.
+
+Metric: sample-steps/s = M * (dt steps per sample) / wall time.
+  value  device-resident inputs (spc_trace_sampling_device)
+  e2e    through the C ABI with host buffers (spc_build_h + spc_trace_sampling:
+         host->device copy of the sample vectors and device->host copy of the
+         populations inside the timed region)
+--impl reference times the CPU oracle (C++ restatement of the Fortran
+reference; the Fortran itself cannot be built here) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from spin_dynamics_gb300 import workloads as W  # noqa: E402
+
+METRIC = "sample-steps/s at dim 55296 (trace sampling, complex128, M=512, m=30)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--window-ns", type=float, default=100.0)
+    p.add_argument("--samples", type=int, default=512)
+    p.add_argument("--krylov", type=int, default=30)
+    p.add_argument("--cpu-samples", type=int, default=0, help="CPU sample size (0 = 2 x cores)")
+    p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def workload(args):
+    sysp, B = W.large_pair()
+    sim = W.large_sim(M=args.samples, t_end_ns=args.window_ns)
+    return sysp, B, sim
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def cpu_leg(args, sysp, B, sim, threads):
+    """Time the oracle (fast build) on a bounded sample of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    e1, e2 = sysp.e1, sysp.e2
+    rp, col, val = pyoracle.build_h_general(e1.g_I, e1.A, e1.gammas, e2.g_I, e2.A, e2.gammas, B,
+                                            sysp.J, sysp.D, sysp.kS, sysp.kT)
+    ns = args.cpu_samples or 2 * threads
+    zk = W.random_phase_samples(sysp.Z, ns)
+    t0 = time.perf_counter()
+    r = pyoracle.trace_sampling(rp, col, val, zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol,
+                                fast=True, threads=threads)
+    el = time.perf_counter() - t0
+    steps = int(round(sim.t_end / sim.dt))
+    return {"value": ns * steps / el, "unit": "sample-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{ns} samples x {steps} dt steps of the same system (Krylov builds "
+                      f"{int(r['n_builds'].sum())}), oracle -O3 native OpenMP, {el:.2f} s, "
+                      f"CPU {cpu_model()}"}
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=6)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    from spin_dynamics_gb300 import _native as nat
+    from spin_dynamics_gb300.dynamics import TraceSampler, num_time_points
+
+    torch.cuda.set_device(local_rank)
+    sysp, B, sim = workload(args)
+    M, m = sim.N_samples, sim.N_krylov
+    T = num_time_points(sim.dt, sim.t_end)
+    steps_per_sample = int(round(sim.t_end / sim.dt))
+    sampler = TraceSampler(local_rank)
+    stream = torch.cuda.current_stream()
+    sampler.set_stream(stream.cuda_stream)
+    zk_host = W.random_phase_samples(sysp.Z, M, seed=7 + rank)
+    zk_dev = torch.from_numpy(zk_host).to(f"cuda:{local_rank}")
+    out_dev = torch.empty(4 * T, dtype=torch.float64, device=f"cuda:{local_rank}")
+
+    def step_device():
+        sampler.build_h(sysp, B, "general")
+        sampler.trace_sampling_device(zk_dev.data_ptr(), M, sim.dt, sim.t_end, m, sim.tol,
+                                      out_dev.data_ptr())
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    # timed region, device-resident inputs; kernel classes timed with events
+    nat.check(nat.lib().spc_set_profiling(sampler.handle, 1))
+    launches = 0
+    builds = 0
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local_rank) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_device()
+            st = sampler.stats()
+            launches += st["kernel_launches"] + 4  # + the Hamiltonian build kernels
+            builds += st["krylov_builds"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    prof = {}
+    import ctypes as C
+    for k in range(nat.SPC_KERNEL_KINDS):
+        a, n, f, b = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
+        nat.lib().spc_get_profile(sampler.handle, k, C.byref(a), C.byref(n), C.byref(f), C.byref(b))
+        prof[nat.lib().spc_kernel_kind_name(k).decode()] = (a.value, n.value, f.value, b.value)
+    nat.check(nat.lib().spc_set_profiling(sampler.handle, 0))
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * M * steps_per_sample / (ms / 1e3)
+
+    # e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        zk_pin = torch.from_numpy(zk_host).pin_memory()
+        zk_np = zk_pin.numpy()
+        step_host = lambda: (sampler.build_h(sysp, B, "general"),
+                             sampler.trace_sampling(zk_np, sim.dt, sim.t_end, m, sim.tol))
+        step_host()
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res = step_host()[1]
+        torch.cuda.synchronize()
+        el = (time.perf_counter() - t0) / args.steps
+        if world > 1:
+            t = torch.tensor([el], device=f"cuda:{local_rank}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        e2e = {"value": world * M * steps_per_sample / el, "unit": "sample-steps/s",
+               "h2d_bytes_per_step": int(zk_host.nbytes), "d2h_bytes_per_step": int(4 * T * 8),
+               "ms_per_step": el * 1e3}
+    fp64 = C.c_double()
+    nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
+    return dict(ms=ms, value=value, e2e=e2e, prof=prof, clocks=clk.summary(), launches=launches,
+                builds=builds, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
+                sysp=sysp, B=B, sim=sim)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    base = {"metric": METRIC, "unit": "sample-steps/s", "higher_is_better": True,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "vs_baseline": None,
+            "dtype": "c128 (complex FP64)", "data": "synthetic (seeded system and random-phase vectors)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sysp, B, sim = workload(args)
+        threads = host_cores()
+        vals = []
+        for _ in range(max(1, args.warmup // 3)):
+            cpu_leg(args, sysp, B, sim, threads)  # warm-up (page-in, OpenMP pool)
+        for _ in range(args.steps):
+            vals.append(cpu_leg(args, sysp, B, sim, threads))
+        v = float(np.median([x["value"] for x in vals]))
+        cb = dict(vals[0])
+        cb["value"] = v
+        line = dict(base, impl="reference", value=v, ms_per_step=None, scaling="weak",
+                    config={"workload": "large pair dim 55296, anisotropic, window "
+                            f"{args.window_ns:g} ns", "samples_per_step": cb["sample"]},
+                    cpu_baseline=cb,
+                    e2e={"value": v, "unit": "sample-steps/s", "h2d_bytes_per_step": 0,
+                         "d2h_bytes_per_step": 0})
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    r = run_ours(args, rank, world, local_rank)
+    if rank != 0:
+        return
+    peaks, peak_src = measured_peaks()
+    prof = r["prof"]
+    dom = max(prof, key=lambda k: prof[k][0])
+    ms_tot, nl, fl, by = prof[dom]
+    avg_s = ms_tot / max(nl, 1) / 1e3
+    ach_gbs = (by / max(nl, 1)) / avg_s / 1e9 if nl else None
+    ach_tf = (fl / max(nl, 1)) / avg_s / 1e12 if nl else None
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_leg(args, r["sysp"], r["B"], r["sim"], host_cores())
+    share = {k: round(v[0] / max(1e-9, sum(x[0] for x in prof.values())), 4) for k, v in prof.items()}
+    line = dict(base, value=r["value"], ms_per_step=r["ms"], scaling="weak",
+                config={"workload": f"large pair dim 55296 (A: 2x14N+5x1H, B: 14N+4x1H), anisotropic "
+                                    f"hyperfine, tilted B 0.05 mT, J 0.01 mT, D -0.4 mT; M={r['M']}, "
+                                    f"m={r['sim'].N_krylov}, tol={r['sim'].tol:g}, dt 1 ns, window "
+                                    f"{args.window_ns:g} ns",
+                        "samples": r["M"], "dt_steps_per_sample": r["steps_per_sample"],
+                        "krylov_builds_per_step": r["builds"] / args.steps,
+                        "l2": "inputs larger than L2 (Krylov basis 13.6 GB per build)",
+                        "parallelism": f"replicas x{args.gpus}"},
+                e2e=r["e2e"], gpu_launches=int(r["launches"]), clocks=r["clocks"],
+                roofline={"kernel": dom, "bound": "hbm", "achieved": ach_gbs,
+                          "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                          "frac": (ach_gbs / peaks["hbm_gbs"]) if ach_gbs else None,
+                          "traffic": None, "peak_source": peak_src,
+                          "fp64": {"achieved_tflops": ach_tf, "peak_tflops": r["fp64_peak"] / 1e12,
+                                   "frac": (ach_tf * 1e12 / r["fp64_peak"]) if ach_tf else None,
+                                   "peak_source": "measured DFMA probe (spc_fp64_peak)"}},
+                kernel_share=share, cpu_baseline=cpu)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,203 @@
+/*
+ * spinchem_gpu.h — C ABI of the GB300 trace-sampling library (libspinchem_gpu.so).
+ *
+ * Drop-in for the quantum hot path of KenHino/Spin_dynamics (`spinchem`):
+ * the sparse spin Hamiltonian build and trace-sampling propagation behind
+ * `trace_sampling_para` (src/qm_dynamics.f90:257-384). Every entry point is
+ * plain C: integers, doubles and pointers, callable from Fortran through
+ * iso_c_binding (bind(C)), from C/C++, and from Python through ctypes.
+ *
+ * Conventions
+ *  - Status: every function returns 0 (SPC_OK) or a positive SPC_ERR_* code;
+ *    spc_last_error() gives the message of the last failure on this thread.
+ *    Where the reference stops the program (`stop 'Error: ...'`) the library
+ *    returns SPC_ERR_UNSUPPORTED or SPC_ERR_ARG with the same message.
+ *  - Complex numbers are complex(dp) / double _Complex: interleaved (re, im)
+ *    pairs of doubles.
+ *  - Units are the reference's internal units after read_inp
+ *    (src/spinsys.f90:88-89,107-108): energies in mT, kS and kT in 1/us
+ *    divided by gamma_e = 176.08596, dt and t_end in ns * gamma_e / 1000.
+ *  - A handle owns one CUDA device, one stream and the device buffers; it is
+ *    not thread-safe. Host pointers are caller-owned and only read/written
+ *    during the call.
+ *  - No CPU fallback: a handle cannot be created without a usable GPU.
+ */
+#ifndef SPINCHEM_GPU_H
+#define SPINCHEM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPC_OK 0
+#define SPC_ERR_ARG 1          /* bad argument (sizes, null pointers, unknown mode) */
+#define SPC_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define SPC_ERR_ALLOC 3        /* device or host allocation failed */
+#define SPC_ERR_UNSUPPORTED 4  /* a system the reference refuses (its `stop` conditions) */
+#define SPC_ERR_NUMERIC 5      /* time-index overflow or non-finite result */
+#define SPC_ERR_STATE 6        /* call order: e.g. propagation before a Hamiltonian exists */
+
+typedef struct spc_handle spc_handle;
+
+/* Spin system, host memory. Replaces the fields of `sys_param`/`electron`
+ * (src/spinsys.f90:21-38) that getHiso_sp reads (src/hamiltonian.f90:17-205),
+ * plus the field vector that app/main.f90:53-54 turns into the Larmor
+ * frequencies w = -B. */
+typedef struct {
+  int n_nuc1, n_nuc2;      /* nuclei on radical 1 and radical 2 */
+  const int* mult1;        /* nuclear multiplicities (2 = 1H, 3 = 14N, ...) */
+  const int* mult2;
+  const double* A1;        /* 9 doubles per nucleus: column-major 3x3 hyperfine tensor (mT),
+                              the order of the A<i> keys in input.ini */
+  const double* A2;
+  const double* gamma1;    /* nuclear gyromagnetic ratios; NULL = by multiplicity as the
+                              reference assigns them (src/hamiltonian.f90:132-138) */
+  const double* gamma2;
+  double B[3];             /* field vector (mT); the reference's scalar B is (0, 0, B) */
+  double J;                /* exchange (mT) */
+  double D[9];             /* dipolar tensor, column-major (mT) */
+  double kS, kT;           /* Haberkorn rates, internal units */
+} spc_system;
+
+/* Compressed sparse row matrix in HOST memory (stdlib CSR_cdp_type layout:
+ * rowptr(n+1), col(nnz), data(nnz) complex). index_base is 0 or 1. */
+typedef struct {
+  int32_t n;
+  int64_t nnz;
+  int32_t* rowptr;
+  int32_t* col;
+  double* val;       /* 2*nnz doubles */
+  int32_t index_base;
+} spc_csr;
+
+/* Hamiltonian build modes for spc_build_h. */
+#define SPC_H_REFERENCE 0  /* getHiso_sp + coo_to_csr: isotropic a = trace(A)/3, field along z
+                              (B[0], B[1] must be 0), axial D; CSR rows in the reference's order */
+#define SPC_H_GENERAL 1    /* anisotropic S.A.I, field vector, full D tensor; columns ascending */
+
+/* Counters of the last propagation call. */
+typedef struct {
+  int64_t krylov_builds;   /* sum over samples of Krylov subspaces built */
+  int64_t rounds;          /* batched build rounds (max builds of any sample) */
+  int64_t sample_steps;    /* sum over samples of dt steps taken */
+  int64_t kernel_launches; /* kernels launched by the library during the call */
+  double seconds;          /* wall time of the call */
+} spc_stats;
+
+/* ---- library / handle ------------------------------------------------- */
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* spc_last_error(void);
+
+/* Create a handle on CUDA device `device` (one stream, no buffers yet).
+ * Returns SPC_ERR_CUDA when no usable GPU is present. */
+int spc_create(int device, spc_handle** out);
+
+/* Release every device buffer and the stream. */
+int spc_destroy(spc_handle* h);
+
+/* Use a caller-owned cudaStream_t (NULL = the handle's own stream). */
+int spc_set_stream(spc_handle* h, void* cuda_stream);
+
+/* ---- Hamiltonian ------------------------------------------------------ */
+
+/* Build H_eff = H - iK/2 on the device and keep it in the handle.
+ * SPC_H_REFERENCE replaces getHiso_sp (src/hamiltonian.f90:17-205) followed by
+ * coo_to_csr (src/utils.f90:52-89): same nonzeros, same within-row order.
+ * SPC_H_GENERAL is the anisotropic extension (no sparse reference counterpart;
+ * hyperfine form of getH_dense, src/hamiltonian.f90:279-311). */
+int spc_build_h(spc_handle* h, const spc_system* sys, int mode);
+
+/* Upload a caller-built CSR (host memory, 0- or 1-based) as the Hamiltonian.
+ * Replaces passing `type(CSR_cdp_type) :: H` into the propagation. */
+int spc_set_h(spc_handle* h, const spc_csr* H);
+
+/* Dimension and nonzero count of the handle's Hamiltonian. */
+int spc_h_size(const spc_handle* h, int32_t* n, int64_t* nnz);
+
+/* Copy the handle's Hamiltonian to caller buffers (rowptr n+1, col nnz,
+ * val 2*nnz), 0-based indices. */
+int spc_get_h(spc_handle* h, int32_t* rowptr, int32_t* col, double* val);
+
+/* ---- propagation ------------------------------------------------------ */
+
+/* Number of output time points: N_steps + 1 with
+ * N_steps = ceiling((t_end + dt)/dt) (src/qm_dynamics.f90:305-306). */
+int spc_num_time_points(double dt, double t_end);
+
+/* Trace-sampling propagation of M caller-supplied nuclear sample vectors.
+ * Replaces the body of trace_sampling_para from the OpenMP region to the
+ * sample average (src/qm_dynamics.f90:322-378): for every sample, psi =
+ * theta (x) z (kron_vector), Arnoldi/MGS Krylov bases of dimension m
+ * (get_krylov :432-467), the Pade-6 exponential of -i dt A (expm,
+ * src/matrix_exponential.f90:14-87), the Krylov-space projectors
+ * (convert_to_krylov :469-498) and the Krylov-reuse dt loop (:340-366) with
+ * the rebuild test |c_m|^2 <= tol |c|^2; then the sample average
+ * (res%update, res%scale(1/M)).
+ *   theta    4 complex, the electronic state (init_el_state :386-414)
+ *   init_pop 4 doubles, populations at t = 0 in the order S, T0, Tp, Tm
+ *   zkets    M x Z complex in host memory, sample-major (Z = n/4)
+ *   outputs  P_S, P_T0, P_Tp, P_Tm: T doubles each, host memory,
+ *            T = spc_num_time_points(dt, t_end); trailing slots the dt loop
+ *            never reaches stay 0 as in the reference.
+ * The host buffers are copied to and from the device inside the call. */
+int spc_trace_sampling(spc_handle* h, const double* theta, const double* init_pop,
+                       const double* zkets, int M, double dt, double t_end, int m, double tol,
+                       double* P_S, double* P_T0, double* P_Tp, double* P_Tm, int T);
+
+/* The same on device-resident buffers (no host copies, asynchronous apart
+ * from one small flag read per build round): zkets_dev is M x Z complex,
+ * out_dev receives 4*T doubles (P_S | P_T0 | P_Tp | P_Tm). */
+int spc_trace_sampling_device(spc_handle* h, const double* theta, const double* init_pop,
+                              const double* zkets_dev, int M, double dt, double t_end, int m,
+                              double tol, double* out_dev, int T);
+
+/* Counters of the last propagation call on this handle. */
+int spc_get_stats(const spc_handle* h, spc_stats* out);
+
+/* ---- host helpers ----------------------------------------------------- */
+
+/* Sample vectors exactly as the reference draws them: the master
+ * xoroshiro128+ generator seeded with `seed` (app/main.f90:48,
+ * src/m_random.f90:90-98); mode 0 = trace_sampling_para (two next() per
+ * sample, then set_seed + sample_SUZ per sample, src/qm_dynamics.f90:315-327),
+ * mode 1 = trace_sampling (one stream, :198-199). out: M x Z complex. */
+int spc_seeded_samples(int64_t seed0, int64_t seed1, int Z, int M, int mode, double* out);
+
+/* Electronic initial state and populations (init_el_state,
+ * src/qm_dynamics.f90:386-414): which = 0 singlet, 1 T0, 2 Tp, 3 Tm. */
+int spc_init_el_state(int which, double* theta, double* init_pop);
+
+/* Singlet/triplet yields by Simpson's rule (get_kinetics,
+ * src/observables.f90:74-101). Inputs T each; Phi_S/Phi_T get T/2 entries,
+ * iden T entries; any output may be NULL. */
+int spc_kinetics(int T, const double* P_S, const double* P_T0, const double* P_Tp,
+                 const double* P_Tm, double dt, double kS, double kT, double* Phi_S,
+                 double* Phi_T, double* iden);
+
+/* ---- diagnostics (no counterpart in the reference) ------------------- */
+
+/* Time every kernel launch of later propagation calls with CUDA events on
+ * the handle's stream, per kernel class (0 disables). */
+int spc_set_profiling(spc_handle* h, int enable);
+
+/* Accumulated time (ms), launches, and the algorithmic FLOPs and bytes of
+ * kernel class `kind` (0 <= kind < SPC_KERNEL_KINDS) since profiling was
+ * enabled. */
+#define SPC_KERNEL_KINDS 11
+int spc_get_profile(const spc_handle* h, int kind, double* ms, int64_t* launches, double* flops,
+                    double* bytes);
+
+/* Name of kernel class `kind` ("spmm", "mgs_axpy_dot", ...). */
+const char* spc_kernel_kind_name(int kind);
+
+/* FP64 FMA throughput of device `device` in TFLOP/s (a dependent-free DFMA
+ * probe, best of 5), the roof of this FP64-bound path. */
+int spc_fp64_peak(int device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPINCHEM_GPU_H */

@@ -1,0 +1,212 @@
+// extern "C" entry points of libspinchem_gpu (declared in include/spinchem_gpu.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "spc_internal.h"
+
+struct spc_handle {
+  spc::Handle h;
+};
+
+namespace spc {
+const char* last_error();
+void clear_error();
+}  // namespace spc
+
+#define CKR(call)                                                                             \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return spc::set_error(SPC_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));    \
+  } while (0)
+
+extern "C" {
+
+int spc_create(int device, spc_handle** out) {
+  if (!out) return spc::set_error(SPC_ERR_ARG, "null output pointer");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0)
+    return spc::set_error(SPC_ERR_CUDA, "no CUDA device available (%s)",
+                          e != cudaSuccess ? cudaGetErrorString(e) : "count = 0");
+  if (device < 0 || device >= count)
+    return spc::set_error(SPC_ERR_ARG, "device %d out of range (%d devices)", device, count);
+  CKR(cudaSetDevice(device));
+  spc_handle* hh = new (std::nothrow) spc_handle();
+  if (!hh) return spc::set_error(SPC_ERR_ALLOC, "host allocation failed");
+  hh->h.device = device;
+  e = cudaStreamCreateWithFlags(&hh->h.own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete hh;
+    return spc::set_error(SPC_ERR_CUDA, "cudaStreamCreate failed: %s", cudaGetErrorString(e));
+  }
+  hh->h.stream = hh->h.own_stream;
+  cudaDeviceGetAttribute(&hh->h.sm_count, cudaDevAttrMultiProcessorCount, device);
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  hh->h.smem_optin = (size_t)optin;
+  *out = hh;
+  spc::clear_error();
+  return SPC_OK;
+}
+
+int spc_destroy(spc_handle* h) {
+  if (!h) return SPC_OK;
+  cudaSetDevice(h->h.device);
+  if (h->h.stream) cudaStreamSynchronize(h->h.stream);
+  delete h;
+  return SPC_OK;
+}
+
+int spc_set_stream(spc_handle* h, void* stream) {
+  if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
+  h->h.stream = stream ? (cudaStream_t)stream : h->h.own_stream;
+  return SPC_OK;
+}
+
+int spc_build_h(spc_handle* h, const spc_system* sys, int mode) {
+  if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
+  CKR(cudaSetDevice(h->h.device));
+  spc::HostSystem hs;
+  int rc = spc::make_host_system(sys, mode, hs);
+  if (rc != SPC_OK) return rc;
+  return spc::build_h_device(&h->h, hs, mode);
+}
+
+int spc_set_h(spc_handle* h, const spc_csr* H) {
+  if (!h || !H || !H->rowptr || !H->col || !H->val || H->n < 4 || H->n % 4 != 0 || H->nnz < 0 ||
+      (H->index_base != 0 && H->index_base != 1))
+    return spc::set_error(SPC_ERR_ARG, "spc_set_h: bad argument (n must be a positive multiple of 4)");
+  if (H->nnz > INT32_MAX) return spc::set_error(SPC_ERR_ARG, "nnz above the int32 CSR limit");
+  const int n = H->n;
+  const int64_t nnz = H->nnz;
+  const int b = H->index_base;
+  if ((int64_t)H->rowptr[0] != b || (int64_t)H->rowptr[n] - b != nnz)
+    return spc::set_error(SPC_ERR_ARG, "row pointer does not match nnz");
+  std::vector<int> rp(n + 1), cl(nnz > 0 ? nnz : 1);
+  for (int i = 0; i <= n; ++i) {
+    rp[i] = H->rowptr[i] - b;
+    if (i > 0 && rp[i] < rp[i - 1]) return spc::set_error(SPC_ERR_ARG, "row pointer not monotone");
+  }
+  for (int64_t k = 0; k < nnz; ++k) {
+    cl[k] = H->col[k] - b;
+    if (cl[k] < 0 || cl[k] >= n) return spc::set_error(SPC_ERR_ARG, "column index out of range");
+  }
+  CKR(cudaSetDevice(h->h.device));
+  if (h->h.ensure_rowptr(n + 1) || h->h.ensure_h_entries(nnz)) return SPC_ERR_ALLOC;
+  CKR(cudaMemcpy(h->h.d_rowptr, rp.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+  if (nnz > 0) {
+    CKR(cudaMemcpy(h->h.d_col, cl.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
+    CKR(cudaMemcpy(h->h.d_val, H->val, sizeof(double2) * nnz, cudaMemcpyHostToDevice));
+  }
+  h->h.n = n;
+  h->h.nnz = nnz;
+  return SPC_OK;
+}
+
+int spc_h_size(const spc_handle* h, int32_t* n, int64_t* nnz) {
+  if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
+  if (n) *n = h->h.n;
+  if (nnz) *nnz = h->h.nnz;
+  return SPC_OK;
+}
+
+int spc_get_h(spc_handle* h, int32_t* rowptr, int32_t* col, double* val) {
+  if (!h || !rowptr || !col || !val) return spc::set_error(SPC_ERR_ARG, "null pointer");
+  if (h->h.n == 0) return spc::set_error(SPC_ERR_STATE, "no Hamiltonian in the handle");
+  CKR(cudaSetDevice(h->h.device));
+  CKR(cudaStreamSynchronize(h->h.stream));
+  CKR(cudaMemcpy(rowptr, h->h.d_rowptr, sizeof(int) * (h->h.n + 1), cudaMemcpyDeviceToHost));
+  if (h->h.nnz > 0) {
+    CKR(cudaMemcpy(col, h->h.d_col, sizeof(int) * h->h.nnz, cudaMemcpyDeviceToHost));
+    CKR(cudaMemcpy(val, h->h.d_val, sizeof(double2) * h->h.nnz, cudaMemcpyDeviceToHost));
+  }
+  return SPC_OK;
+}
+
+int spc_num_time_points(double dt, double t_end) {
+  if (!(dt > 0.0)) return -1;
+  return spc::num_time_points(dt, t_end);
+}
+
+static int check_prop_args(spc_handle* h, const double* theta, const double* init_pop, int M,
+                           double dt, int m, int T) {
+  if (!h || !theta || !init_pop) return spc::set_error(SPC_ERR_ARG, "null pointer");
+  if (h->h.n == 0) return spc::set_error(SPC_ERR_STATE, "no Hamiltonian: call spc_build_h or spc_set_h first");
+  if (M < 1) return spc::set_error(SPC_ERR_ARG, "need at least one sample");
+  if (!(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt must be positive");
+  if (m < 1 || m > 48) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d outside [1, 48]", m);
+  if (m > h->h.n) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d exceeds the Hilbert dimension %d", m, h->h.n);
+  if (T < 1) return spc::set_error(SPC_ERR_ARG, "need at least one output slot");
+  return SPC_OK;
+}
+
+int spc_trace_sampling_device(spc_handle* h, const double* theta, const double* init_pop,
+                              const double* zkets_dev, int M, double dt, double t_end, int m,
+                              double tol, double* out_dev, int T) {
+  int rc = check_prop_args(h, theta, init_pop, M, dt, m, T);
+  if (rc) return rc;
+  if (!zkets_dev || !out_dev) return spc::set_error(SPC_ERR_ARG, "null device pointer");
+  if (T != spc::num_time_points(dt, t_end))
+    return spc::set_error(SPC_ERR_ARG, "T must be spc_num_time_points(dt, t_end) = %d",
+                          spc::num_time_points(dt, t_end));
+  CKR(cudaSetDevice(h->h.device));
+  return spc::propagate(&h->h, theta, init_pop, zkets_dev, M, dt, t_end, m, tol, out_dev, T);
+}
+
+int spc_trace_sampling(spc_handle* h, const double* theta, const double* init_pop,
+                       const double* zkets, int M, double dt, double t_end, int m, double tol,
+                       double* P_S, double* P_T0, double* P_Tp, double* P_Tm, int T) {
+  int rc = check_prop_args(h, theta, init_pop, M, dt, m, T);
+  if (rc) return rc;
+  if (!zkets || !P_S || !P_T0 || !P_Tp || !P_Tm) return spc::set_error(SPC_ERR_ARG, "null pointer");
+  if (T != spc::num_time_points(dt, t_end))
+    return spc::set_error(SPC_ERR_ARG, "T must be spc_num_time_points(dt, t_end) = %d",
+                          spc::num_time_points(dt, t_end));
+  CKR(cudaSetDevice(h->h.device));
+  const int64_t Z = h->h.n / 4;
+  spc::Handle& H = h->h;
+  if (H.ensure(H.zk, sizeof(double) * 2 * Z * M) || H.ensure(H.out, sizeof(double) * 4 * T))
+    return SPC_ERR_ALLOC;
+  CKR(cudaMemcpyAsync(H.zk.p, zkets, sizeof(double) * 2 * Z * M, cudaMemcpyHostToDevice, H.stream));
+  rc = spc::propagate(&H, theta, init_pop, (const double*)H.zk.p, M, dt, t_end, m, tol,
+                      (double*)H.out.p, T);
+  if (rc) return rc;
+  double* outs[4] = {P_S, P_T0, P_Tp, P_Tm};
+  for (int q = 0; q < 4; ++q)
+    CKR(cudaMemcpyAsync(outs[q], (double*)H.out.p + (size_t)q * T, sizeof(double) * T,
+                        cudaMemcpyDeviceToHost, H.stream));
+  CKR(cudaStreamSynchronize(H.stream));
+  return SPC_OK;
+}
+
+int spc_set_profiling(spc_handle* h, int enable) {
+  if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
+  h->h.prof.on = enable != 0;
+  h->h.prof.reset();
+  return SPC_OK;
+}
+
+int spc_get_profile(const spc_handle* h, int kind, double* ms, int64_t* launches, double* flops,
+                    double* bytes) {
+  if (!h || kind < 0 || kind >= spc::PROF_KINDS) return spc::set_error(SPC_ERR_ARG, "bad argument");
+  const spc::Prof& p = h->h.prof;
+  if (ms) *ms = p.ms[kind];
+  if (launches) *launches = p.launches[kind];
+  if (flops) *flops = p.flops[kind];
+  if (bytes) *bytes = p.bytes[kind];
+  return SPC_OK;
+}
+
+int spc_get_stats(const spc_handle* h, spc_stats* out) {
+  if (!h || !out) return spc::set_error(SPC_ERR_ARG, "null pointer");
+  *out = h->h.stats;
+  return SPC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,319 @@
+// Device-side sparse Hamiltonian assembly.
+//
+// Both builders generate CSR rows directly from the Kronecker structure of
+// the radical-pair basis (row = e*Z + n, electron state e = 2*s1 + s2 with
+// s = 0 for m = +1/2, nuclear index n row-major over radical-1 then radical-2
+// nuclei, each from m = +I down). A row's entries are computed by one thread;
+// counts -> exclusive scan -> fill.
+//
+// SPC_H_REFERENCE reproduces getHiso_sp (src/hamiltonian.f90:17-205) followed
+// by coo_to_csr (src/utils.f90:52-89): the same nonzeros (explicit zeros
+// included), the same values rounded at the same points (no FMA contraction:
+// __dmul_rn/__dadd_rn), and the same within-row order, which is the reverse
+// of the order the COO blocks are appended in:
+//   diag | S1+S2- | S1-S2+ | per radical-1 nucleus: S1+I-, S1-I+ | per
+//   radical-2 nucleus: S2+I-, S2-I+
+// SPC_H_GENERAL is the anisotropic extension (no sparse reference
+// counterpart): every S_r I_c product of S.A.I, nuclear Zeeman along the
+// field vector, the full electron-electron tensor; columns ascending, fixed
+// structural pattern.
+#include "spc_common.cuh"
+#include "spc_internal.h"
+
+namespace spc {
+
+// ---- exact (uncontracted) complex arithmetic -------------------------------
+__device__ __forceinline__ double2 xmul(double2 a, double2 b) {
+  return make_double2(__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)),
+                      __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ double2 xadd(double2 a, double2 b) {
+  return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y));
+}
+__device__ __forceinline__ double2 xrscale(double s, double2 a) {
+  return make_double2(__dmul_rn(s, a.x), __dmul_rn(s, a.y));
+}
+
+// nuclear state of nucleus j in nuclear index n
+__device__ __forceinline__ int nuc_state(const NucInfo& q, int64_t n) {
+  return (int)((n / q.stride) % q.g);
+}
+
+// Spin-I ladder element sqrt(S(S+1) - m_a m_b) as get_spinop_sp computes it
+// (src/spinop.f90:88-92): m values S, S-1, ...; S(S+1) minus the complex
+// product of the two Sz entries.
+__device__ __forceinline__ double ladder(int g, int a, int b) {
+  double S = ((double)g - 1.0) / 2.0;
+  double ma = S - (double)a, mb = S - (double)b;
+  return __dsqrt_rn(__dsub_rn(__dmul_rn(S, __dadd_rn(S, 1.0)), __dmul_rn(ma, mb)));
+}
+
+// ---------------------------------------------------------------------------
+// reference builder
+__device__ int ref_row_count(int64_t row, int64_t Z, int nn, const NucInfo* nuc) {
+  int e = (int)(row / Z);
+  int64_t n = row - (int64_t)e * Z;
+  int s1 = e >> 1, s2 = e & 1;
+  int cnt = 1 + (e == 1) + (e == 2);
+  for (int j = 0; j < nn; ++j) {
+    const NucInfo& q = nuc[j];
+    int a = nuc_state(q, n);
+    int s = q.owner == 0 ? s1 : s2;
+    // S+ I- : electron up (s == 0), nucleus not at the top (a >= 1)
+    if (s == 0 && a >= 1) cnt++;
+    // S- I+ : electron down, nucleus not at the bottom
+    if (s == 1 && a <= q.g - 2) cnt++;
+  }
+  return cnt;
+}
+
+__global__ void k_ref_count(int64_t N, int64_t Z, int nn, const NucInfo* __restrict__ nuc,
+                            int* __restrict__ cnt) {
+  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  cnt[row] = ref_row_count(row, Z, nn, nuc);
+}
+
+__global__ void k_ref_fill(int64_t N, int64_t Z, int nn, const NucInfo* __restrict__ nuc,
+                           RefElectron el, const int* __restrict__ rowptr, int* __restrict__ col,
+                           double2* __restrict__ val) {
+  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  int e = (int)(row / Z);
+  int64_t n = row - (int64_t)e * Z;
+  int s1 = e >> 1, s2 = e & 1;
+  int k = rowptr[row];
+  // reverse COO block order: last nucleus of radical 2 first
+  for (int j = nn - 1; j >= 0; --j) {
+    const NucInfo& q = nuc[j];
+    int a = nuc_state(q, n);
+    int s = q.owner == 0 ? s1 : s2;
+    int eflip = q.owner == 0 ? 2 : 1;  // electron-index offset of a spin flip
+    // block S- I+ (appended after S+ I-, so it comes first here)
+    if (s == 1 && a <= q.g - 2) {
+      double2 v = xmul(make_double2(q.a_half, 0.0), make_double2(ladder(q.g, a, a + 1), 0.0));
+      col[k] = (int)((int64_t)(e - eflip) * Z + n + q.stride);
+      val[k] = v;
+      k++;
+    }
+    if (s == 0 && a >= 1) {
+      double2 v = xmul(make_double2(q.a_half, 0.0), make_double2(ladder(q.g, a, a - 1), 0.0));
+      col[k] = (int)((int64_t)(e + eflip) * Z + n - q.stride);
+      val[k] = v;
+      k++;
+    }
+  }
+  if (e == 2) {  // S1- S2+ : |ba> -> |ab>
+    col[k] = (int)(1 * Z + n);
+    val[k] = el.flip_ba;
+    k++;
+  }
+  if (e == 1) {  // S1+ S2- : |ab> -> |ba>
+    col[k] = (int)(2 * Z + n);
+    val[k] = el.flip_ab;
+    k++;
+  }
+  // diagonal: electronic part, then each nucleus in assembly order
+  double2 d = el.diag[e];
+  for (int j = 0; j < nn; ++j) {
+    const NucInfo& q = nuc[j];
+    int a = nuc_state(q, n);
+    int s = q.owner == 0 ? s1 : s2;
+    double sz = s == 0 ? 0.5 : -0.5;
+    double2 x = xadd(xrscale(q.a_iso, make_double2(sz, 0.0)), xrscale(q.zf, make_double2(1.0, 0.0)));
+    double S = ((double)q.g - 1.0) / 2.0;
+    double m = S - (double)a;
+    d = xadd(d, xmul(x, make_double2(m, 0.0)));
+  }
+  col[k] = (int)row;
+  val[k] = d;
+}
+
+// ---------------------------------------------------------------------------
+// general builder (mirrors the ascending-column generator of the oracle)
+__device__ __forceinline__ double2 spin_half_el(int r, int a, int b) {
+  if (r == 2) return a == b ? make_double2(a == 0 ? 0.5 : -0.5, 0.0) : cz();
+  if (a == b) return cz();
+  if (r == 0) return make_double2(0.5, 0.0);
+  return a == 0 ? make_double2(0.0, -0.5) : make_double2(0.0, 0.5);
+}
+__device__ __forceinline__ double2 pair_el(int k, int r, int e, int ep) {
+  int s1 = e >> 1, s2 = e & 1, t1 = ep >> 1, t2 = ep & 1;
+  if (k == 0) return s2 == t2 ? spin_half_el(r, s1, t1) : cz();
+  return s1 == t1 ? spin_half_el(r, s2, t2) : cz();
+}
+__device__ __forceinline__ double2 nuc_el(int g, int c, int a, int b) {
+  double I = (g - 1) / 2.0;
+  double ma = I - a, mb = I - b;
+  if (c == 2) return a == b ? make_double2(ma, 0.0) : cz();
+  double l;
+  if (a == b - 1 || a == b + 1)
+    l = __dsqrt_rn(__dsub_rn(__dmul_rn(I, __dadd_rn(I, 1.0)), __dmul_rn(ma, mb)));
+  else
+    return cz();
+  if (c == 0) return make_double2(__dmul_rn(0.5, l), 0.0);
+  return a == b - 1 ? make_double2(0.0, __dmul_rn(-0.5, l)) : make_double2(0.0, __dmul_rn(0.5, l));
+}
+
+__device__ int gen_row_count(int64_t row, int64_t Z, int nn, const NucInfo* nuc) {
+  int64_t n = row % Z;
+  int cnt = 4;
+  for (int j = 0; j < nn; ++j) {
+    int a = nuc_state(nuc[j], n);
+    int nb = (a > 0) + (a < nuc[j].g - 1);
+    cnt += 2 * nb;
+  }
+  return cnt;
+}
+
+__global__ void k_gen_count(int64_t N, int64_t Z, int nn, const NucInfo* __restrict__ nuc,
+                            int* __restrict__ cnt) {
+  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  cnt[row] = gen_row_count(row, Z, nn, nuc);
+}
+
+// One thread per row; entries accumulated in generation order into the
+// row's CSR slots, then insertion-sorted by column.
+__global__ void k_gen_fill(int64_t N, int64_t Z, int nn, const NucInfo* __restrict__ nuc,
+                           GenElectron el, const int* __restrict__ rowptr, int* __restrict__ col,
+                           double2* __restrict__ val) {
+  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  int e = (int)(row / Z);
+  int64_t nidx = row - (int64_t)e * Z;
+  int base = rowptr[row];
+  int ne = 0;
+  auto put = [&](int64_t c, double2 v) {
+    for (int t = 0; t < ne; ++t)
+      if (col[base + t] == (int)c) {
+        val[base + t] = xadd(val[base + t], v);
+        return;
+      }
+    col[base + ne] = (int)c;
+    val[base + ne] = v;
+    ne++;
+  };
+  for (int ep = 0; ep < 4; ++ep) put((int64_t)ep * Z + nidx, el.H[e][ep]);
+  for (int j = 0; j < nn; ++j) {
+    const NucInfo& q = nuc[j];
+    int g = q.g, k = q.owner;
+    int mj = nuc_state(q, nidx);
+    for (int mp = mj - 1; mp <= mj + 1; ++mp) {
+      if (mp < 0 || mp >= g) continue;
+      int64_t nc = nidx + (int64_t)(mp - mj) * q.stride;
+      for (int ep = 0; ep < 4; ++ep) {
+        int other_same = k == 0 ? ((e & 1) == (ep & 1)) : ((e >> 1) == (ep >> 1));
+        if (!other_same) continue;
+        double2 v = cz();
+        for (int r = 0; r < 3; ++r) {
+          double2 se = pair_el(k, r, e, ep);
+          for (int c = 0; c < 3; ++c) {
+            double2 ie = nuc_el(g, c, mj, mp);
+            v = xadd(v, xrscale(q.A[r * 3 + c], xmul(se, ie)));
+          }
+        }
+        if (ep == e)
+          for (int c = 0; c < 3; ++c) v = xadd(v, xrscale(q.zeta[c], nuc_el(g, c, mj, mp)));
+        put((int64_t)ep * Z + nc, v);
+      }
+    }
+  }
+  // insertion sort by column
+  for (int i = 1; i < ne; ++i) {
+    int c = col[base + i];
+    double2 v = val[base + i];
+    int t = i - 1;
+    while (t >= 0 && col[base + t] > c) {
+      col[base + t + 1] = col[base + t];
+      val[base + t + 1] = val[base + t];
+      t--;
+    }
+    col[base + t + 1] = c;
+    val[base + t + 1] = v;
+  }
+}
+
+// Exclusive scan of per-row counts into rowptr (one CTA of 1024 threads).
+__global__ void k_scan_rows(const int* __restrict__ cnt, int* __restrict__ rowptr, int64_t N,
+                            long long* __restrict__ total) {
+  __shared__ long long s[1024];
+  long long carry = 0;
+  for (int64_t base = 0; base < N; base += 1024) {
+    int64_t i = base + threadIdx.x;
+    long long v = i < N ? cnt[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      long long t = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < N) rowptr[i] = (int)(carry + s[threadIdx.x] - v);
+    long long blk = s[1023];
+    __syncthreads();
+    carry += blk;
+  }
+  if (threadIdx.x == 0) {
+    rowptr[N] = (int)carry;
+    *total = carry;
+  }
+}
+
+// ---------------------------------------------------------------------------
+int build_h_device(Handle* h, const HostSystem& hs, int mode) {
+  const int64_t N = hs.N, Z = hs.Z;
+  int nn = (int)hs.nuc.size();
+  NucInfo* d_nuc = nullptr;
+  int* d_cnt = nullptr;
+  long long* d_total = nullptr;
+  cudaStream_t st = h->stream;
+  int rc = SPC_OK;
+  if (cudaMalloc(&d_nuc, sizeof(NucInfo) * (nn > 0 ? nn : 1)) != cudaSuccess ||
+      cudaMalloc(&d_cnt, sizeof(int) * N) != cudaSuccess ||
+      cudaMalloc(&d_total, sizeof(long long)) != cudaSuccess) {
+    cudaFree(d_nuc);
+    cudaFree(d_cnt);
+    cudaFree(d_total);
+    return set_error(SPC_ERR_ALLOC, "device allocation for the Hamiltonian build failed");
+  }
+  if (nn > 0) cudaMemcpyAsync(d_nuc, hs.nuc.data(), sizeof(NucInfo) * nn, cudaMemcpyHostToDevice, st);
+  int threads = 256;
+  int blocks = (int)((N + threads - 1) / threads);
+  if (mode == SPC_H_REFERENCE)
+    k_ref_count<<<blocks, threads, 0, st>>>(N, Z, nn, d_nuc, d_cnt);
+  else
+    k_gen_count<<<blocks, threads, 0, st>>>(N, Z, nn, d_nuc, d_cnt);
+  h->ensure_rowptr(N + 1);
+  k_scan_rows<<<1, 1024, 0, st>>>(d_cnt, h->d_rowptr, N, d_total);
+  long long nnz = 0;
+  cudaMemcpyAsync(&nnz, d_total, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) {
+    rc = set_error(SPC_ERR_CUDA, "Hamiltonian count/scan failed: %s",
+                   cudaGetErrorString(cudaGetLastError()));
+  } else if (nnz > INT32_MAX) {
+    rc = set_error(SPC_ERR_ARG, "Hamiltonian has %lld nonzeros, above the int32 CSR limit", nnz);
+  } else if (h->ensure_h_entries(nnz) != SPC_OK) {
+    rc = SPC_ERR_ALLOC;
+  } else {
+    if (mode == SPC_H_REFERENCE)
+      k_ref_fill<<<blocks, threads, 0, st>>>(N, Z, nn, d_nuc, hs.ref, h->d_rowptr, h->d_col,
+                                              h->d_val);
+    else
+      k_gen_fill<<<blocks, threads, 0, st>>>(N, Z, nn, d_nuc, hs.gen, h->d_rowptr, h->d_col,
+                                              h->d_val);
+    h->count_launch(4);
+    if (cudaStreamSynchronize(st) != cudaSuccess)
+      rc = set_error(SPC_ERR_CUDA, "Hamiltonian fill failed: %s",
+                     cudaGetErrorString(cudaGetLastError()));
+    h->n = (int)N;
+    h->nnz = nnz;
+  }
+  cudaFree(d_nuc);
+  cudaFree(d_cnt);
+  cudaFree(d_total);
+  return rc;
+}
+
+}  // namespace spc

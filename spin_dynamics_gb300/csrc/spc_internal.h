@@ -1,0 +1,123 @@
+// Internal declarations shared by the translation units of libspinchem_gpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/spinchem_gpu.h"
+
+namespace spc {
+
+// Per-nucleus description used by both device Hamiltonian builders.
+struct NucInfo {
+  int g;            // multiplicity
+  int owner;        // 0 = radical 1, 1 = radical 2
+  int64_t stride;   // stride of this nucleus in the nuclear index
+  double a_iso;     // trace(A)/3 (reference builder)
+  double a_half;    // 0.5 * a_iso (reference builder off-diagonals)
+  double zf;        // nuclear Zeeman factor -w*gamma/gamma_e (reference builder)
+  double A[9];      // full tensor, A[r*3+c] (general builder)
+  double zeta[3];   // (gamma/gamma_e) * B_c (general builder)
+};
+
+// Electronic 4x4 pieces of getHiso_sp, rounded as the reference rounds them.
+struct RefElectron {
+  double2 diag[4];  // Hel_diag: Zeeman + (2J + 2i dk + D33) S1zS2z - i kbar/2
+  double2 flip_ab;  // (J + i dk + D11/2) on S1+S2-
+  double2 flip_ba;  // (J + i dk + D22/2) on S1-S2+
+};
+// Full 4x4 electronic Hamiltonian of the general builder.
+struct GenElectron {
+  double2 H[4][4];
+};
+
+struct HostSystem {
+  int64_t Z = 1, N = 4;
+  std::vector<NucInfo> nuc;
+  RefElectron ref;
+  GenElectron gen;
+};
+
+// Builds the host-side description; returns SPC_OK or an error code with
+// the message set.
+int make_host_system(const spc_system* sys, int mode, HostSystem& out);
+
+// Kernel classes timed by the optional profiler.
+enum ProfKind {
+  PK_SPMM = 0,
+  PK_DOT,
+  PK_AXPY_DOT,
+  PK_AXPY_NORM,
+  PK_SCALE,
+  PK_EXPM,
+  PK_PROJ,
+  PK_PROJ_REDUCE,
+  PK_DTLOOP,
+  PK_PSI,
+  PK_SETUP,
+  PROF_KINDS
+};
+const char* prof_kind_name(int k);
+
+// CUDA-event timing of each launch on its own stream, with the algorithmic
+// FLOPs and bytes of the launch, accumulated per kernel class.
+struct Prof {
+  struct Pending {
+    int kind;
+    double flops, bytes;
+    int ev;
+  };
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  int used = 0;
+  std::vector<Pending> pend;
+  double ms[PROF_KINDS] = {}, flops[PROF_KINDS] = {}, bytes[PROF_KINDS] = {};
+  int64_t launches[PROF_KINDS] = {};
+  int begin(cudaStream_t st);
+  void end(cudaStream_t st, int idx, int kind, double f, double b);
+  void collect();  // after a stream synchronize
+  void reset();
+  ~Prof();
+};
+
+struct Handle {
+  Prof prof;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  // Hamiltonian (CSR, 0-based)
+  int n = 0;
+  int64_t nnz = 0;
+  int* d_rowptr = nullptr;
+  int* d_col = nullptr;
+  double2* d_val = nullptr;
+  size_t cap_rowptr = 0, cap_h = 0;
+  // propagation workspace (grow-only)
+  struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+  };
+  Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
+      map, obs, out, zk, err, nbuild;
+  std::vector<void*> host_pinned;
+  spc_stats stats{};
+  int64_t launches = 0;
+  int sm_count = 148;
+  size_t smem_optin = 48 * 1024;
+
+  int ensure_rowptr(size_t count);
+  int ensure_h_entries(size_t count);
+  int ensure(Buf& b, size_t bytes);
+  void count_launch(int k = 1) { launches += k; }
+  ~Handle();
+};
+
+int set_error(int code, const char* fmt, ...);
+int build_h_device(Handle* h, const HostSystem& hs, int mode);
+int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev,
+              int M, double dt, double t_end, int m, double tol, double* out_dev, int T);
+int num_time_points(double dt, double t_end);
+
+}  // namespace spc

@@ -1,0 +1,262 @@
+"""Host-side mirror of module `dynamics` (src/qm_dynamics.f90) over the C ABI.
+
+`TraceSampler` owns one libspinchem_gpu handle (one GPU, one stream). The
+module-level functions keep the reference's names and argument meaning:
+
+  trace_sampling_para(sys, sim, out=None)   src/qm_dynamics.f90:257-384
+  trace_sampling(sys, sim, out=None)        src/qm_dynamics.f90:139-255
+  exact_dynamics(sys, sim, out=None)        src/qm_dynamics.f90:24-137
+
+`sys.e1.w` / `sys.e2.w` carry the Larmor frequency w = -B that the driver
+sets per field (app/main.f90:53-54), exactly as in the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native as nat
+from .observables import Observables
+from .spinsys import SimParam, SpinchemError, SysParam
+
+INIT_STATES = {"singlet": 0, "T0": 1, "Tp": 2, "Tm": 3}
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def make_system(sys: SysParam, B) -> tuple:
+    """Fill an spc_system from a SysParam and a field (scalar along z, or a
+    3-vector). Returns (struct, keepalive arrays)."""
+    Bv = np.array([0.0, 0.0, float(B)]) if np.isscalar(B) else np.asarray(B, np.float64).reshape(3)
+    keep = []
+
+    def arr(x, dt):
+        a = np.ascontiguousarray(x, dtype=dt)
+        if a.size == 0:
+            a = np.zeros(1, dtype=dt)
+        keep.append(a)
+        return a
+
+    s = nat.spc_system()
+    s.n_nuc1 = len(sys.e1.g_I)
+    s.n_nuc2 = len(sys.e2.g_I)
+    m1 = arr(sys.e1.g_I, np.int32)
+    m2 = arr(sys.e2.g_I, np.int32)
+    # 9 values per nucleus in column-major (input.ini) order
+    A1 = arr([a.reshape(3, 3).T.reshape(9) for a in sys.e1.A] or np.zeros(9), np.float64)
+    A2 = arr([a.reshape(3, 3).T.reshape(9) for a in sys.e2.A] or np.zeros(9), np.float64)
+    s.mult1 = m1.ctypes.data_as(C.POINTER(C.c_int))
+    s.mult2 = m2.ctypes.data_as(C.POINTER(C.c_int))
+    s.A1 = A1.ctypes.data_as(C.POINTER(C.c_double))
+    s.A2 = A2.ctypes.data_as(C.POINTER(C.c_double))
+    if sys.e1.gamma_I is not None:
+        g1 = arr(sys.e1.gamma_I, np.float64)
+        s.gamma1 = g1.ctypes.data_as(C.POINTER(C.c_double))
+    if sys.e2.gamma_I is not None:
+        g2 = arr(sys.e2.gamma_I, np.float64)
+        s.gamma2 = g2.ctypes.data_as(C.POINTER(C.c_double))
+    for i in range(3):
+        s.B[i] = float(Bv[i])
+    s.J = float(sys.J)
+    Dc = np.asarray(sys.D, np.float64).reshape(3, 3).T.reshape(9)
+    for i in range(9):
+        s.D[i] = float(Dc[i])
+    s.kS = float(sys.kS)
+    s.kT = float(sys.kT)
+    return s, keep
+
+
+def num_time_points(dt: float, t_end: float) -> int:
+    return nat.lib().spc_num_time_points(float(dt), float(t_end))
+
+
+def init_el_state(which: str):
+    """init_el_state (src/qm_dynamics.f90:386-414): (theta[4] complex, init_pop[4])."""
+    if which not in INIT_STATES:
+        raise SpinchemError("Error: Invalid initial radical pair state entered.")
+    th = np.zeros(8)
+    pop = np.zeros(4)
+    nat.check(nat.lib().spc_init_el_state(INIT_STATES[which], _dptr(th), _dptr(pop)))
+    return th.view(np.complex128), pop
+
+
+def seeded_samples(seed: Sequence[int], Z: int, M: int, serial: bool = False) -> np.ndarray:
+    """Sample vectors as the reference draws them (M x Z complex)."""
+    out = np.zeros(2 * Z * M)
+    s0 = int(seed[0])
+    s1 = int(seed[1])
+    s0 = s0 - 2**64 if s0 >= 2**63 else s0
+    s1 = s1 - 2**64 if s1 >= 2**63 else s1
+    nat.check(nat.lib().spc_seeded_samples(s0, s1, Z, M, 1 if serial else 0, _dptr(out)))
+    return out.view(np.complex128).reshape(M, Z)
+
+
+class TraceSampler:
+    """One GPU handle: a device Hamiltonian plus the batched propagator."""
+
+    def __init__(self, device: int = 0):
+        L = nat.lib()
+        h = C.c_void_p()
+        nat.check(L.spc_create(int(device), C.byref(h)))
+        self._h = h
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            nat.lib().spc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int) -> None:
+        nat.check(nat.lib().spc_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    # ---- Hamiltonian ----
+    def build_h(self, sys: SysParam, B, mode: str = "reference") -> tuple:
+        """getHiso_sp + coo_to_csr on the device (mode 'reference'), or the
+        anisotropic general builder (mode 'general'). Returns (n, nnz)."""
+        m = {"reference": nat.SPC_H_REFERENCE, "general": nat.SPC_H_GENERAL}[mode]
+        s, keep = make_system(sys, B)
+        nat.check(nat.lib().spc_build_h(self._h, C.byref(s), m))
+        return self.h_size()
+
+    def set_h(self, rowptr, col, val, index_base: int = 0) -> None:
+        rp = np.ascontiguousarray(rowptr, np.int32)
+        cl = np.ascontiguousarray(col, np.int32)
+        vv = np.ascontiguousarray(np.asarray(val, np.complex128)).view(np.float64)
+        csr = nat.spc_csr(len(rp) - 1, len(cl), rp.ctypes.data_as(C.POINTER(C.c_int32)),
+                          cl.ctypes.data_as(C.POINTER(C.c_int32)),
+                          vv.ctypes.data_as(C.POINTER(C.c_double)), index_base)
+        nat.check(nat.lib().spc_set_h(self._h, C.byref(csr)))
+
+    def h_size(self) -> tuple:
+        n = C.c_int32()
+        nnz = C.c_int64()
+        nat.check(nat.lib().spc_h_size(self._h, C.byref(n), C.byref(nnz)))
+        return n.value, nnz.value
+
+    def get_h(self):
+        n, nnz = self.h_size()
+        rp = np.zeros(n + 1, np.int32)
+        cl = np.zeros(max(nnz, 1), np.int32)
+        vv = np.zeros(2 * max(nnz, 1))
+        nat.check(nat.lib().spc_get_h(self._h, _dptr(rp), _dptr(cl), _dptr(vv)))
+        return rp, cl[:nnz], vv.view(np.complex128)[:nnz]
+
+    # ---- propagation ----
+    def trace_sampling(self, zkets: np.ndarray, dt: float, t_end: float, m: int, tol: float,
+                       init_state: str = "singlet") -> Observables:
+        """Propagate the M x Z sample vectors (host memory) and return the
+        sample-averaged populations."""
+        zk = np.ascontiguousarray(np.asarray(zkets, np.complex128))
+        if zk.ndim != 2:
+            raise ValueError("zkets must be M x Z")
+        M = zk.shape[0]
+        th, pop = init_el_state(init_state)
+        th = np.ascontiguousarray(th).view(np.float64)
+        T = num_time_points(dt, t_end)
+        outs = [np.zeros(T) for _ in range(4)]
+        nat.check(nat.lib().spc_trace_sampling(
+            self._h, _dptr(th), _dptr(pop), _dptr(zk.view(np.float64)), M, float(dt), float(t_end),
+            int(m), float(tol), *(_dptr(o) for o in outs), T))
+        return Observables(*outs)
+
+    def trace_sampling_device(self, zkets_ptr: int, M: int, dt: float, t_end: float, m: int,
+                              tol: float, out_ptr: int, init_state: str = "singlet") -> None:
+        """Same on device-resident buffers: zkets_ptr -> M x Z complex128,
+        out_ptr -> 4*T float64 (P_S | P_T0 | P_Tp | P_Tm)."""
+        th, pop = init_el_state(init_state)
+        th = np.ascontiguousarray(th).view(np.float64)
+        T = num_time_points(dt, t_end)
+        nat.check(nat.lib().spc_trace_sampling_device(
+            self._h, _dptr(th), _dptr(pop), C.c_void_p(zkets_ptr), int(M), float(dt),
+            float(t_end), int(m), float(tol), C.c_void_p(out_ptr), T))
+
+    def stats(self) -> dict:
+        s = nat.spc_stats()
+        nat.check(nat.lib().spc_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in nat.spc_stats._fields_}
+
+
+# ---------------------------------------------------------------------------
+# reference-named drivers
+_DEFAULT: Optional[TraceSampler] = None
+
+
+def default_sampler() -> TraceSampler:
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = TraceSampler(0)
+    return _DEFAULT
+
+
+def _field(sys: SysParam) -> float:
+    # main sets sys%e1%w = sys%e2%w = -B (app/main.f90:53-54)
+    return -float(sys.e1.w)
+
+
+def _require_isotropic(sys: SysParam) -> None:
+    if not (sys.e1.isotropic and sys.e2.isotropic):
+        raise SpinchemError("Anisotropic Hamiltoninans have not been implemented yet")
+
+
+def trace_sampling_para(sys: SysParam, sim: SimParam, out: Optional[str] = None,
+                        sampler: Optional[TraceSampler] = None) -> Observables:
+    """trace_sampling_para (src/qm_dynamics.f90:257-384): H from getHiso_sp on
+    the device, per-sample seeds drawn from sim.seed, the batched Krylov
+    propagation, the sample average; writes the output files when `out` is
+    given (without yields, as the reference)."""
+    _require_isotropic(sys)
+    sp = sampler or default_sampler()
+    sp.build_h(sys, _field(sys), "reference")
+    zk = seeded_samples(sim.seed, sys.Z, sim.N_samples)
+    res = sp.trace_sampling(zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol, sim.init_state)
+    if out is not None:
+        res.output(out)
+    return res
+
+
+def trace_sampling(sys: SysParam, sim: SimParam, out: Optional[str] = None,
+                   sampler: Optional[TraceSampler] = None) -> Observables:
+    """trace_sampling (serial variant, src/qm_dynamics.f90:139-255): one RNG
+    stream across samples; propagation as trace_sampling_para."""
+    _require_isotropic(sys)
+    sp = sampler or default_sampler()
+    sp.build_h(sys, _field(sys), "reference")
+    zk = seeded_samples(sim.seed, sys.Z, sim.N_samples, serial=True)
+    res = sp.trace_sampling(zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol, sim.init_state)
+    if out is not None:
+        res.output(out)
+    return res
+
+
+def exact_dynamics(sys: SysParam, sim: SimParam, out: Optional[str] = None,
+                   sampler: Optional[TraceSampler] = None) -> Observables:
+    """exact_dynamics (src/qm_dynamics.f90:24-137): the same propagator over
+    all Z nuclear basis states, averaged with weight 1/Z."""
+    _require_isotropic(sys)
+    sp = sampler or default_sampler()
+    sp.build_h(sys, _field(sys), "reference")
+    zk = np.eye(sys.Z, dtype=np.complex128)
+    res = sp.trace_sampling(zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol, sim.init_state)
+    if out is not None:
+        res.output(out)
+    return res
