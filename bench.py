@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--window-ns", type=float, default=100.0)
     p.add_argument("--samples", type=int, default=512)
     p.add_argument("--krylov", type=int, default=30)
+    p.add_argument("--method", default="auto", choices=["auto", "mgs", "lanczos"],
+                   help="Krylov orthogonalisation: auto = Lanczos with MGS fallback when kS == kT")
     p.add_argument("--cpu-samples", type=int, default=0, help="CPU sample size (0 = 2 x cores)")
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--no-e2e", action="store_true")
@@ -171,6 +173,7 @@ def run_ours(args, rank, world, local_rank):
     T = num_time_points(sim.dt, sim.t_end)
     steps_per_sample = int(round(sim.t_end / sim.dt))
     sampler = TraceSampler(local_rank)
+    sampler.set_krylov(args.method)
     stream = torch.cuda.current_stream()
     sampler.set_stream(stream.cuda_stream)
     zk_host = W.random_phase_samples(sysp.Z, M, seed=7 + rank)
@@ -193,6 +196,7 @@ def run_ours(args, rank, world, local_rank):
     nat.check(nat.lib().spc_set_profiling(sampler.handle, 1))
     launches = 0
     builds = 0
+    fallbacks = 0
     barrier()
     torch.cuda.synchronize()
     with Clocks(local_rank) as clk:
@@ -204,6 +208,7 @@ def run_ours(args, rank, world, local_rank):
             st = sampler.stats()
             launches += st["kernel_launches"] + 4  # + the Hamiltonian build kernels
             builds += st["krylov_builds"]
+            fallbacks += st["lanczos_fallbacks"]
         e1.record(stream)
         torch.cuda.synchronize()
     barrier()
@@ -246,7 +251,7 @@ def run_ours(args, rank, world, local_rank):
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
     return dict(ms=ms, value=value, e2e=e2e, prof=prof, clocks=clk.summary(), launches=launches,
-                builds=builds, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
+                builds=builds, fallbacks=fallbacks, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
                 sysp=sysp, B=B, sim=sim)
 
 
@@ -304,6 +309,8 @@ def main():
                                     f"{args.window_ns:g} ns",
                         "samples": r["M"], "dt_steps_per_sample": r["steps_per_sample"],
                         "krylov_builds_per_step": r["builds"] / args.steps,
+                        "krylov_method": args.method,
+                        "lanczos_fallbacks_per_step": r["fallbacks"] / args.steps,
                         "l2": "inputs larger than L2 (Krylov basis 13.6 GB per build)",
                         "parallelism": f"replicas x{args.gpus}"},
                 e2e=r["e2e"], gpu_launches=int(r["launches"]), clocks=r["clocks"],

@@ -77,9 +77,18 @@ typedef struct {
                               (B[0], B[1] must be 0), axial D; CSR rows in the reference's order */
 #define SPC_H_GENERAL 1    /* anisotropic S.A.I, field vector, full D tensor; columns ascending */
 
+/* Krylov methods for spc_set_krylov. */
+#define SPC_KRYLOV_MGS 0      /* Arnoldi with full modified Gram-Schmidt, as get_krylov
+                                 (src/qm_dynamics.f90:432-467); the default */
+#define SPC_KRYLOV_LANCZOS 1  /* three-term recurrence; only for H_eff = Hermitian - i*kappa
+                                 (kS == kT); a basis whose Gram matrix drifts from the identity
+                                 by more than 1e-12 is rebuilt with full MGS */
+#define SPC_KRYLOV_AUTO 2     /* Lanczos when H_eff is Hermitian - i*kappa, else MGS */
+
 /* Counters of the last propagation call. */
 typedef struct {
   int64_t krylov_builds;   /* sum over samples of Krylov subspaces built */
+  int64_t lanczos_fallbacks; /* Lanczos bases rebuilt with full MGS */
   int64_t rounds;          /* batched build rounds (max builds of any sample) */
   int64_t sample_steps;    /* sum over samples of dt steps taken */
   int64_t kernel_launches; /* kernels launched by the library during the call */
@@ -153,6 +162,12 @@ int spc_trace_sampling(spc_handle* h, const double* theta, const double* init_po
 int spc_trace_sampling_device(spc_handle* h, const double* theta, const double* init_pop,
                               const double* zkets_dev, int M, double dt, double t_end, int m,
                               double tol, double* out_dev, int T);
+
+/* Select the Krylov orthogonalisation (SPC_KRYLOV_*). In exact arithmetic
+ * Lanczos and MGS give the same basis when H_eff = Hermitian - i*kappa; the
+ * Lanczos path skips the O(m^2 n) re-orthogonalisation and verifies the
+ * basis through the projector Grams (their sum is Q^H Q). */
+int spc_set_krylov(spc_handle* h, int method);
 
 /* Counters of the last propagation call on this handle. */
 int spc_get_stats(const spc_handle* h, spc_stats* out);

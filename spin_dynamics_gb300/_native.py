@@ -19,6 +19,9 @@ SPC_ERR_NUMERIC = 5
 SPC_ERR_STATE = 6
 SPC_H_REFERENCE = 0
 SPC_H_GENERAL = 1
+SPC_KRYLOV_MGS = 0
+SPC_KRYLOV_LANCZOS = 1
+SPC_KRYLOV_AUTO = 2
 
 
 class SpcError(RuntimeError):
@@ -45,7 +48,8 @@ class spc_csr(C.Structure):
 
 
 class spc_stats(C.Structure):
-    _fields_ = [("krylov_builds", C.c_int64), ("rounds", C.c_int64), ("sample_steps", C.c_int64),
+    _fields_ = [("krylov_builds", C.c_int64), ("lanczos_fallbacks", C.c_int64),
+                ("rounds", C.c_int64), ("sample_steps", C.c_int64),
                 ("kernel_launches", C.c_int64), ("seconds", C.c_double)]
 
 
@@ -69,6 +73,7 @@ SIGNATURES = {
     "spc_seeded_samples": (_I, [C.c_int64, C.c_int64, _I, _I, _I, _P]),
     "spc_init_el_state": (_I, [_I, _P, _P]),
     "spc_kinetics": (_I, [_I, _P, _P, _P, _P, _D, _D, _D, _P, _P, _P]),
+    "spc_set_krylov": (_I, [_P, _I]),
     "spc_set_profiling": (_I, [_P, _I]),
     "spc_get_profile": (_I, [_P, _I, C.POINTER(_D), C.POINTER(C.c_int64), C.POINTER(_D),
                              C.POINTER(_D)]),

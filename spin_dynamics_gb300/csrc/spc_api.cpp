@@ -1,6 +1,7 @@
 // extern "C" entry points of libspinchem_gpu (declared in include/spinchem_gpu.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -24,7 +25,68 @@ void clear_error();
       return spc::set_error(SPC_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));    \
   } while (0)
 
+// True when H = A - i*kappa*1 with A exactly Hermitian (duplicates summed):
+// every diagonal entry has the same imaginary part and H(c,r) = conj(H(r,c))
+// for r != c, bit for bit.
+static bool is_hermitian_plus_shift(int n, const std::vector<int>& rp, const std::vector<int>& cl,
+                                    const double* val) {
+  std::vector<std::pair<int64_t, std::pair<double, double>>> e;
+  e.reserve(rp[n]);
+  for (int r = 0; r < n; ++r)
+    for (int k = rp[r]; k < rp[r + 1]; ++k)
+      e.push_back({(int64_t)r * n + cl[k], {val[2 * (size_t)k], val[2 * (size_t)k + 1]}});
+  std::sort(e.begin(), e.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  std::vector<std::pair<int64_t, std::pair<double, double>>> u;
+  for (const auto& x : e) {
+    if (!u.empty() && u.back().first == x.first) {
+      u.back().second.first += x.second.first;
+      u.back().second.second += x.second.second;
+    } else {
+      u.push_back(x);
+    }
+  }
+  bool have_shift = false;
+  double shift = 0.0;
+  for (const auto& x : u) {
+    const int r = (int)(x.first / n), c = (int)(x.first % n);
+    if (r == c) {
+      if (!have_shift) {
+        shift = x.second.second;
+        have_shift = true;
+      } else if (x.second.second != shift) {
+        return false;
+      }
+      continue;
+    }
+    const int64_t key = (int64_t)c * n + r;
+    auto it = std::lower_bound(u.begin(), u.end(), key,
+                               [](const auto& a, int64_t k) { return a.first < k; });
+    const bool zero = x.second.first == 0.0 && x.second.second == 0.0;
+    if (it == u.end() || it->first != key) {
+      if (!zero) return false;
+      continue;
+    }
+    if (it->second.first != x.second.first || it->second.second != -x.second.second) return false;
+  }
+  // rows without a stored diagonal have imaginary part 0 there
+  for (int r = 0; r < n; ++r) {
+    const int64_t key = (int64_t)r * n + r;
+    auto it = std::lower_bound(u.begin(), u.end(), key,
+                               [](const auto& a, int64_t k) { return a.first < k; });
+    if ((it == u.end() || it->first != key) && have_shift && shift != 0.0) return false;
+  }
+  return true;
+}
+
 extern "C" {
+
+int spc_set_krylov(spc_handle* h, int method) {
+  if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
+  if (method < SPC_KRYLOV_MGS || method > SPC_KRYLOV_AUTO)
+    return spc::set_error(SPC_ERR_ARG, "unknown Krylov method %d", method);
+  h->h.krylov_method = method;
+  return SPC_OK;
+}
 
 int spc_create(int device, spc_handle** out) {
   if (!out) return spc::set_error(SPC_ERR_ARG, "null output pointer");
@@ -106,6 +168,7 @@ int spc_set_h(spc_handle* h, const spc_csr* H) {
   }
   h->h.n = n;
   h->h.nnz = nnz;
+  h->h.herm_shift = is_hermitian_plus_shift(n, rp, cl, H->val);
   return SPC_OK;
 }
 
@@ -156,6 +219,8 @@ int spc_trace_sampling_device(spc_handle* h, const double* theta, const double* 
     return spc::set_error(SPC_ERR_ARG, "T must be spc_num_time_points(dt, t_end) = %d",
                           spc::num_time_points(dt, t_end));
   CKR(cudaSetDevice(h->h.device));
+  if (h->h.krylov_method == SPC_KRYLOV_LANCZOS && !h->h.herm_shift)
+    return spc::set_error(SPC_ERR_ARG, "Lanczos needs H_eff = Hermitian - i*kappa (kS == kT)");
   return spc::propagate(&h->h, theta, init_pop, zkets_dev, M, dt, t_end, m, tol, out_dev, T);
 }
 
@@ -169,6 +234,8 @@ int spc_trace_sampling(spc_handle* h, const double* theta, const double* init_po
     return spc::set_error(SPC_ERR_ARG, "T must be spc_num_time_points(dt, t_end) = %d",
                           spc::num_time_points(dt, t_end));
   CKR(cudaSetDevice(h->h.device));
+  if (h->h.krylov_method == SPC_KRYLOV_LANCZOS && !h->h.herm_shift)
+    return spc::set_error(SPC_ERR_ARG, "Lanczos needs H_eff = Hermitian - i*kappa (kS == kT)");
   const int64_t Z = h->h.n / 4;
   spc::Handle& H = h->h;
   if (H.ensure(H.zk, sizeof(double) * 2 * Z * M) || H.ensure(H.out, sizeof(double) * 4 * T))

@@ -309,6 +309,7 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode) {
                      cudaGetErrorString(cudaGetLastError()));
     h->n = (int)N;
     h->nnz = nnz;
+    h->herm_shift = hs.herm_shift;
   }
   cudaFree(d_nuc);
   cudaFree(d_cnt);

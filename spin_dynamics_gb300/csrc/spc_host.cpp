@@ -66,7 +66,7 @@ int Handle::ensure_h_entries(size_t count) {
 }
 Handle::~Handle() {
   Buf* all[] = {&psi, &Q,  &P,    &partial, &counters, &coef, &rbeta, &Ahess, &Aexp, &proj, &projpart,
-                &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild};
+                &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag};
   for (Buf* b : all)
     if (b->p) cudaFree(b->p);
   if (d_rowptr) cudaFree(d_rowptr);
@@ -157,6 +157,10 @@ int make_host_system(const spc_system* sys, int mode, HostSystem& hs) {
   const double kS = sys->kS, kT = sys->kT, J = sys->J;
   const double* D = sys->D;  // column-major
   const double k_bar = (kS + 3.0 * kT) / 4.0, dk = (kS - kT) / 4.0;
+  // With kS == kT the Haberkorn term is the scalar -i*kbar/2 and H_eff is a
+  // Hermitian matrix shifted by it (the reference builder additionally needs
+  // D11 == D22 exactly for its two flip-flop entries to be equal).
+  hs.herm_shift = (kS == kT) && (mode == SPC_H_GENERAL || D[0] == D[4]);
   if (mode == SPC_H_REFERENCE) {
     if (sys->B[0] != 0.0 || sys->B[1] != 0.0)
       return set_error(SPC_ERR_ARG, "the reference Hamiltonian takes a field along z only");

@@ -38,6 +38,7 @@ struct HostSystem {
   std::vector<NucInfo> nuc;
   RefElectron ref;
   GenElectron gen;
+  bool herm_shift = false;  // kS == kT: H_eff is Hermitian minus i*kbar/2
 };
 
 // Builds the host-side description; returns SPC_OK or an error code with
@@ -100,7 +101,14 @@ struct Handle {
     size_t bytes = 0;
   };
   Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
-      map, obs, out, zk, err, nbuild;
+      map, obs, out, zk, err, nbuild, flag;
+  // Krylov method: 0 full MGS (the reference's get_krylov), 1 Lanczos, 2 auto
+  int krylov_method = 0;
+  // H_eff = (Hermitian) - i*kappa*1 for the current Hamiltonian: Lanczos applies
+  bool herm_shift = false;
+  bool lanczos_active() const {
+    return herm_shift && (krylov_method == 1 || krylov_method == 2);
+  }
   std::vector<void*> host_pinned;
   spc_stats stats{};
   int64_t launches = 0;

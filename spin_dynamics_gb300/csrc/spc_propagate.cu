@@ -36,6 +36,7 @@ enum PassKind { PASS_NORM_GATHER = 0, PASS_DOT = 1, PASS_AXPY_DOT = 2, PASS_AXPY
 struct PassArgs {
   int64_t N;
   int ld, Ma, rpb, m, col_i, row_j;
+  int lanczos;        // AXPY_NORM also seeds the next Lanczos coefficient
   const double2* X;   // NORM_GATHER: psi (ldp columns, gathered through map); DOT: Q_0
   double2* P;         // Arnoldi work vector
   const double2* Qj;  // AXPY_*: the basis vector removed from P
@@ -67,6 +68,12 @@ __device__ __forceinline__ void pass_finalize(const PassArgs& a, int w, double2 
     a.Ahess[(size_t)w * mm + a.row_j + (size_t)a.col_i * a.m] = make_double2(b, 0.0);
     // exact breakdown (p == 0): the next basis vector is 0 instead of 0/0
     a.rbeta[w] = b > 0.0 ? 1.0 / b : 0.0;
+    if (a.lanczos) {
+      // Hermitian tridiagonal: A(i, i+1) = beta_i, the coefficient of Q_i
+      // in the next step's three-term recurrence
+      a.Ahess[(size_t)w * mm + a.col_i + (size_t)a.row_j * a.m] = make_double2(b, 0.0);
+      a.coef[w] = make_double2(b, 0.0);
+    }
   }
 }
 
@@ -445,18 +452,47 @@ __global__ void k_proj_reduce(int Ma, int m, int ncombo, int nsplit,
   if (i != j) P[j + i * m] = make_double2(s.x, -s.y);
 }
 
+// Orthonormality of a Lanczos basis from the projector Grams:
+// max_ij |(Tp + S + T0 + Tm)_ij - delta_ij| > tol flags the sample.
+#define ORTHO_TOL 1e-12
+__global__ void __launch_bounds__(128)
+    k_ortho_check(int m, int Ma, const double2* __restrict__ proj, double tol, int* __restrict__ flag) {
+  __shared__ double red[128];
+  const int w = blockIdx.x;
+  const size_t mm = (size_t)m * m;
+  const double2* P = proj + (size_t)w * 4 * mm;
+  double mx = 0.0;
+  for (int idx = threadIdx.x; idx < (int)mm; idx += blockDim.x) {
+    const double2 g = cadd(cadd(P[idx], P[mm + idx]), cadd(P[2 * mm + idx], P[3 * mm + idx]));
+    const double d = (idx % (m + 1) == 0) ? 1.0 : 0.0;
+    const double e = fmax(fabs(g.x - d), fabs(g.y));
+    mx = (e > mx || e != e) ? e : mx;  // NaN flags too
+  }
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = 64; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      const double v = red[threadIdx.x + o];
+      if (v > red[threadIdx.x] || v != v) red[threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) flag[w] = !(red[0] <= tol);
+}
+
 // ---------------------------------------------------------------------------
 // dt loop (src/qm_dynamics.f90:348-364), one warp per sample. Projector types
 // in `proj`: 0 Tp, 1 S, 2 T0, 3 Tm; obs slots per sample: 0 S, 1 T0, 2 Tp, 3 Tm.
 __global__ void __launch_bounds__(128)
-    k_dtloop(int m, int Ma, int T, const int* __restrict__ map, const double2* __restrict__ Aexp,
+    k_dtloop(int m, int Ma, int T, const int* __restrict__ map, const int* __restrict__ skip,
+             const double2* __restrict__ Aexp,
              const double2* __restrict__ proj, double2* __restrict__ cvec, double* __restrict__ tt,
              int* __restrict__ kk, int* __restrict__ done, double* __restrict__ obs, double dt,
              double t_end, double tol, long long* __restrict__ nsteps, int* __restrict__ err) {
   __shared__ double2 cs[4][SPC_MAX_M];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w = blockIdx.x * 4 + warp;
-  if (w >= Ma) return;
+  if (w >= Ma || skip[w]) return;
   const int s = map[w];
   const size_t mm = (size_t)m * m;
   const double2* E = Aexp + (size_t)w * mm;
@@ -524,7 +560,8 @@ __global__ void __launch_bounds__(128)
 
 // psi[:, map[w]] = Q c  (src/qm_dynamics.f90:365)
 __global__ void __launch_bounds__(256)
-    k_psi_update(int64_t N, int ld, int Ma, int rpb, int m, const int* __restrict__ map, int ldp,
+    k_psi_update(int64_t N, int ld, int Ma, int rpb, int m, const int* __restrict__ map,
+                 const int* __restrict__ skip, int ldp,
                  const double2* __restrict__ Q, const double2* __restrict__ cvec,
                  double2* __restrict__ psi) {
   __shared__ double2 cs[SPC_MAX_M][SPC_LANES];
@@ -533,7 +570,7 @@ __global__ void __launch_bounds__(256)
   const bool act = w < Ma;
   for (int j = ty; j < m; j += SPC_WARPS) cs[j][tx] = act ? cvec[(size_t)w * m + j] : cz();
   __syncthreads();
-  if (!act) return;
+  if (!act || skip[w]) return;
   const int s = map[w];
   const size_t qstride = (size_t)N * ld;
   const int64_t r0 = (int64_t)blockIdx.y * rpb;
@@ -635,8 +672,9 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
       h->ensure(h->cvec, sizeof(double2) * m * ld) || h->ensure(h->tt, sizeof(double) * M) ||
       h->ensure(h->kk, sizeof(int) * M) || h->ensure(h->done, sizeof(int) * M) ||
       h->ensure(h->map, sizeof(int) * ld) || h->ensure(h->obs, sizeof(double) * 4 * (size_t)T * M) ||
-      h->ensure(h->err, 16))
+      h->ensure(h->err, 16) || h->ensure(h->flag, sizeof(int) * ld))
     return SPC_ERR_ALLOC;
+  int* d_flag = (int*)h->flag.p;
   double2* d_psi = (double2*)h->psi.p;
   double2* d_Q = (double2*)h->Q.p;
   double2* d_P = (double2*)h->P.p;
@@ -698,17 +736,25 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   std::vector<int> active;
   if (0.0 < t_end)
     for (int s = 0; s < M; ++s) active.push_back(s);
-  std::vector<int> done_h(M, 0);
-  int64_t builds = 0, rounds = 0;
+  std::vector<int> done_h(M, 0), flag_h(ld, 0);
+  int64_t builds = 0, rounds = 0, fallbacks = 0;
   const dim3 blk(SPC_LANES, SPC_WARPS);
-  while (!active.empty()) {
-    const int Ma = (int)active.size();
+  const bool use_lanczos = h->lanczos_active();
+
+  // One build round for the samples in `list`: Krylov basis (Lanczos or full
+  // MGS), expm, projectors; then the dt loop and psi = Q c for every sample
+  // whose basis passed the orthogonality check. Returns the samples that
+  // failed it (Lanczos only); their state is left untouched.
+  auto round = [&](const std::vector<int>& list, bool lanczos, std::vector<int>& failed) -> int {
+    failed.clear();
+    const int Ma = (int)list.size();
     const int tiles = (Ma + SPC_LANES - 1) / SPC_LANES;
     int nrb, rpb;
     geometry(N, tiles, h->sm_count, nrb, rpb);
     const dim3 grid(tiles, nrb);
-    CK(cudaMemcpyAsync(d_map, active.data(), sizeof(int) * Ma, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_map, list.data(), sizeof(int) * Ma, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(d_A, 0, sizeof(double2) * mm * Ma, st));
+    CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * ld, st));
     PassArgs a{};
     a.N = N;
     a.ld = ld;
@@ -724,6 +770,7 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
     a.partial = d_part;
     a.counters = d_cnt;
     a.P = d_P;
+    a.lanczos = lanczos ? 1 : 0;
     // c = ||psi|| e1 ; Q0 = psi/||psi||
     a.X = d_psi;
     const double elems = (double)N * Ma;
@@ -742,14 +789,23 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
       // algorithmic traffic: H once, X once, Y once
       h->prof.end(st, pe, PK_SPMM, 8.0 * (double)h->nnz * Ma,
                   20.0 * (double)h->nnz + 4.0 * (N + 1) + 32.0 * elems);
+      h->count_launch();
       a.col_i = i;
-      a.row_j = 0;
-      a.X = d_Q;
-      pe = h->prof.begin(st);
-      k_rowpass<PASS_DOT><<<grid, blk, 0, st>>>(a);
-      h->prof.end(st, pe, PK_DOT, 8.0 * elems, 32.0 * elems);
-      h->count_launch(2);
-      for (int j = 0; j < i; ++j) {
+      // MGS (get_krylov :453-456) projects p on Q_0..Q_i in order. Lanczos
+      // (H_eff Hermitian up to -i*kappa) needs only Q_{i-1} (coefficient
+      // beta_{i-1}, already in coef) and Q_i.
+      int j0 = 0;
+      if (lanczos && i > 0) {
+        j0 = i - 1;
+      } else {
+        a.row_j = 0;
+        a.X = d_Q;
+        pe = h->prof.begin(st);
+        k_rowpass<PASS_DOT><<<grid, blk, 0, st>>>(a);
+        h->prof.end(st, pe, PK_DOT, 8.0 * elems, 32.0 * elems);
+        h->count_launch();
+      }
+      for (int j = j0; j < i; ++j) {
         a.Qj = d_Q + (size_t)j * qs;
         a.Qn = d_Q + (size_t)(j + 1) * qs;
         a.row_j = j + 1;
@@ -790,23 +846,47 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
       k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(Ma, m, ncombo, nsplit, d_combos, d_ppart,
                                                              d_proj);
       h->prof.end(st, pe, PK_PROJ_REDUCE, 2.0 * tot * nsplit, 16.0 * tot * (nsplit + 1));
+      h->count_launch(3);
+    }
+    if (lanczos) {
+      // G = Q^H Q = Tp + S + T0 + Tm; a basis that drifted from orthonormal
+      // beyond ORTHO_TOL is rebuilt with full MGS
+      k_ortho_check<<<Ma, 128, 0, st>>>(m, Ma, d_proj, ORTHO_TOL, d_flag);
+      h->count_launch();
+      CK(cudaMemcpyAsync(flag_h.data(), d_flag, sizeof(int) * Ma, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int w = 0; w < Ma; ++w)
+        if (flag_h[w]) failed.push_back(list[w]);
     }
     pe = h->prof.begin(st);
-    k_dtloop<<<(Ma + 3) / 4, 128, 0, st>>>(m, Ma, T, d_map, d_E, d_proj, d_c, d_t, d_k, d_done, d_obs,
-                                           dt, t_end, tol, d_nsteps, d_err);
+    k_dtloop<<<(Ma + 3) / 4, 128, 0, st>>>(m, Ma, T, d_map, d_flag, d_E, d_proj, d_c, d_t, d_k, d_done,
+                                           d_obs, dt, t_end, tol, d_nsteps, d_err);
     h->prof.end(st, pe, PK_DTLOOP, 0.0, 0.0);
     pe = h->prof.begin(st);
-    k_psi_update<<<grid, blk, 0, st>>>(N, ld, Ma, rpb, m, d_map, ldp, d_Q, d_c, d_psi);
+    k_psi_update<<<grid, blk, 0, st>>>(N, ld, Ma, rpb, m, d_map, d_flag, ldp, d_Q, d_c, d_psi);
     h->prof.end(st, pe, PK_PSI, 8.0 * m * elems, 16.0 * (m + 1) * elems);
-    h->count_launch(5);
+    h->count_launch(2);
     CK(cudaGetLastError());
+    return SPC_OK;
+  };
+
+  std::vector<int> failed, failed2;
+  while (!active.empty()) {
+    int rc = round(active, use_lanczos, failed);
+    if (rc) return rc;
+    builds += (int64_t)active.size() - (int64_t)failed.size();
+    if (!failed.empty()) {
+      fallbacks += (int64_t)failed.size();
+      rc = round(failed, false, failed2);
+      if (rc) return rc;
+      builds += (int64_t)failed.size();
+    }
     CK(cudaMemcpyAsync(done_h.data(), d_done, sizeof(int) * M, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     h->prof.collect();
-    builds += Ma;
     rounds++;
     std::vector<int> next;
-    next.reserve(Ma);
+    next.reserve(active.size());
     for (int s : active)
       if (!done_h[s]) next.push_back(s);
     active.swap(next);
@@ -820,6 +900,7 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   long long nsteps = 0;
   std::memcpy(&nsteps, &err_h[2], 8);
   h->stats.krylov_builds = builds;
+  h->stats.lanczos_fallbacks = fallbacks;
   h->stats.rounds = rounds;
   h->stats.sample_steps = nsteps;
   h->stats.kernel_launches = h->launches - launches0;

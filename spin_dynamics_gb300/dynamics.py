@@ -129,6 +129,13 @@ class TraceSampler:
     def set_stream(self, stream_ptr: int) -> None:
         nat.check(nat.lib().spc_set_stream(self._h, C.c_void_p(stream_ptr)))
 
+    def set_krylov(self, method: str) -> None:
+        """'mgs' (full modified Gram-Schmidt, the reference's get_krylov),
+        'lanczos' (kS == kT only) or 'auto' (Lanczos when it applies)."""
+        code = {"mgs": nat.SPC_KRYLOV_MGS, "lanczos": nat.SPC_KRYLOV_LANCZOS,
+                "auto": nat.SPC_KRYLOV_AUTO}[method]
+        nat.check(nat.lib().spc_set_krylov(self._h, code))
+
     # ---- Hamiltonian ----
     def build_h(self, sys: SysParam, B, mode: str = "reference") -> tuple:
         """getHiso_sp + coo_to_csr on the device (mode 'reference'), or the
@@ -172,7 +179,8 @@ class TraceSampler:
         M = zk.shape[0]
         th, pop = init_el_state(init_state)
         th = np.ascontiguousarray(th).view(np.float64)
-        T = num_time_points(dt, t_end)
+        # an invalid dt gives T = -1; the C ABI reports the argument error
+        T = max(num_time_points(dt, t_end), 1)
         outs = [np.zeros(T) for _ in range(4)]
         nat.check(nat.lib().spc_trace_sampling(
             self._h, _dptr(th), _dptr(pop), _dptr(zk.view(np.float64)), M, float(dt), float(t_end),
