@@ -64,6 +64,8 @@ SIGNATURES = {
     "spc_set_stream": (_I, [_P, _P]),
     "spc_build_h": (_I, [_P, C.POINTER(spc_system), _I]),
     "spc_set_h": (_I, [_P, C.POINTER(spc_csr)]),
+    "spc_build_h_noalloc": (_I, [C.POINTER(spc_system), _I, _P, _P, _P, C.c_int64,
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_int64), _P]),
     "spc_h_size": (_I, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
     "spc_get_h": (_I, [_P, _P, _P, _P]),
     "spc_num_time_points": (_I, [_D, _D]),

@@ -318,3 +318,113 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode) {
 }
 
 }  // namespace spc
+
+// ===========================================================================
+// Allocation-free Hamiltonian build (spc_build_h_noalloc).
+//
+// For callers that must not allocate device memory themselves or through
+// the library: code running under a CUDA stream capture or inside a memory
+// pool whose budget is fixed up front, or hosts (Fortran programs, plugins)
+// that only hand over buffers they own. The caller passes the system and the
+// CSR output buffers; the per-row counts, the nucleus table and the nonzero
+// total live in the file-scope array below, which every GPU that loads the
+// library holds until the process exits (about 4.2 MB).
+//
+// Limits: at most SPC_NOALLOC_MAX_ROWS rows (Hilbert dimension) and
+// SPC_NOALLOC_MAX_NUC nuclei; larger systems are rejected with SPC_ERR_ARG.
+// Every call on a device shares the one array and it keeps the last call's
+// contents (counts and table are rewritten before use); calls that overlap
+// on the GPU (different streams, or different host threads on one device)
+// race on it and must be serialised by the caller.
+#include <mutex>
+
+#define SPC_NOALLOC_MAX_ROWS (1 << 20)
+#define SPC_NOALLOC_MAX_NUC 64
+#define SPC_NOALLOC_MAX_DEVICES 64
+
+namespace {
+struct NoAllocScratch {
+  int cnt[SPC_NOALLOC_MAX_ROWS];
+  spc::NucInfo nuc[SPC_NOALLOC_MAX_NUC];
+  long long total;
+};
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// Device address of g_noalloc_scratch for each device, looked up once per
+// device (with that device current) on the first call there.
+static void* g_noalloc_ptr[SPC_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_scratch(int device, NoAllocScratch** out) {
+  if (device < 0 || device >= SPC_NOALLOC_MAX_DEVICES)
+    return spc::set_error(SPC_ERR_ARG, "device %d above the supported range", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return spc::set_error(SPC_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed: %s",
+                            cudaGetErrorString(e));
+    g_noalloc_ptr[device] = p;
+  }
+  *out = (NoAllocScratch*)g_noalloc_ptr[device];
+  return SPC_OK;
+}
+
+extern "C" int spc_build_h_noalloc(const spc_system* sys, int mode, int32_t* rowptr_dev,
+                                   int32_t* col_dev, double* val_dev, int64_t cap_nnz,
+                                   int32_t* n_out, int64_t* nnz_out, void* stream) {
+  if (!rowptr_dev || !col_dev || !val_dev || !n_out || !nnz_out || cap_nnz < 0)
+    return spc::set_error(SPC_ERR_ARG, "spc_build_h_noalloc: null output or negative capacity");
+  spc::HostSystem hs;
+  int rc = spc::make_host_system(sys, mode, hs);
+  if (rc != SPC_OK) return rc;
+  if (hs.N > SPC_NOALLOC_MAX_ROWS)
+    return spc::set_error(SPC_ERR_ARG,
+                          "spc_build_h_noalloc: dimension %lld above the %d rows of its scratch",
+                          (long long)hs.N, SPC_NOALLOC_MAX_ROWS);
+  if ((int)hs.nuc.size() > SPC_NOALLOC_MAX_NUC)
+    return spc::set_error(SPC_ERR_ARG, "spc_build_h_noalloc: more than %d nuclei",
+                          SPC_NOALLOC_MAX_NUC);
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess)
+    return spc::set_error(SPC_ERR_CUDA, "cudaGetDevice failed");
+  NoAllocScratch* scr = nullptr;
+  rc = noalloc_scratch(device, &scr);
+  if (rc != SPC_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t N = hs.N, Z = hs.Z;
+  const int nn = (int)hs.nuc.size();
+  if (nn > 0 && cudaMemcpyAsync(scr->nuc, hs.nuc.data(), sizeof(spc::NucInfo) * nn,
+                                cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return spc::set_error(SPC_ERR_CUDA, "copy of the nucleus table failed");
+  const int threads = 256;
+  const int blocks = (int)((N + threads - 1) / threads);
+  if (mode == SPC_H_REFERENCE)
+    spc::k_ref_count<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, scr->cnt);
+  else
+    spc::k_gen_count<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, scr->cnt);
+  spc::k_scan_rows<<<1, 1024, 0, st>>>(scr->cnt, rowptr_dev, N, &scr->total);
+  long long nnz = 0;
+  cudaMemcpyAsync(&nnz, &scr->total, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess)
+    return spc::set_error(SPC_ERR_CUDA, "Hamiltonian count/scan failed: %s", cudaGetErrorString(e));
+  *n_out = (int32_t)N;
+  *nnz_out = nnz;
+  if (nnz > cap_nnz)
+    return spc::set_error(SPC_ERR_ARG, "spc_build_h_noalloc: %lld nonzeros exceed the capacity %lld",
+                          nnz, (long long)cap_nnz);
+  if (mode == SPC_H_REFERENCE)
+    spc::k_ref_fill<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, hs.ref, rowptr_dev, col_dev,
+                                                (double2*)val_dev);
+  else
+    spc::k_gen_fill<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, hs.gen, rowptr_dev, col_dev,
+                                                (double2*)val_dev);
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess)
+    return spc::set_error(SPC_ERR_CUDA, "Hamiltonian fill failed: %s", cudaGetErrorString(e));
+  return SPC_OK;
+}
