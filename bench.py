@@ -37,6 +37,13 @@ from spin_dynamics_gb300 import workloads as W  # noqa: E402
 
 METRIC = "sample-steps/s at dim 55296 (trace sampling, complex128, M=512, m=30)"
 
+# DRAM traffic per k_spmm launch (dram__bytes_read.sum + dram__bytes_write.sum)
+# from one ncu capture at 64 sample columns (profiles/k_spmm_dim55296_M64_full.md:
+# 180 MB = 33 MB of Hamiltonian + 147 MB that scales with the columns), scaled
+# to the launch's column count.
+SPMM_TRAFFIC_H = 33.2e6
+SPMM_TRAFFIC_PER_COLUMN = (180.1e6 - 33.2e6) / 64
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -49,7 +56,7 @@ def parse():
     p.add_argument("--krylov", type=int, default=30)
     p.add_argument("--method", default="auto", choices=["auto", "mgs", "lanczos"],
                    help="Krylov orthogonalisation: auto = Lanczos with MGS fallback when kS == kT")
-    p.add_argument("--cpu-samples", type=int, default=0, help="CPU sample size (0 = 2 x cores)")
+    p.add_argument("--cpu-samples", type=int, default=0, help="CPU sample size (0 = 12 x cores)")
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
@@ -88,7 +95,7 @@ def cpu_leg(args, sysp, B, sim, threads):
     e1, e2 = sysp.e1, sysp.e2
     rp, col, val = pyoracle.build_h_general(e1.g_I, e1.A, e1.gammas, e2.g_I, e2.A, e2.gammas, B,
                                             sysp.J, sysp.D, sysp.kS, sysp.kT)
-    ns = args.cpu_samples or 2 * threads
+    ns = args.cpu_samples or 12 * threads
     zk = W.random_phase_samples(sysp.Z, ns)
     t0 = time.perf_counter()
     r = pyoracle.trace_sampling(rp, col, val, zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol,
@@ -317,7 +324,10 @@ def main():
                 roofline={"kernel": dom, "bound": "hbm", "achieved": ach_gbs,
                           "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                           "frac": (ach_gbs / peaks["hbm_gbs"]) if ach_gbs else None,
-                          "traffic": None, "peak_source": peak_src,
+                          "traffic": (SPMM_TRAFFIC_H + SPMM_TRAFFIC_PER_COLUMN * r["M"])
+                          if dom == "spmm" else None,
+                          "algorithmic_bytes": (by / max(nl, 1)) if nl else None,
+                          "peak_source": peak_src,
                           "fp64": {"achieved_tflops": ach_tf, "peak_tflops": r["fp64_peak"] / 1e12,
                                    "frac": (ach_tf * 1e12 / r["fp64_peak"]) if ach_tf else None,
                                    "peak_source": "measured DFMA probe (spc_fp64_peak)"}},

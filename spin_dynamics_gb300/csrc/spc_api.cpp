@@ -169,7 +169,7 @@ int spc_set_h(spc_handle* h, const spc_csr* H) {
   h->h.n = n;
   h->h.nnz = nnz;
   h->h.herm_shift = is_hermitian_plus_shift(n, rp, cl, H->val);
-  return SPC_OK;
+  return spc::prepare_spmm_rows(&h->h);
 }
 
 int spc_h_size(const spc_handle* h, int32_t* n, int64_t* nnz) {

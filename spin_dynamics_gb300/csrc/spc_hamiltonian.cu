@@ -310,6 +310,7 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode) {
     h->n = (int)N;
     h->nnz = nnz;
     h->herm_shift = hs.herm_shift;
+    if (rc == SPC_OK) rc = prepare_spmm_rows(h);
   }
   cudaFree(d_nuc);
   cudaFree(d_cnt);

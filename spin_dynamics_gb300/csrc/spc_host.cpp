@@ -66,7 +66,7 @@ int Handle::ensure_h_entries(size_t count) {
 }
 Handle::~Handle() {
   Buf* all[] = {&psi, &Q,  &P,    &partial, &counters, &coef, &rbeta, &Ahess, &Aexp, &proj, &projpart,
-                &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag};
+                &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag, &xcol, &xval, &xsplit};
   for (Buf* b : all)
     if (b->p) cudaFree(b->p);
   if (d_rowptr) cudaFree(d_rowptr);

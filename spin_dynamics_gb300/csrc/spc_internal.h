@@ -101,7 +101,7 @@ struct Handle {
     size_t bytes = 0;
   };
   Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
-      map, obs, out, zk, err, nbuild, flag;
+      map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit;
   // Krylov method: 0 full MGS (the reference's get_krylov), 1 Lanczos, 2 auto
   int krylov_method = 0;
   // H_eff = (Hermitian) - i*kappa*1 for the current Hamiltonian: Lanczos applies
@@ -127,5 +127,7 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode);
 int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev,
               int M, double dt, double t_end, int m, double tol, double* out_dev, int T);
 int num_time_points(double dt, double t_end);
+// Execution order of H's rows for k_spmm (complex entries first).
+int prepare_spmm_rows(Handle* h);
 
 }  // namespace spc

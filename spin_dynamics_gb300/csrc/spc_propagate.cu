@@ -167,20 +167,25 @@ __global__ void __launch_bounds__(256)
 }
 
 // Y = H X for a tile of 32 sample columns; one warp per row at a time, the
-// row's (col, val) entries broadcast to all lanes.
+// row's (col, val) entries broadcast to all lanes. Rows are stored in the
+// execution order of k_split_rows: entries with a nonzero imaginary part
+// first (4 DFMA each), then real ones from split[r] on (2 DFMA each).
 __global__ void __launch_bounds__(256)
     k_spmm(int64_t N, int ld, int Ma, int rpb, const int* __restrict__ rowptr,
-           const int* __restrict__ col, const double2* __restrict__ val,
-           const double2* __restrict__ X, double2* __restrict__ Y) {
+           const int* __restrict__ split, const int* __restrict__ col,
+           const double2* __restrict__ val, const double2* __restrict__ X,
+           double2* __restrict__ Y) {
   const int w = blockIdx.x * SPC_LANES + threadIdx.x;
   const bool act = w < Ma;
-  const int64_t r0 = (int64_t)blockIdx.y * rpb;
-  const int64_t r1 = min(N, r0 + rpb);
-  for (int64_t r = r0 + threadIdx.y; r < r1; r += SPC_WARPS) {
-    const int k0 = __ldg(rowptr + r), k1 = __ldg(rowptr + r + 1);
+  (void)rpb;
+  // rows interleaved over the CTAs of a sample tile: balanced row lengths,
+  // and all CTAs sweep X together (L2 reuse of the Kronecker neighbours)
+  const int64_t stride = (int64_t)gridDim.y * SPC_WARPS;
+  for (int64_t r = (int64_t)blockIdx.y * SPC_WARPS + threadIdx.y; r < N; r += stride) {
+    const int k0 = __ldg(rowptr + r), ks = __ldg(split + r), k1 = __ldg(rowptr + r + 1);
     double2 a0 = cz(), a1 = cz();
     int k = k0;
-    for (; k + 1 < k1; k += 2) {
+    for (; k + 1 < ks; k += 2) {
       const int c0 = __ldg(col + k), c1 = __ldg(col + k + 1);
       const double2 v0 = __ldg(val + k), v1 = __ldg(val + k + 1);
       if (act) {
@@ -190,13 +195,74 @@ __global__ void __launch_bounds__(256)
         a1 = cfma(v1, x1, a1);
       }
     }
-    if (k < k1) {
+    if (k < ks) {
       const int c0 = __ldg(col + k);
       const double2 v0 = __ldg(val + k);
       if (act) a0 = cfma(v0, X[(size_t)c0 * ld + w], a0);
+      k++;
+    }
+    for (; k + 1 < k1; k += 2) {
+      const int c0 = __ldg(col + k), c1 = __ldg(col + k + 1);
+      const double v0 = __ldg(&val[k].x), v1 = __ldg(&val[k + 1].x);
+      if (act) {
+        const double2 x0 = X[(size_t)c0 * ld + w];
+        const double2 x1 = X[(size_t)c1 * ld + w];
+        a0.x = fma(v0, x0.x, a0.x);
+        a0.y = fma(v0, x0.y, a0.y);
+        a1.x = fma(v1, x1.x, a1.x);
+        a1.y = fma(v1, x1.y, a1.y);
+      }
+    }
+    if (k < k1) {
+      const int c0 = __ldg(col + k);
+      const double v0 = __ldg(&val[k].x);
+      if (act) {
+        const double2 x0 = X[(size_t)c0 * ld + w];
+        a0.x = fma(v0, x0.x, a0.x);
+        a0.y = fma(v0, x0.y, a0.y);
+      }
     }
     if (act) Y[(size_t)r * ld + w] = cadd(a0, a1);
   }
+}
+
+// Execution copy of a CSR for k_spmm: each row's entries reordered so that
+// those with a nonzero imaginary part come first (original order kept within
+// each class); split[r] is the index of the row's first real entry.
+__global__ void k_split_rows(int64_t N, const int* __restrict__ rowptr, const int* __restrict__ col,
+                             const double2* __restrict__ val, int* __restrict__ xcol,
+                             double2* __restrict__ xval, int* __restrict__ split) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const int k0 = rowptr[r], k1 = rowptr[r + 1];
+  int o = k0;
+  for (int k = k0; k < k1; ++k)
+    if (val[k].y != 0.0) {
+      xcol[o] = col[k];
+      xval[o] = val[k];
+      o++;
+    }
+  split[r] = o;
+  for (int k = k0; k < k1; ++k)
+    if (val[k].y == 0.0) {
+      xcol[o] = col[k];
+      xval[o] = val[k];
+      o++;
+    }
+}
+
+int prepare_spmm_rows(Handle* h) {
+  const int64_t N = h->n, nnz = h->nnz;
+  if (h->ensure(h->xcol, sizeof(int) * (nnz > 0 ? nnz : 1)) ||
+      h->ensure(h->xval, sizeof(double2) * (nnz > 0 ? nnz : 1)) || h->ensure(h->xsplit, sizeof(int) * N))
+    return SPC_ERR_ALLOC;
+  k_split_rows<<<(int)((N + 255) / 256), 256, 0, h->stream>>>(
+      N, h->d_rowptr, h->d_col, h->d_val, (int*)h->xcol.p, (double2*)h->xval.p, (int*)h->xsplit.p);
+  h->count_launch();
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess)
+    return set_error(SPC_ERR_CUDA, "row split of the Hamiltonian failed: %s", cudaGetErrorString(e));
+  return SPC_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -626,11 +692,12 @@ __global__ void k_average(int M, int T, const double* __restrict__ obs, double* 
 }
 
 // ---------------------------------------------------------------------------
-static void geometry(int64_t N, int tiles, int sm, int& nrb, int& rpb) {
-  const int64_t target = (int64_t)sm * 8;
-  int64_t want = (target + tiles - 1) / tiles;
+// Row blocks per sample tile so that the grid fills one wave of resident
+// CTAs (tiles x nrb <= resident), with at least 32 rows per block.
+static void geometry(int64_t N, int tiles, int resident, int& nrb, int& rpb) {
+  int64_t want = std::max<int64_t>(1, resident / tiles);
   const int64_t maxb = std::max<int64_t>(1, (N + 31) / 32);
-  want = std::min(std::max<int64_t>(want, 1), maxb);
+  want = std::min(want, maxb);
   rpb = (int)((N + want - 1) / want);
   nrb = (int)((N + rpb - 1) / rpb);
 }
@@ -656,12 +723,12 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   const int ld = ldp;
   const size_t mm = (size_t)m * m;
   const int tiles_max = ld / SPC_LANES;
-  const int64_t pmax = std::min<int64_t>(std::max<int64_t>(1, (N + 31) / 32), (int64_t)h->sm_count * 8);
+  const int64_t pmax = std::min<int64_t>(std::max<int64_t>(1, (N + 31) / 32), (int64_t)h->sm_count * 32);
   const int ncombo = 4 * m * (m + 1) / 2;
-  // Z splits of the projector Grams: enough CTAs for ~8 waves, >= 64 rows each
-  const int64_t resident = (int64_t)h->sm_count * 3;
-  int nsplit = (int)std::max<int64_t>(
-      1, std::min<int64_t>((Z + 63) / 64, (8 * resident + M - 1) / M));
+  // Z splits of the projector Grams (chosen per round, at most nsplit_max,
+  // at least 64 rows each); the partial buffer is sized for nsplit_max
+  const int nsplit_max = (int)std::max<int64_t>(1, std::min<int64_t>(16, (Z + 63) / 64));
+  const int nsplit = nsplit_max;
   // buffers
   if (h->ensure(h->psi, sizeof(double2) * N * ldp) || h->ensure(h->Q, sizeof(double2) * m * N * ld) ||
       h->ensure(h->P, sizeof(double2) * N * ld) || h->ensure(h->partial, sizeof(double2) * pmax * ld) ||
@@ -726,12 +793,21 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   const size_t proj_smem = sizeof(double2) * 4 * m * PROJ_NC;
   CK(cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expm_smem));
   const int maxc = (ncombo + 255) / 256;
-  if (maxc <= 8)
-    CK(cudaFuncSetAttribute(k_proj<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)proj_smem));
-  else if (maxc <= 16)
-    CK(cudaFuncSetAttribute(k_proj<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)proj_smem));
-  else
-    CK(cudaFuncSetAttribute(k_proj<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)proj_smem));
+  const void* proj_fn = maxc <= 8 ? (const void*)k_proj<8> : maxc <= 16 ? (const void*)k_proj<16>
+                                                                         : (const void*)k_proj<24>;
+  CK(cudaFuncSetAttribute(proj_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)proj_smem));
+  // resident CTAs per kernel: grids are sized to whole waves
+  auto resident = [&](const void* fn, int threads, size_t smem) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, threads, smem) != cudaSuccess) b = 1;
+    return std::max(1, b) * h->sm_count;
+  };
+  const int res_spmm = resident((const void*)k_spmm, 256, 0);
+  const int res_pass = std::min(resident((const void*)k_rowpass<PASS_AXPY_DOT>, 256, 0),
+                                resident((const void*)k_rowpass<PASS_AXPY_NORM>, 256, 0));
+  const int res_scale = resident((const void*)k_scale, 256, 0);
+  const int res_psi = resident((const void*)k_psi_update, 256, 0);
+  const int res_proj = resident(proj_fn, 256, proj_smem);
 
   std::vector<int> active;
   if (0.0 < t_end)
@@ -749,9 +825,26 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
     failed.clear();
     const int Ma = (int)list.size();
     const int tiles = (Ma + SPC_LANES - 1) / SPC_LANES;
-    int nrb, rpb;
-    geometry(N, tiles, h->sm_count, nrb, rpb);
-    const dim3 grid(tiles, nrb);
+    int nrb, rpb, nrb_s, rpb_s, nrb_c, rpb_c, nrb_u, rpb_u;
+    geometry(N, tiles, res_pass, nrb, rpb);
+    geometry(N, tiles, res_spmm, nrb_s, rpb_s);
+    geometry(N, tiles, res_scale, nrb_c, rpb_c);
+    geometry(N, tiles, res_psi, nrb_u, rpb_u);
+    const dim3 grid(tiles, nrb), grid_s(tiles, nrb_s), grid_c(tiles, nrb_c), grid_u(tiles, nrb_u);
+    // projector split: the count in [1, nsplit_max] whose grid wastes the
+    // least of its last wave
+    int ns = 1;
+    {
+      double best = 1e30;
+      for (int c = 1; c <= nsplit_max; ++c) {
+        const double waves = (double)Ma * c / res_proj;
+        const double loss = std::ceil(waves) / waves - 1.0 + 0.002 * c;
+        if (loss < best) {
+          best = loss;
+          ns = c;
+        }
+      }
+    }
     CK(cudaMemcpyAsync(d_map, list.data(), sizeof(int) * Ma, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(d_A, 0, sizeof(double2) * mm * Ma, st));
     CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * ld, st));
@@ -778,14 +871,15 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
     k_rowpass<PASS_NORM_GATHER><<<grid, blk, 0, st>>>(a);
     h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
     pe = h->prof.begin(st);
-    k_scale<<<grid, blk, 0, st>>>(N, ld, Ma, rpb, d_psi, ldp, d_map, 1, d_rb, d_Q);
+    k_scale<<<grid_c, blk, 0, st>>>(N, ld, Ma, rpb_c, d_psi, ldp, d_map, 1, d_rb, d_Q);
     h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
     h->count_launch(2);
     const size_t qs = (size_t)N * ld;
     for (int i = 0; i < m; ++i) {
       const double2* Qi = d_Q + (size_t)i * qs;
       pe = h->prof.begin(st);
-      k_spmm<<<grid, blk, 0, st>>>(N, ld, Ma, rpb, h->d_rowptr, h->d_col, h->d_val, Qi, d_P);
+      k_spmm<<<grid_s, blk, 0, st>>>(N, ld, Ma, rpb_s, h->d_rowptr, (const int*)h->xsplit.p,
+                                     (const int*)h->xcol.p, (const double2*)h->xval.p, Qi, d_P);
       // algorithmic traffic: H once, X once, Y once
       h->prof.end(st, pe, PK_SPMM, 8.0 * (double)h->nnz * Ma,
                   20.0 * (double)h->nnz + 4.0 * (N + 1) + 32.0 * elems);
@@ -821,8 +915,8 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
         k_rowpass<PASS_AXPY_NORM><<<grid, blk, 0, st>>>(a);
         h->prof.end(st, pe, PK_AXPY_NORM, 12.0 * elems, 48.0 * elems);
         pe = h->prof.begin(st);
-        k_scale<<<grid, blk, 0, st>>>(N, ld, Ma, rpb, d_P, ldp, d_map, 0, d_rb,
-                                        d_Q + (size_t)(i + 1) * qs);
+        k_scale<<<grid_c, blk, 0, st>>>(N, ld, Ma, rpb_c, d_P, ldp, d_map, 0, d_rb,
+                                          d_Q + (size_t)(i + 1) * qs);
         h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
         h->count_launch(2);
       }
@@ -830,22 +924,22 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
     pe = h->prof.begin(st);
     k_expm<<<Ma, 128, expm_smem, st>>>(m, Ma, d_A, d_E, dt, d_err);
     h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * Ma, 32.0 * (double)mm * Ma);
-    const dim3 pgrid(Ma, nsplit);
+    const dim3 pgrid(Ma, ns);
     pe = h->prof.begin(st);
     if (maxc <= 8)
-      k_proj<8><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, nsplit, d_ppart);
+      k_proj<8><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, ns, d_ppart);
     else if (maxc <= 16)
-      k_proj<16><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, nsplit, d_ppart);
+      k_proj<16><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, ns, d_ppart);
     else
-      k_proj<24><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, nsplit, d_ppart);
+      k_proj<24><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, ns, d_ppart);
     h->prof.end(st, pe, PK_PROJ, 8.0 * (double)ncombo * Z * Ma + 4.0 * (double)m * Z * Ma,
                 16.0 * (double)m * N * Ma);
     {
       const int64_t tot = (int64_t)Ma * ncombo;
       pe = h->prof.begin(st);
-      k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(Ma, m, ncombo, nsplit, d_combos, d_ppart,
+      k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(Ma, m, ncombo, ns, d_combos, d_ppart,
                                                              d_proj);
-      h->prof.end(st, pe, PK_PROJ_REDUCE, 2.0 * tot * nsplit, 16.0 * tot * (nsplit + 1));
+      h->prof.end(st, pe, PK_PROJ_REDUCE, 2.0 * tot * ns, 16.0 * tot * (ns + 1));
       h->count_launch(3);
     }
     if (lanczos) {
@@ -863,7 +957,7 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
                                            d_obs, dt, t_end, tol, d_nsteps, d_err);
     h->prof.end(st, pe, PK_DTLOOP, 0.0, 0.0);
     pe = h->prof.begin(st);
-    k_psi_update<<<grid, blk, 0, st>>>(N, ld, Ma, rpb, m, d_map, d_flag, ldp, d_Q, d_c, d_psi);
+    k_psi_update<<<grid_u, blk, 0, st>>>(N, ld, Ma, rpb_u, m, d_map, d_flag, ldp, d_Q, d_c, d_psi);
     h->prof.end(st, pe, PK_PSI, 8.0 * m * elems, 16.0 * (m + 1) * elems);
     h->count_launch(2);
     CK(cudaGetLastError());
