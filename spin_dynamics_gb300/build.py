@@ -55,13 +55,31 @@ def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_cli()
+    return LIB
+
+
+CLI = os.path.join(OUT, "spinchem")
+CLI_SRC = os.path.join(CSRC, "spinchem_main.cpp")
+
+
+def build_cli() -> str:
+    """The `spinchem input.ini` drop-in executable, linked against the library."""
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(CLI_SRC),
+                                                           os.path.getmtime(LIB)):
+        return CLI
+    cxx = shutil.which(os.environ.get("CXX", "g++")) or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", CLI_SRC, "-o", CLI, "-L", OUT, "-lspinchem_gpu",
+           "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    return LIB
+        raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -1,0 +1,106 @@
+"""The two drop-in drivers (C++ `spinchem` and `python -m spin_dynamics_gb300`)
+on an input.ini: same folders and files as the reference, populations equal
+to the oracle's on the reference's own sample stream within 1e-10."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from spin_dynamics_gb300.spinsys import read_inp
+
+pytestmark = pytest.mark.gpu
+
+INI = """[system variables]
+J = 0.1
+D = 0.0 0.0 0.0 0.0 0.0 0.0 0.0 0.0 0.0
+kS = 2.0
+kT = 2.0
+[electron 1]
+g = 2.0023193
+I = 2 3
+N_I = 1 1
+A1 = 0.5 0.0 0.0 0.0 0.5 0.0 0.0 0.0 0.5
+A2 = 0.3 0.0 0.0 0.0 0.3 0.0 0.0 0.0 0.3
+[electron 2]
+g = 2.0023193
+I = 2
+N_I = 1
+A1 = 0.4 0.0 0.0 0.0 0.4 0.0 0.0 0.0 0.4
+[simulation parameters]
+simulation_type = {kind}
+output_folder = {out}
+seed = 42 99
+B = 0.0 0.2
+initial_state = singlet
+N_samples = 12
+simulation_time = 60
+dt = 0.5
+N_krylov = 10
+integrator_tolerance = 1e-08
+"""
+
+
+def run_cli(cmd, tmp_path, kind):
+    out = tmp_path / "out"
+    out.mkdir()
+    ini = tmp_path / "input.ini"
+    ini.write_text(INI.format(kind=kind, out=out))
+    r = subprocess.run(cmd + [str(ini)], capture_output=True, text=True, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    return str(ini), out
+
+
+def expected(oracle, ini, B):
+    sys_, sim = read_inp(ini)
+    e1, e2 = sys_.e1, sys_.e2
+    rp, col, val = oracle.build_h_iso(e1.g_I, e1.a_iso, e2.g_I, e2.a_iso, B, sys_.J, sys_.D,
+                                      sys_.kS, sys_.kT)
+    if sim.type == "exact_dynamics":
+        zk = np.eye(sys_.Z, dtype=complex)
+    else:
+        zk = oracle.seeded_samples(sim.seed, sys_.Z, sim.N_samples,
+                                   mode=1 if sim.type == "trace_sampling_serial" else 0)
+    return oracle.trace_sampling(rp, col, val, zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol)
+
+
+@pytest.mark.parametrize("driver", ["cpp", "python"])
+@pytest.mark.parametrize("kind", ["trace_sampling", "trace_sampling_serial", "exact_dynamics"])
+def test_driver_output_files(tmp_path, oracle, driver, kind):
+    cmd = ([os.path.join(ROOT, "spin_dynamics_gb300", "_build", "spinchem")] if driver == "cpp"
+           else [sys.executable, "-m", "spin_dynamics_gb300"])
+    ini, out = run_cli(cmd, tmp_path, kind)
+    assert sorted(os.listdir(out)) == [".000", ".200"]
+    for B, sub in ((0.0, ".000"), (0.2, ".200")):
+        ref = expected(oracle, ini, B)
+        assert sorted(os.listdir(out / sub)) == ["S_prob.data", "T0_prob.data", "Tm_prob.data", "Tp_prob.data"]
+        for fname, key in (("S_prob.data", "P_S"), ("T0_prob.data", "P_T0"), ("Tp_prob.data", "P_Tp"),
+                           ("Tm_prob.data", "P_Tm")):
+            got = np.loadtxt(out / sub / fname)
+            assert got.shape == ref[key].shape
+            assert np.max(np.abs(got - ref[key])) <= 1e-10
+
+
+def test_cpp_and_python_writers_agree_byte_for_byte(tmp_path):
+    a = tmp_path / "a"
+    b = tmp_path / "b"
+    a.mkdir()
+    b.mkdir()
+    _, out_a = run_cli([os.path.join(ROOT, "spin_dynamics_gb300", "_build", "spinchem")], a, "exact_dynamics")
+    _, out_b = run_cli([sys.executable, "-m", "spin_dynamics_gb300"], b, "exact_dynamics")
+    for f in ("S_prob.data", "Tm_prob.data"):
+        assert (out_a / ".200" / f).read_text() == (out_b / ".200" / f).read_text()
+
+
+def test_driver_errors(tmp_path):
+    out = tmp_path / "out"
+    out.mkdir()
+    ini = tmp_path / "input.ini"
+    ini.write_text(INI.format(kind="trace_sampling", out=out).replace("A1 = 0.5 0.0 0.0 0.0 0.5",
+                                                                      "A1 = 0.5 0.0 0.0 0.0 0.6"))
+    for cmd in ([os.path.join(ROOT, "spin_dynamics_gb300", "_build", "spinchem")],
+                [sys.executable, "-m", "spin_dynamics_gb300"]):
+        r = subprocess.run(cmd + [str(ini)], capture_output=True, text=True, cwd=ROOT)
+        assert r.returncode == 1 and "Anisotropic Hamiltoninans" in r.stderr

@@ -198,3 +198,23 @@ def test_argument_errors(sampler, oracle):
         sampler.trace_sampling(zk, 0.1, 1.0, 500, 1e-5)  # m > n
     with pytest.raises(SpcError):
         sampler.trace_sampling(zk, -0.1, 1.0, 8, 1e-5)   # dt <= 0
+
+
+def test_exact_krylov_breakdown_gives_the_exact_answer(sampler, oracle):
+    """One proton, m = 8 = n: the Krylov space is exhausted and the reference's
+    get_krylov divides by a zero norm (NaN, reproduced by the oracle). The
+    device path continues with a zero basis vector and returns the closed form
+    P_S(t) = 5/8 + 3/8 cos(a t)."""
+    from spin_dynamics_gb300.spinsys import Electron, SysParam
+    a = 0.8
+    sysp = SysParam(e1=Electron(g_I=[2], A=[np.eye(3) * a]), e2=Electron(g_I=[], A=[]))
+    rp, col, val = iso_csr(oracle, sysp, 0.0)
+    dt = 0.5 * GAMMA_E / 1000
+    zk = np.eye(2, dtype=complex)
+    ref = oracle.trace_sampling(rp, col, val, zk, dt, 30 * dt, 8, 1e-14)
+    assert np.isnan(ref["P_S"][1])
+    sampler.set_h(rp, col, val)
+    got = sampler.trace_sampling(zk, dt, 30 * dt, 8, 1e-14)
+    n = int(np.ceil(30 * dt / dt)) + 1
+    t = np.arange(n) * dt
+    assert np.max(np.abs(got.P_S[:n] - (5 / 8 + 3 / 8 * np.cos(a * t)))) < 1e-12
