@@ -200,6 +200,12 @@ int spc_get_stats(const spc_handle* h, spc_stats* out);
  * mode 1 = trace_sampling (one stream, :198-199). out: M x Z complex. */
 int spc_seeded_samples(int64_t seed0, int64_t seed1, int Z, int M, int mode, double* out);
 
+/* The raw next() stream of a generator seeded with `seed` (set_seed then
+ * next(), src/m_random.f90:90-98,321-331): what the drivers draw per-sample
+ * or per-block seeds from (src/qm_dynamics.f90:317-320,
+ * src/symmetry.f90:76-79). */
+int spc_rng_stream(int64_t seed0, int64_t seed1, int n, uint64_t* out);
+
 /* Electronic initial state and populations (init_el_state,
  * src/qm_dynamics.f90:386-414): which = 0 singlet, 1 T0, 2 Tp, 3 Tm. */
 int spc_init_el_state(int which, double* theta, double* init_pop);

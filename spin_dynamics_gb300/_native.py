@@ -74,6 +74,7 @@ SIGNATURES = {
     "spc_get_stats": (_I, [_P, C.POINTER(spc_stats)]),
     "spc_seeded_samples": (_I, [C.c_int64, C.c_int64, _I, _I, _I, _P]),
     "spc_init_el_state": (_I, [_I, _P, _P]),
+    "spc_rng_stream": (_I, [C.c_int64, C.c_int64, _I, _P]),
     "spc_kinetics": (_I, [_I, _P, _P, _P, _P, _D, _D, _D, _P, _P, _P]),
     "spc_set_krylov": (_I, [_P, _I]),
     "spc_set_profiling": (_I, [_P, _I]),

@@ -324,6 +324,14 @@ int spc_seeded_samples(int64_t seed0, int64_t seed1, int Z, int M, int mode, dou
   return SPC_OK;
 }
 
+int spc_rng_stream(int64_t seed0, int64_t seed1, int n, uint64_t* out) {
+  if (n < 0 || (n > 0 && !out)) return spc::set_error(SPC_ERR_ARG, "spc_rng_stream: bad argument");
+  Rng g;
+  rng_seed(g, (uint64_t)seed0, (uint64_t)seed1);
+  for (int i = 0; i < n; ++i) out[i] = rng_next(g);
+  return SPC_OK;
+}
+
 int spc_init_el_state(int which, double* theta, double* init_pop) {
   if (!theta || !init_pop) return spc::set_error(SPC_ERR_ARG, "null pointer");
   const double h = 1.0 / std::sqrt(2.0);
