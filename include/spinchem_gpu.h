@@ -182,6 +182,33 @@ int spc_trace_sampling_device(spc_handle* h, const double* theta, const double* 
                               const double* zkets_dev, int M, double dt, double t_end, int m,
                               double tol, double* out_dev, int T);
 
+/* ---- batches: many independent systems in one propagation ------------ */
+
+/* Build the Hamiltonians of n_sys systems (same mode) and keep them in the
+ * handle as a batch; system k is addressed by index k below. Replaces the
+ * per-block / per-field calls of getHiso_sp in symmetrised_dynamics
+ * (src/symmetry.f90:102-110) and the field loop of app/main.f90:48-79 with
+ * one device-resident set. The handle's single Hamiltonian is overwritten. */
+int spc_build_h_batch(spc_handle* h, int n_sys, const spc_system* systems, int mode);
+
+/* Trace-sample n_jobs jobs together: job k propagates M[k] caller-supplied
+ * vectors under system job_sys[k] (NULL: system k). Jobs may have different
+ * dimensions; each job's samples are averaged separately. Every build round
+ * batches the Krylov builds of all unfinished samples of all jobs in one set
+ * of launches. zkets: the jobs' M[k] x Z_k complex blocks back to back (host
+ * memory); out: n_jobs x (P_S | P_T0 | P_Tp | P_Tm), T doubles each.
+ * dt, t_end, m, tol, theta and init_pop are shared by all jobs; Lanczos
+ * applies only when every job's H_eff is Hermitian - i*kappa. */
+int spc_trace_sampling_batch(spc_handle* h, int n_jobs, const int* job_sys, const int* M,
+                             const double* theta, const double* init_pop, const double* zkets,
+                             double dt, double t_end, int m, double tol, double* out, int T);
+
+/* The same with device-resident zkets and out. */
+int spc_trace_sampling_batch_device(spc_handle* h, int n_jobs, const int* job_sys, const int* M,
+                                    const double* theta, const double* init_pop,
+                                    const double* zkets_dev, double dt, double t_end, int m,
+                                    double tol, double* out_dev, int T);
+
 /* Select the Krylov orthogonalisation (SPC_KRYLOV_*). In exact arithmetic
  * Lanczos and MGS give the same basis when H_eff = Hermitian - i*kappa; the
  * Lanczos path skips the O(m^2 n) re-orthogonalisation and verifies the

@@ -77,6 +77,9 @@ SIGNATURES = {
     "spc_rng_stream": (_I, [C.c_int64, C.c_int64, _I, _P]),
     "spc_kinetics": (_I, [_I, _P, _P, _P, _P, _D, _D, _D, _P, _P, _P]),
     "spc_set_krylov": (_I, [_P, _I]),
+    "spc_build_h_batch": (_I, [_P, _I, _P, _I]),
+    "spc_trace_sampling_batch": (_I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _I, _D, _P, _I]),
+    "spc_trace_sampling_batch_device": (_I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _I, _D, _P, _I]),
     "spc_set_profiling": (_I, [_P, _I]),
     "spc_get_profile": (_I, [_P, _I, C.POINTER(_D), C.POINTER(C.c_int64), C.POINTER(_D),
                              C.POINTER(_D)]),

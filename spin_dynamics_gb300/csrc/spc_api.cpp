@@ -252,6 +252,122 @@ int spc_trace_sampling(spc_handle* h, const double* theta, const double* init_po
   return SPC_OK;
 }
 
+int spc_build_h_batch(spc_handle* h, int n_sys, const spc_system* systems, int mode) {
+  if (!h || n_sys < 1 || !systems) return spc::set_error(SPC_ERR_ARG, "spc_build_h_batch: bad argument");
+  CKR(cudaSetDevice(h->h.device));
+  spc::Handle& H = h->h;
+  std::vector<spc::HostSystem> hs(n_sys);
+  auto& B = H.hb;
+  B.n.assign(n_sys, 0);
+  B.nnz.assign(n_sys, 0);
+  B.rp_off.assign(n_sys, 0);
+  B.nz_off.assign(n_sys, 0);
+  B.herm.assign(n_sys, 0);
+  int64_t rp_tot = 0, nz_tot = 0;
+  for (int k = 0; k < n_sys; ++k) {
+    int rc = spc::make_host_system(&systems[k], mode, hs[k]);
+    if (rc != SPC_OK) return rc;
+    B.n[k] = (int)hs[k].N;
+    B.nnz[k] = spc::predict_nnz(hs[k], mode);
+    B.rp_off[k] = rp_tot;
+    B.nz_off[k] = nz_tot;
+    B.herm[k] = hs[k].herm_shift;
+    rp_tot += hs[k].N + 1;
+    nz_tot += B.nnz[k];
+  }
+  if (H.ensure(B.rowptr, sizeof(int) * rp_tot) || H.ensure(B.split, sizeof(int) * rp_tot) ||
+      H.ensure(B.col, sizeof(int) * nz_tot) || H.ensure(B.val, sizeof(double2) * nz_tot))
+    return SPC_ERR_ALLOC;
+  for (int k = 0; k < n_sys; ++k) {
+    int rc = spc::build_h_device(&H, hs[k], mode);
+    if (rc != SPC_OK) return rc;
+    if (H.nnz != B.nnz[k]) return spc::set_error(SPC_ERR_STATE, "internal: nonzero count mismatch");
+    cudaStream_t st = H.stream;
+    CKR(cudaMemcpyAsync((int*)B.rowptr.p + B.rp_off[k], H.d_rowptr, sizeof(int) * (B.n[k] + 1),
+                        cudaMemcpyDeviceToDevice, st));
+    CKR(cudaMemcpyAsync((int*)B.split.p + B.rp_off[k], H.xsplit.p, sizeof(int) * B.n[k],
+                        cudaMemcpyDeviceToDevice, st));
+    CKR(cudaMemcpyAsync((int*)B.col.p + B.nz_off[k], H.xcol.p, sizeof(int) * B.nnz[k],
+                        cudaMemcpyDeviceToDevice, st));
+    CKR(cudaMemcpyAsync((double2*)B.val.p + B.nz_off[k], H.xval.p, sizeof(double2) * B.nnz[k],
+                        cudaMemcpyDeviceToDevice, st));
+  }
+  CKR(cudaStreamSynchronize(H.stream));
+  return SPC_OK;
+}
+
+static int batch_jobs(spc_handle* h, int n_jobs, const int* job_sys, const int* M,
+                      const double2* zk_dev, double* out_dev, int T, std::vector<spc::JobSpec>& jobs) {
+  const auto& B = h->h.hb;
+  if (B.n.empty()) return spc::set_error(SPC_ERR_STATE, "no batch Hamiltonians: call spc_build_h_batch first");
+  jobs.resize(n_jobs);
+  int64_t zoff = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    const int s = job_sys ? job_sys[k] : k;
+    if (s < 0 || s >= (int)B.n.size()) return spc::set_error(SPC_ERR_ARG, "job %d refers to system %d", k, s);
+    if (M[k] < 1) return spc::set_error(SPC_ERR_ARG, "job %d has no samples", k);
+    spc::JobSpec& j = jobs[k];
+    j.n = B.n[s];
+    j.nnz = B.nnz[s];
+    j.M = M[k];
+    j.rowptr = (const int*)B.rowptr.p + B.rp_off[s];
+    j.split = (const int*)B.split.p + B.rp_off[s];
+    j.col = (const int*)B.col.p + B.nz_off[s];
+    j.val = (const double2*)B.val.p + B.nz_off[s];
+    j.zk = zk_dev + zoff;
+    j.out = out_dev + (size_t)k * 4 * T;
+    j.herm_shift = B.herm[s] != 0;
+    zoff += (int64_t)M[k] * (j.n / 4);
+  }
+  return SPC_OK;
+}
+
+int spc_trace_sampling_batch_device(spc_handle* h, int n_jobs, const int* job_sys, const int* M,
+                                    const double* theta, const double* init_pop,
+                                    const double* zkets_dev, double dt, double t_end, int m,
+                                    double tol, double* out_dev, int T) {
+  if (!h || n_jobs < 1 || !M || !theta || !init_pop || !zkets_dev || !out_dev)
+    return spc::set_error(SPC_ERR_ARG, "spc_trace_sampling_batch: null argument");
+  if (!(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt must be positive");
+  if (m < 1 || m > 48) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d outside [1, 48]", m);
+  if (T != spc::num_time_points(dt, t_end))
+    return spc::set_error(SPC_ERR_ARG, "T must be spc_num_time_points(dt, t_end) = %d",
+                          spc::num_time_points(dt, t_end));
+  CKR(cudaSetDevice(h->h.device));
+  std::vector<spc::JobSpec> jobs;
+  int rc = batch_jobs(h, n_jobs, job_sys, M, (const double2*)zkets_dev, out_dev, T, jobs);
+  if (rc) return rc;
+  for (const auto& j : jobs)
+    if (m > j.n) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d exceeds a job's dimension %d", m, j.n);
+  return spc::propagate_batch(&h->h, theta, init_pop, jobs, dt, t_end, m, tol, T);
+}
+
+int spc_trace_sampling_batch(spc_handle* h, int n_jobs, const int* job_sys, const int* M,
+                             const double* theta, const double* init_pop, const double* zkets,
+                             double dt, double t_end, int m, double tol, double* out, int T) {
+  if (!h || n_jobs < 1 || !M || !zkets || !out)
+    return spc::set_error(SPC_ERR_ARG, "spc_trace_sampling_batch: null argument");
+  const auto& B = h->h.hb;
+  int64_t ztot = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    const int s = job_sys ? job_sys[k] : k;
+    if (s < 0 || s >= (int)B.n.size()) return spc::set_error(SPC_ERR_ARG, "job %d refers to system %d", k, s);
+    ztot += (int64_t)M[k] * (B.n[s] / 4);
+  }
+  spc::Handle& H = h->h;
+  CKR(cudaSetDevice(H.device));
+  if (H.ensure(H.zk, sizeof(double) * 2 * ztot) || H.ensure(H.out, sizeof(double) * 4 * T * (size_t)n_jobs))
+    return SPC_ERR_ALLOC;
+  CKR(cudaMemcpyAsync(H.zk.p, zkets, sizeof(double) * 2 * ztot, cudaMemcpyHostToDevice, H.stream));
+  int rc = spc_trace_sampling_batch_device(h, n_jobs, job_sys, M, theta, init_pop, (const double*)H.zk.p,
+                                           dt, t_end, m, tol, (double*)H.out.p, T);
+  if (rc) return rc;
+  CKR(cudaMemcpyAsync(out, H.out.p, sizeof(double) * 4 * T * (size_t)n_jobs, cudaMemcpyDeviceToHost,
+                      H.stream));
+  CKR(cudaStreamSynchronize(H.stream));
+  return SPC_OK;
+}
+
 int spc_set_profiling(spc_handle* h, int enable) {
   if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
   h->h.prof.on = enable != 0;

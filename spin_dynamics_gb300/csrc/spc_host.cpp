@@ -66,7 +66,8 @@ int Handle::ensure_h_entries(size_t count) {
 }
 Handle::~Handle() {
   Buf* all[] = {&psi, &Q,  &P,    &partial, &counters, &coef, &rbeta, &Ahess, &Aexp, &proj, &projpart,
-                &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag, &xcol, &xval, &xsplit};
+                &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag, &xcol, &xval, &xsplit, &plan, &jobtab,
+                &hb.rowptr, &hb.split, &hb.col, &hb.val};
   for (Buf* b : all)
     if (b->p) cudaFree(b->p);
   if (d_rowptr) cudaFree(d_rowptr);
@@ -214,6 +215,16 @@ int make_host_system(const spc_system* sys, int mode, HostSystem& hs) {
       }
   }
   return SPC_OK;
+}
+
+int64_t predict_nnz(const HostSystem& hs, int mode) {
+  // per nucleus of multiplicity g: the reference builder stores (g-1)/g of the
+  // rows once (S+I- or S-I+), the general builder 4(g-1)/g (two electron
+  // patterns times the m -> m+1 and m -> m-1 neighbours); src/hamiltonian.f90:62-73
+  const int64_t N = hs.N;
+  int64_t nnz = mode == SPC_H_REFERENCE ? N + N / 2 : 4 * N;
+  for (const NucInfo& q : hs.nuc) nnz += (mode == SPC_H_REFERENCE ? 1 : 4) * (N / q.g) * (q.g - 1);
+  return nnz;
 }
 
 }  // namespace spc

@@ -101,7 +101,14 @@ struct Handle {
     size_t bytes = 0;
   };
   Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
-      map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit;
+      map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit, plan, jobtab;
+  // Hamiltonians of a batch (spc_build_h_batch): execution-order CSRs back to back
+  struct HBatch {
+    std::vector<int> n;
+    std::vector<int64_t> nnz, rp_off, nz_off;
+    std::vector<char> herm;
+    Buf rowptr, split, col, val;
+  } hb;
   // Krylov method: 0 full MGS (the reference's get_krylov), 1 Lanczos, 2 auto
   int krylov_method = 0;
   // H_eff = (Hermitian) - i*kappa*1 for the current Hamiltonian: Lanczos applies
@@ -122,10 +129,30 @@ struct Handle {
   ~Handle();
 };
 
+// One job of a batched propagation: a Hamiltonian (execution-order CSR on the
+// device), its sample vectors and its output.
+struct JobSpec {
+  int n = 0;               // Hilbert dimension
+  int64_t nnz = 0;
+  int M = 0;               // samples
+  const int* rowptr = nullptr;
+  const int* split = nullptr;
+  const int* col = nullptr;
+  const double2* val = nullptr;
+  const double2* zk = nullptr;  // device, M x n/4 complex, sample-major
+  double* out = nullptr;        // device, 4*T
+  bool herm_shift = false;
+};
+
 int set_error(int code, const char* fmt, ...);
 int build_h_device(Handle* h, const HostSystem& hs, int mode);
 int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev,
               int M, double dt, double t_end, int m, double tol, double* out_dev, int T);
+int propagate_batch(Handle* h, const double* theta, const double* init_pop,
+                    const std::vector<JobSpec>& jobs, double dt, double t_end, int m, double tol,
+                    int T);
+// Nonzero count spc_build_h produces for a system (closed form per mode).
+int64_t predict_nnz(const HostSystem& hs, int mode);
 int num_time_points(double dt, double t_end);
 // Execution order of H's rows for k_spmm (complex entries first).
 int prepare_spmm_rows(Handle* h);

@@ -1,25 +1,34 @@
 // Batched trace-sampling propagation on the device.
 //
-// Restates trace_sampling_para (src/qm_dynamics.f90:257-384) for all M
-// samples at once. Samples are the columns of every vector array, stored
-// row-major with the sample index fastest: X[row * ld + w]. Each round, every
-// sample that has not reached t_end builds a new Krylov basis (the reference
-// rebuilds each sample independently; the build does not depend on t, so
-// batching the builds of all unfinished samples is the same computation),
-// then runs its own dt loop until its own rebuild test fires. Finished
-// samples leave the batch (column map `map[w] -> sample`).
+// Restates trace_sampling_para (src/qm_dynamics.f90:257-384) for many samples
+// of one or many independent systems ("jobs": radical pairs, field
+// orientations, symmetry blocks) at once. Every job keeps its own
+// Hamiltonian and dimension; its samples are grouped into tiles of 32, and a
+// tile's vectors are stored as a self-contained [rows][32] block with the
+// sample index fastest, so a warp reads 32 samples of one row as one 512-byte
+// transaction and tiles of jobs of any size mix freely in one launch.
+//
+// Each round, every sample that has not reached t_end builds a new Krylov
+// basis (the reference rebuilds each sample independently; the build does not
+// depend on t, so batching the builds of all unfinished samples is the same
+// computation), then runs its own dt loop until its own rebuild test fires.
+// Finished samples leave the next round's tiles.
 //
 // Per round:
 //   norm/scale passes      c = ||psi|| e1, Q0 = psi/||psi||      (get_krylov :445-449)
-//   m x [ SpMM p = H Q_i ; MGS dot/axpy passes ; scale ]           (:451-465)
+//   m x [ SpMM p = H Q_i ; MGS (or Lanczos) passes ; scale ]       (:451-465)
 //   Pade-6 expm of -i dt A per sample, one CTA each               (matrix_exponential.f90)
 //   Krylov projectors as Hermitian Grams per sample               (convert_to_krylov :469-498)
 //   dt loop per sample, one warp each                             (:351-364)
 //   psi = Q c                                                      (:365)
 //
-// All reductions are two-level and in a fixed order (per-CTA partials, then
-// the last CTA of each sample tile sums them), so results do not depend on
-// scheduling.
+// Row kernels run over work items (tile, phase): an item takes every
+// (items_of_tile * 8)-th row of its tile starting at phase*8 + warp, so row
+// lengths balance and all items of a tile sweep its rows together. Item
+// counts per tile are proportional to the tile's rows and sum to about one
+// wave of resident CTAs. Reductions are two-level and in a fixed order
+// (per-item partials, then the last item of each tile sums them), so results
+// do not depend on scheduling.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -31,24 +40,42 @@
 
 namespace spc {
 
+// Per-tile description (device copy built each round).
+struct TileInfo {
+  int job;           // job index
+  int n;             // rows = Hilbert dimension of the job
+  int ldp;           // leading dimension of the job's psi block
+  int ip0, nip;      // first pass item, pass items of this tile
+  int is0, nis;      // first SpMM item, SpMM items of this tile
+  int pad;
+  int64_t q_off;     // Q_t[j] = Q + q_off + j * n * 32
+  int64_t p_off;     // P_t = P + p_off
+  int64_t psi_off;   // job psi block
+  const int* rowptr;
+  const int* split;
+  const int* col;
+  const double2* val;
+};
+
 enum PassKind { PASS_NORM_GATHER = 0, PASS_DOT = 1, PASS_AXPY_DOT = 2, PASS_AXPY_NORM = 3 };
 
 struct PassArgs {
-  int64_t N;
-  int ld, Ma, rpb, m, col_i, row_j;
+  const TileInfo* tiles;
+  const int2* items;  // pass items (tile, phase)
+  int m, col_i, row_j;
   int lanczos;        // AXPY_NORM also seeds the next Lanczos coefficient
-  const double2* X;   // NORM_GATHER: psi (ldp columns, gathered through map); DOT: Q_0
-  double2* P;         // Arnoldi work vector
-  const double2* Qj;  // AXPY_*: the basis vector removed from P
-  const double2* Qn;  // AXPY_DOT: the next basis vector to project on
-  const int* map;
-  int ldp;
-  double2* coef;      // current MGS coefficient per sample
-  double* rbeta;      // 1/norm per sample
-  double2* Ahess;     // Hessenberg matrices, m x m column-major per sample
-  double2* cvec;      // Krylov coordinates per sample
-  double2* partial;   // [row blocks][ld]
-  unsigned* counters; // per sample tile
+  int jx, jn;         // basis indices: DOT reads Q_jx; AXPY removes Q_jx, dots with Q_jn
+  const double2* Q;
+  double2* P;
+  const double2* psi;
+  const int* map;     // slot -> global sample (or -1)
+  const int* scol;    // slot -> column in its job's psi
+  double2* coef;      // current MGS coefficient per slot
+  double* rbeta;      // 1/norm per slot
+  double2* Ahess;     // Hessenberg matrices, m x m column-major per slot
+  double2* cvec;      // Krylov coordinates per slot
+  double2* partial;   // [items][32]
+  unsigned* counters; // per tile
 };
 
 template <int KIND>
@@ -77,39 +104,47 @@ __device__ __forceinline__ void pass_finalize(const PassArgs& a, int w, double2 
   }
 }
 
-// One pass over all rows for a tile of 32 samples: element update + per-sample
-// reduction. Grid (sample tiles, row blocks), block (32, SPC_WARPS).
+// One pass over the rows of a work item: element update + per-slot
+// reduction. Grid = pass items, block (32, SPC_WARPS).
 template <int KIND>
 __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
   __shared__ double2 red[SPC_WARPS][SPC_LANES];
   __shared__ bool am_last;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int w = blockIdx.x * SPC_LANES + tx;
-  const bool act = w < a.Ma;
-  const int64_t r0 = (int64_t)blockIdx.y * a.rpb;
-  const int64_t r1 = min(a.N, r0 + a.rpb);
+  const int2 it = a.items[blockIdx.x];
+  const TileInfo& T = a.tiles[it.x];
+  const int w = it.x * SPC_LANES + tx;
+  const bool act = a.map[w] >= 0;
+  const int n = T.n;
+  const int stride = T.nip * SPC_WARPS;
+  const size_t vs = (size_t)n * SPC_LANES;
   double2 acc = cz();
   if (act) {
     if (KIND == PASS_NORM_GATHER) {
-      const int src = a.map[w];
-      for (int64_t r = r0 + ty; r < r1; r += SPC_WARPS) {
-        double2 x = a.X[(size_t)r * a.ldp + src];
+      const double2* src = a.psi + T.psi_off + a.scol[w];
+      for (int r = it.y * SPC_WARPS + ty; r < n; r += stride) {
+        double2 x = src[(size_t)r * T.ldp];
         acc.x = fma(x.x, x.x, acc.x);
         acc.x = fma(x.y, x.y, acc.x);
       }
     } else if (KIND == PASS_DOT) {
-      for (int64_t r = r0 + ty; r < r1; r += SPC_WARPS) {
-        size_t o = (size_t)r * a.ld + w;
-        acc = cjfma(a.X[o], a.P[o], acc);
+      const double2* X = a.Q + T.q_off + a.jx * vs + tx;
+      const double2* P = a.P + T.p_off + tx;
+      for (int r = it.y * SPC_WARPS + ty; r < n; r += stride) {
+        const size_t o = (size_t)r * SPC_LANES;
+        acc = cjfma(X[o], P[o], acc);
       }
     } else {
       const double2 cf = a.coef[w];
-      for (int64_t r = r0 + ty; r < r1; r += SPC_WARPS) {
-        size_t o = (size_t)r * a.ld + w;
-        double2 p = cfms(cf, a.Qj[o], a.P[o]);
-        a.P[o] = p;
+      const double2* Qj = a.Q + T.q_off + a.jx * vs + tx;
+      const double2* Qn = a.Q + T.q_off + a.jn * vs + tx;
+      double2* P = a.P + T.p_off + tx;
+      for (int r = it.y * SPC_WARPS + ty; r < n; r += stride) {
+        const size_t o = (size_t)r * SPC_LANES;
+        double2 p = cfms(cf, Qj[o], P[o]);
+        P[o] = p;
         if (KIND == PASS_AXPY_DOT) {
-          acc = cjfma(a.Qn[o], p, acc);
+          acc = cjfma(Qn[o], p, acc);
         } else {
           acc.x = fma(p.x, p.x, acc.x);
           acc.x = fma(p.y, p.y, acc.x);
@@ -123,20 +158,20 @@ __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
     double2 s = red[0][tx];
 #pragma unroll
     for (int y = 1; y < SPC_WARPS; ++y) s = cadd(s, red[y][tx]);
-    a.partial[(size_t)blockIdx.y * a.ld + w] = s;
+    a.partial[(size_t)blockIdx.x * SPC_LANES + tx] = s;
   }
   __threadfence();
   __syncthreads();
   if (tx == 0 && ty == 0) {
-    unsigned t = atomicAdd(&a.counters[blockIdx.x], 1u);
-    am_last = (t == gridDim.y - 1);
+    unsigned t = atomicAdd(&a.counters[it.x], 1u);
+    am_last = (t == (unsigned)T.nip - 1);
   }
   __syncthreads();
   if (!am_last) return;
   __threadfence();
   double2 s = cz();
-  for (int b = ty; b < (int)gridDim.y; b += SPC_WARPS)
-    s = cadd(s, __ldcg(&a.partial[(size_t)b * a.ld + w]));
+  for (int b = ty; b < T.nip; b += SPC_WARPS)
+    s = cadd(s, __ldcg(&a.partial[(size_t)(T.ip0 + b) * SPC_LANES + tx]));
   red[ty][tx] = s;
   __syncthreads();
   if (ty == 0) {
@@ -144,44 +179,62 @@ __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
 #pragma unroll
     for (int y = 1; y < SPC_WARPS; ++y) tot = cadd(tot, red[y][tx]);
     if (act) pass_finalize<KIND>(a, w, tot);
-    if (tx == 0) a.counters[blockIdx.x] = 0u;
+    if (tx == 0) a.counters[it.x] = 0u;
   }
 }
 
-// Q_{i+1} = P / ||P||  (or Q_0 = psi[:, map] / ||psi|| when gather != 0)
+// Q_{jd} = P / ||P||  (or Q_0 = psi[:, scol] / ||psi|| when gather != 0);
+// grid = pass items.
 __global__ void __launch_bounds__(256)
-    k_scale(int64_t N, int ld, int Ma, int rpb, const double2* __restrict__ src, int ldp,
-            const int* __restrict__ map, int gather, const double* __restrict__ rbeta,
-            double2* __restrict__ dst) {
-  const int w = blockIdx.x * SPC_LANES + threadIdx.x;
-  if (w >= Ma) return;
+    k_scale(const TileInfo* __restrict__ tiles, const int2* __restrict__ items,
+            const int* __restrict__ map, const int* __restrict__ scol,
+            const double2* __restrict__ psi, const double2* __restrict__ P, int gather, int jd,
+            const double* __restrict__ rbeta, double2* __restrict__ Q) {
+  const int2 it = items[blockIdx.x];
+  const TileInfo& T = tiles[it.x];
+  const int tx = threadIdx.x;
+  const int w = it.x * SPC_LANES + tx;
+  if (map[w] < 0) return;
   const double rb = rbeta[w];
-  const int col = gather ? map[w] : w;
-  const int lds = gather ? ldp : ld;
-  const int64_t r0 = (int64_t)blockIdx.y * rpb;
-  const int64_t r1 = min(N, r0 + rpb);
-  for (int64_t r = r0 + threadIdx.y; r < r1; r += SPC_WARPS) {
-    double2 x = src[(size_t)r * lds + col];
-    dst[(size_t)r * ld + w] = make_double2(x.x * rb, x.y * rb);
+  const int n = T.n;
+  const int stride = T.nip * SPC_WARPS;
+  double2* dst = Q + T.q_off + (size_t)jd * n * SPC_LANES + tx;
+  if (gather) {
+    const double2* src = psi + T.psi_off + scol[w];
+    for (int r = it.y * SPC_WARPS + threadIdx.y; r < n; r += stride) {
+      const double2 x = src[(size_t)r * T.ldp];
+      dst[(size_t)r * SPC_LANES] = make_double2(x.x * rb, x.y * rb);
+    }
+  } else {
+    const double2* src = P + T.p_off + tx;
+    for (int r = it.y * SPC_WARPS + threadIdx.y; r < n; r += stride) {
+      const double2 x = src[(size_t)r * SPC_LANES];
+      dst[(size_t)r * SPC_LANES] = make_double2(x.x * rb, x.y * rb);
+    }
   }
 }
 
-// Y = H X for a tile of 32 sample columns; one warp per row at a time, the
+// P_t = H Q_t[i] for the tile of a SpMM item; one warp per row at a time, the
 // row's (col, val) entries broadcast to all lanes. Rows are stored in the
 // execution order of k_split_rows: entries with a nonzero imaginary part
 // first (4 DFMA each), then real ones from split[r] on (2 DFMA each).
 __global__ void __launch_bounds__(256)
-    k_spmm(int64_t N, int ld, int Ma, int rpb, const int* __restrict__ rowptr,
-           const int* __restrict__ split, const int* __restrict__ col,
-           const double2* __restrict__ val, const double2* __restrict__ X,
-           double2* __restrict__ Y) {
-  const int w = blockIdx.x * SPC_LANES + threadIdx.x;
-  const bool act = w < Ma;
-  (void)rpb;
-  // rows interleaved over the CTAs of a sample tile: balanced row lengths,
-  // and all CTAs sweep X together (L2 reuse of the Kronecker neighbours)
-  const int64_t stride = (int64_t)gridDim.y * SPC_WARPS;
-  for (int64_t r = (int64_t)blockIdx.y * SPC_WARPS + threadIdx.y; r < N; r += stride) {
+    k_spmm(const TileInfo* __restrict__ tiles, const int2* __restrict__ items,
+           const int* __restrict__ map, int i, const double2* __restrict__ Q,
+           double2* __restrict__ Pout) {
+  const int2 it = items[blockIdx.x];
+  const TileInfo& T = tiles[it.x];
+  const int tx = threadIdx.x;
+  const bool act = map[it.x * SPC_LANES + tx] >= 0;
+  const int n = T.n;
+  const int* __restrict__ rowptr = T.rowptr;
+  const int* __restrict__ split = T.split;
+  const int* __restrict__ col = T.col;
+  const double2* __restrict__ val = T.val;
+  const double2* X = Q + T.q_off + (size_t)i * n * SPC_LANES + tx;
+  double2* Y = Pout + T.p_off + tx;
+  const int stride = T.nis * SPC_WARPS;
+  for (int r = it.y * SPC_WARPS + threadIdx.y; r < n; r += stride) {
     const int k0 = __ldg(rowptr + r), ks = __ldg(split + r), k1 = __ldg(rowptr + r + 1);
     double2 a0 = cz(), a1 = cz();
     int k = k0;
@@ -189,8 +242,8 @@ __global__ void __launch_bounds__(256)
       const int c0 = __ldg(col + k), c1 = __ldg(col + k + 1);
       const double2 v0 = __ldg(val + k), v1 = __ldg(val + k + 1);
       if (act) {
-        const double2 x0 = X[(size_t)c0 * ld + w];
-        const double2 x1 = X[(size_t)c1 * ld + w];
+        const double2 x0 = X[(size_t)c0 * SPC_LANES];
+        const double2 x1 = X[(size_t)c1 * SPC_LANES];
         a0 = cfma(v0, x0, a0);
         a1 = cfma(v1, x1, a1);
       }
@@ -198,15 +251,15 @@ __global__ void __launch_bounds__(256)
     if (k < ks) {
       const int c0 = __ldg(col + k);
       const double2 v0 = __ldg(val + k);
-      if (act) a0 = cfma(v0, X[(size_t)c0 * ld + w], a0);
+      if (act) a0 = cfma(v0, X[(size_t)c0 * SPC_LANES], a0);
       k++;
     }
     for (; k + 1 < k1; k += 2) {
       const int c0 = __ldg(col + k), c1 = __ldg(col + k + 1);
       const double v0 = __ldg(&val[k].x), v1 = __ldg(&val[k + 1].x);
       if (act) {
-        const double2 x0 = X[(size_t)c0 * ld + w];
-        const double2 x1 = X[(size_t)c1 * ld + w];
+        const double2 x0 = X[(size_t)c0 * SPC_LANES];
+        const double2 x1 = X[(size_t)c1 * SPC_LANES];
         a0.x = fma(v0, x0.x, a0.x);
         a0.y = fma(v0, x0.y, a0.y);
         a1.x = fma(v1, x1.x, a1.x);
@@ -217,12 +270,12 @@ __global__ void __launch_bounds__(256)
       const int c0 = __ldg(col + k);
       const double v0 = __ldg(&val[k].x);
       if (act) {
-        const double2 x0 = X[(size_t)c0 * ld + w];
+        const double2 x0 = X[(size_t)c0 * SPC_LANES];
         a0.x = fma(v0, x0.x, a0.x);
         a0.y = fma(v0, x0.y, a0.y);
       }
     }
-    if (act) Y[(size_t)r * ld + w] = cadd(a0, a1);
+    if (act) Y[(size_t)r * SPC_LANES] = cadd(a0, a1);
   }
 }
 
@@ -279,8 +332,8 @@ __device__ void smem_matmul(int m, const double2* A, const double2* B, double2* 
 }
 
 __global__ void __launch_bounds__(128)
-    k_expm(int m, int Ma, const double2* __restrict__ Ahess, double2* __restrict__ Aexp, double dt,
-           int* __restrict__ err) {
+    k_expm(int m, int nslots, const int* __restrict__ map, const double2* __restrict__ Ahess,
+           double2* __restrict__ Aexp, double dt, int* __restrict__ err) {
   extern __shared__ double2 sm[];
   __shared__ double rowsum[SPC_MAX_M];
   __shared__ int piv[SPC_MAX_M];
@@ -288,7 +341,7 @@ __global__ void __launch_bounds__(128)
   const int mm = m * m;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int w = blockIdx.x;
-  if (w >= Ma) return;
+  if (w >= nslots || map[w] < 0) return;
   double2* A2 = sm;
   double2* X = A2 + mm;
   double2* E = X + mm;
@@ -438,16 +491,21 @@ __global__ void __launch_bounds__(128)
 //   S  = 1/2 (Q_b2 - Q_b3)^H (Q_b2 - Q_b3),  T0 = 1/2 (Q_b2 + Q_b3)^H (Q_b2 + Q_b3)
 // with b1..b4 the Z-row blocks |aa>, |ab>, |ba>, |bb>. S and T0 are the
 // Hermitian parts of the reference's P_S, P_T0; Re(c^H P c) is unchanged.
-// Grid (samples, Z splits); 256 threads each own up to MAXC (type, i<=j).
+// Grid (slots, Z splits); 256 threads each own up to MAXC (type, i<=j).
 #define PROJ_NC 32
 template <int MAXC>
 __global__ void __launch_bounds__(256)
-    k_proj(int64_t N, int64_t Z, int ld, int m, int ncombo, const unsigned* __restrict__ combos,
-           const double2* __restrict__ Q, int nsplit, double2* __restrict__ part) {
+    k_proj(const TileInfo* __restrict__ tiles, const int* __restrict__ map, int m, int ncombo,
+           const unsigned* __restrict__ combos, const double2* __restrict__ Q, int nsplit,
+           double2* __restrict__ part) {
   extern __shared__ double2 V[];  // [4][m][PROJ_NC]
   const int w = blockIdx.x;
+  if (map[w] < 0) return;
+  const TileInfo& Ti = tiles[w / SPC_LANES];
+  const int lane = w % SPC_LANES;
   const int split = blockIdx.y;
   const int tid = threadIdx.x;
+  const int64_t Z = Ti.n / 4;
   const int64_t per = (Z + nsplit - 1) / nsplit;
   const int64_t n0 = (int64_t)split * per;
   const int64_t n1 = min(Z, n0 + per);
@@ -466,19 +524,20 @@ __global__ void __launch_bounds__(256)
       oi[q] = oj[q] = 0;
     }
   }
-  const size_t qstride = (size_t)N * ld;
+  const size_t vs = (size_t)Ti.n * SPC_LANES;
+  const double2* Qt = Q + Ti.q_off + lane;
   for (int64_t c0 = n0; c0 < n1; c0 += PROJ_NC) {
     const int len = (int)min((int64_t)PROJ_NC, n1 - c0);
     for (int idx = tid; idx < m * PROJ_NC; idx += 256) {
       const int j = idx / PROJ_NC, nn = idx % PROJ_NC;
       double2 q1 = cz(), q2 = cz(), q3 = cz(), q4 = cz();
       if (nn < len) {
-        const double2* base = Q + (size_t)j * qstride + w;
+        const double2* base = Qt + (size_t)j * vs;
         const int64_t n = c0 + nn;
-        q1 = base[(size_t)n * ld];
-        q2 = base[(size_t)(Z + n) * ld];
-        q3 = base[(size_t)(2 * Z + n) * ld];
-        q4 = base[(size_t)(3 * Z + n) * ld];
+        q1 = base[(size_t)n * SPC_LANES];
+        q2 = base[(size_t)(Z + n) * SPC_LANES];
+        q3 = base[(size_t)(2 * Z + n) * SPC_LANES];
+        q4 = base[(size_t)(3 * Z + n) * SPC_LANES];
       }
       V[(0 * m + j) * PROJ_NC + nn] = q1;
       V[(1 * m + j) * PROJ_NC + nn] = csub(q2, q3);
@@ -502,14 +561,15 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void k_proj_reduce(int Ma, int m, int ncombo, int nsplit,
-                              const unsigned* __restrict__ combos, const double2* __restrict__ part,
-                              double2* __restrict__ proj) {
+__global__ void k_proj_reduce(int nslots, const int* __restrict__ map, int m, int ncombo,
+                              int nsplit, const unsigned* __restrict__ combos,
+                              const double2* __restrict__ part, double2* __restrict__ proj) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (int64_t)Ma * ncombo) return;
+  if (idx >= (int64_t)nslots * ncombo) return;
   const int w = (int)(idx / ncombo), cid = (int)(idx % ncombo);
+  if (map[w] < 0) return;
   double2 s = cz();
-  for (int sp = 0; sp < nsplit; ++sp) s = cadd(s, part[((size_t)sp * Ma + w) * ncombo + cid]);
+  for (int sp = 0; sp < nsplit; ++sp) s = cadd(s, part[((size_t)sp * nslots + w) * ncombo + cid]);
   const unsigned cb = combos[cid];
   const int t = cb >> 16, i = (cb >> 8) & 255, j = cb & 255;
   if (t == 1 || t == 2) s = make_double2(0.5 * s.x, 0.5 * s.y);
@@ -519,12 +579,14 @@ __global__ void k_proj_reduce(int Ma, int m, int ncombo, int nsplit,
 }
 
 // Orthonormality of a Lanczos basis from the projector Grams:
-// max_ij |(Tp + S + T0 + Tm)_ij - delta_ij| > tol flags the sample.
+// max_ij |(Tp + S + T0 + Tm)_ij - delta_ij| > tol flags the slot.
 #define ORTHO_TOL 1e-12
 __global__ void __launch_bounds__(128)
-    k_ortho_check(int m, int Ma, const double2* __restrict__ proj, double tol, int* __restrict__ flag) {
+    k_ortho_check(int m, const int* __restrict__ map, const double2* __restrict__ proj, double tol,
+                  int* __restrict__ flag) {
   __shared__ double red[128];
   const int w = blockIdx.x;
+  if (map[w] < 0) return;
   const size_t mm = (size_t)m * m;
   const double2* P = proj + (size_t)w * 4 * mm;
   double mx = 0.0;
@@ -547,18 +609,18 @@ __global__ void __launch_bounds__(128)
 }
 
 // ---------------------------------------------------------------------------
-// dt loop (src/qm_dynamics.f90:348-364), one warp per sample. Projector types
+// dt loop (src/qm_dynamics.f90:348-364), one warp per slot. Projector types
 // in `proj`: 0 Tp, 1 S, 2 T0, 3 Tm; obs slots per sample: 0 S, 1 T0, 2 Tp, 3 Tm.
 __global__ void __launch_bounds__(128)
-    k_dtloop(int m, int Ma, int T, const int* __restrict__ map, const int* __restrict__ skip,
-             const double2* __restrict__ Aexp,
-             const double2* __restrict__ proj, double2* __restrict__ cvec, double* __restrict__ tt,
-             int* __restrict__ kk, int* __restrict__ done, double* __restrict__ obs, double dt,
-             double t_end, double tol, long long* __restrict__ nsteps, int* __restrict__ err) {
+    k_dtloop(int m, int nslots, int T, const int* __restrict__ map, const int* __restrict__ skip,
+             const double2* __restrict__ Aexp, const double2* __restrict__ proj,
+             double2* __restrict__ cvec, double* __restrict__ tt, int* __restrict__ kk,
+             int* __restrict__ done, double* __restrict__ obs, double dt, double t_end, double tol,
+             long long* __restrict__ nsteps, int* __restrict__ err) {
   __shared__ double2 cs[4][SPC_MAX_M];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w = blockIdx.x * 4 + warp;
-  if (w >= Ma || skip[w]) return;
+  if (w >= nslots || map[w] < 0 || skip[w]) return;
   const int s = map[w];
   const size_t mm = (size_t)m * m;
   const double2* E = Aexp + (size_t)w * mm;
@@ -624,53 +686,63 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// psi[:, map[w]] = Q c  (src/qm_dynamics.f90:365)
+// psi[:, scol] = Q c for the tile of a pass item (src/qm_dynamics.f90:365)
 __global__ void __launch_bounds__(256)
-    k_psi_update(int64_t N, int ld, int Ma, int rpb, int m, const int* __restrict__ map,
-                 const int* __restrict__ skip, int ldp,
-                 const double2* __restrict__ Q, const double2* __restrict__ cvec,
-                 double2* __restrict__ psi) {
+    k_psi_update(const TileInfo* __restrict__ tiles, const int2* __restrict__ items, int m,
+                 const int* __restrict__ map, const int* __restrict__ scol,
+                 const int* __restrict__ skip, const double2* __restrict__ Q,
+                 const double2* __restrict__ cvec, double2* __restrict__ psi) {
   __shared__ double2 cs[SPC_MAX_M][SPC_LANES];
+  const int2 it = items[blockIdx.x];
+  const TileInfo& T = tiles[it.x];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int w = blockIdx.x * SPC_LANES + tx;
-  const bool act = w < Ma;
+  const int w = it.x * SPC_LANES + tx;
+  const bool act = map[w] >= 0 && !skip[w];
   for (int j = ty; j < m; j += SPC_WARPS) cs[j][tx] = act ? cvec[(size_t)w * m + j] : cz();
   __syncthreads();
-  if (!act || skip[w]) return;
-  const int s = map[w];
-  const size_t qstride = (size_t)N * ld;
-  const int64_t r0 = (int64_t)blockIdx.y * rpb;
-  const int64_t r1 = min(N, r0 + rpb);
-  for (int64_t r = r0 + ty; r < r1; r += SPC_WARPS) {
+  if (!act) return;
+  const int n = T.n;
+  const size_t vs = (size_t)n * SPC_LANES;
+  const double2* q = Q + T.q_off + tx;
+  double2* dst = psi + T.psi_off + scol[w];
+  const int stride = T.nip * SPC_WARPS;
+  for (int r = it.y * SPC_WARPS + ty; r < n; r += stride) {
     double2 acc = cz();
-    const double2* q = Q + (size_t)r * ld + w;
-    for (int j = 0; j < m; ++j) acc = cfma(q[(size_t)j * qstride], cs[j][tx], acc);
-    psi[(size_t)r * ldp + s] = acc;
+    const double2* qr = q + (size_t)r * SPC_LANES;
+    for (int j = 0; j < m; ++j) acc = cfma(qr[(size_t)j * vs], cs[j][tx], acc);
+    dst[(size_t)r * T.ldp] = acc;
   }
 }
 
-// kron_vector(theta, Z_ket) for every sample (src/kroenecker.f90:85-97)
+// kron_vector(theta, Z_ket) for every sample of every job (src/kroenecker.f90:85-97)
 struct Theta {
   double2 v[4];
 };
-__global__ void k_kron_init(int64_t Z, int M, int ldp, Theta th, const double2* __restrict__ zk,
+struct JobInit {
+  int64_t Z, psi_off;
+  int M, ldp;
+  const double2* zk;  // M x Z, sample-major
+};
+__global__ void k_kron_init(const JobInit* __restrict__ jobs, int j0, Theta th,
                             double2* __restrict__ psi) {
-  const int64_t total = Z * (int64_t)M;
+  const JobInit J = jobs[j0 + blockIdx.y];
+  const int64_t total = J.Z * (int64_t)J.M;
+  double2* p = psi + J.psi_off;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    const int s = (int)(idx % M);
-    const int64_t n = idx / M;
-    const double2 z = zk[(size_t)s * Z + n];
+    const int s = (int)(idx % J.M);
+    const int64_t n = idx / J.M;
+    const double2 z = J.zk[(size_t)s * J.Z + n];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) psi[(size_t)(e * Z + n) * ldp + s] = cmul(th.v[e], z);
+    for (int e = 0; e < 4; ++e) p[(size_t)(e * J.Z + n) * J.ldp + s] = cmul(th.v[e], z);
   }
 }
 
-__global__ void k_obs_init(int M, int T, double p0, double p1, double p2, double p3,
+__global__ void k_obs_init(int G, int T, double p0, double p1, double p2, double p3,
                            double* __restrict__ obs, double* __restrict__ tt, int* __restrict__ kk,
                            int* __restrict__ done) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= M) return;
+  if (s >= G) return;
   double* o = obs + (size_t)s * 4 * T;
   o[0] = p0;
   o[T] = p1;
@@ -681,25 +753,20 @@ __global__ void k_obs_init(int M, int T, double p0, double p1, double p2, double
   done[s] = 0;
 }
 
-// res%update over samples in order, then res%scale(1/M)
-__global__ void k_average(int M, int T, const double* __restrict__ obs, double* __restrict__ out) {
+// res%update over a job's samples in order, then res%scale(1/M)
+struct JobOut {
+  int base, M;
+  double* out;  // 4*T
+};
+__global__ void k_average(const JobOut* __restrict__ jobs, int j0, int T,
+                          const double* __restrict__ obs) {
+  const JobOut J = jobs[j0 + blockIdx.y];
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= 4 * T) return;
   const int q = idx / T, t = idx % T;
   double acc = 0.0;
-  for (int s = 0; s < M; ++s) acc = acc + obs[((size_t)s * 4 + q) * T + t];
-  out[idx] = acc * (1.0 / (double)M);
-}
-
-// ---------------------------------------------------------------------------
-// Row blocks per sample tile so that the grid fills one wave of resident
-// CTAs (tiles x nrb <= resident), with at least 32 rows per block.
-static void geometry(int64_t N, int tiles, int resident, int& nrb, int& rpb) {
-  int64_t want = std::max<int64_t>(1, resident / tiles);
-  const int64_t maxb = std::max<int64_t>(1, (N + 31) / 32);
-  want = std::min(want, maxb);
-  rpb = (int)((N + want - 1) / want);
-  nrb = (int)((N + rpb - 1) / rpb);
+  for (int s = 0; s < J.M; ++s) acc = acc + obs[((size_t)(J.base + s) * 4 + q) * T + t];
+  J.out[idx] = acc * (1.0 / (double)J.M);
 }
 
 int num_time_points(double dt, double t_end) {
@@ -714,34 +781,72 @@ int num_time_points(double dt, double t_end) {
       return set_error(SPC_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
-int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev, int M,
-              double dt, double t_end, int m, double tol, double* out_dev, int T) {
+// Work items per tile, proportional to the tile's rows and summing to about
+// one wave of `resident` CTAs; at least 32 rows per item.
+static void plan_items(const std::vector<int>& tile_n, int resident, std::vector<int>& first,
+                       std::vector<int>& count, std::vector<int2>& items) {
+  int64_t W = 0;
+  for (int n : tile_n) W += n;
+  first.resize(tile_n.size());
+  count.resize(tile_n.size());
+  items.clear();
+  for (size_t t = 0; t < tile_n.size(); ++t) {
+    const int n = tile_n[t];
+    int64_t c = W > 0 ? (int64_t)n * resident / W : 1;
+    c = std::max<int64_t>(1, std::min<int64_t>(c, (n + 31) / 32));
+    first[t] = (int)items.size();
+    count[t] = (int)c;
+    for (int q = 0; q < c; ++q) items.push_back(make_int2((int)t, q));
+  }
+}
+
+int propagate_batch(Handle* h, const double* theta, const double* init_pop,
+                    const std::vector<JobSpec>& jobs, double dt, double t_end, int m, double tol,
+                    int T) {
   auto t_start = std::chrono::steady_clock::now();
-  const int64_t N = h->n, Z = N / 4;
   cudaStream_t st = h->stream;
-  const int ldp = (M + SPC_LANES - 1) / SPC_LANES * SPC_LANES;
-  const int ld = ldp;
+  const int nj = (int)jobs.size();
   const size_t mm = (size_t)m * m;
-  const int tiles_max = ld / SPC_LANES;
-  const int64_t pmax = std::min<int64_t>(std::max<int64_t>(1, (N + 31) / 32), (int64_t)h->sm_count * 32);
   const int ncombo = 4 * m * (m + 1) / 2;
-  // Z splits of the projector Grams (chosen per round, at most nsplit_max,
-  // at least 64 rows each); the partial buffer is sized for nsplit_max
-  const int nsplit_max = (int)std::max<int64_t>(1, std::min<int64_t>(16, (Z + 63) / 64));
-  const int nsplit = nsplit_max;
-  // buffers
-  if (h->ensure(h->psi, sizeof(double2) * N * ldp) || h->ensure(h->Q, sizeof(double2) * m * N * ld) ||
-      h->ensure(h->P, sizeof(double2) * N * ld) || h->ensure(h->partial, sizeof(double2) * pmax * ld) ||
-      h->ensure(h->counters, sizeof(unsigned) * tiles_max) || h->ensure(h->coef, sizeof(double2) * ld) ||
-      h->ensure(h->rbeta, sizeof(double) * ld) || h->ensure(h->Ahess, sizeof(double2) * mm * ld) ||
-      h->ensure(h->Aexp, sizeof(double2) * mm * ld) || h->ensure(h->proj, sizeof(double2) * 4 * mm * ld) ||
-      h->ensure(h->projpart, sizeof(double2) * (size_t)nsplit * ld * ncombo + sizeof(unsigned) * ncombo) ||
-      h->ensure(h->cvec, sizeof(double2) * m * ld) || h->ensure(h->tt, sizeof(double) * M) ||
-      h->ensure(h->kk, sizeof(int) * M) || h->ensure(h->done, sizeof(int) * M) ||
-      h->ensure(h->map, sizeof(int) * ld) || h->ensure(h->obs, sizeof(double) * 4 * (size_t)T * M) ||
-      h->ensure(h->err, 16) || h->ensure(h->flag, sizeof(int) * ld))
+  // job layout: psi blocks and global sample numbering
+  std::vector<int64_t> psi_off(nj);
+  std::vector<int> ldp(nj), base(nj);
+  int64_t psi_total = 0, qcap = 0, pcap = 0;
+  int G = 0, slots_cap = 0, tiles_cap = 0;
+  int64_t Zmax = 1;
+  for (int k = 0; k < nj; ++k) {
+    ldp[k] = (jobs[k].M + SPC_LANES - 1) / SPC_LANES * SPC_LANES;
+    psi_off[k] = psi_total;
+    psi_total += (int64_t)jobs[k].n * ldp[k];
+    qcap += (int64_t)m * jobs[k].n * ldp[k];
+    pcap += (int64_t)jobs[k].n * ldp[k];
+    base[k] = G;
+    G += jobs[k].M;
+    slots_cap += ldp[k];
+    tiles_cap += ldp[k] / SPC_LANES;
+    Zmax = std::max<int64_t>(Zmax, jobs[k].n / 4);
+  }
+  const int nsplit_max = (int)std::max<int64_t>(1, std::min<int64_t>(16, (Zmax + 63) / 64));
+  // upper bound on work items per round: one wave of the most resident kernel plus one per tile
+  const int items_cap = h->sm_count * 32 + tiles_cap;
+  if (h->ensure(h->psi, sizeof(double2) * psi_total) || h->ensure(h->Q, sizeof(double2) * qcap) ||
+      h->ensure(h->P, sizeof(double2) * pcap) ||
+      h->ensure(h->partial, sizeof(double2) * (size_t)items_cap * SPC_LANES) ||
+      h->ensure(h->counters, sizeof(unsigned) * tiles_cap) ||
+      h->ensure(h->coef, sizeof(double2) * slots_cap) || h->ensure(h->rbeta, sizeof(double) * slots_cap) ||
+      h->ensure(h->Ahess, sizeof(double2) * mm * slots_cap) ||
+      h->ensure(h->Aexp, sizeof(double2) * mm * slots_cap) ||
+      h->ensure(h->proj, sizeof(double2) * 4 * mm * slots_cap) ||
+      h->ensure(h->projpart, sizeof(double2) * (size_t)nsplit_max * slots_cap * ncombo +
+                                 sizeof(unsigned) * ncombo) ||
+      h->ensure(h->cvec, sizeof(double2) * m * slots_cap) || h->ensure(h->tt, sizeof(double) * G) ||
+      h->ensure(h->kk, sizeof(int) * G) || h->ensure(h->done, sizeof(int) * G) ||
+      h->ensure(h->obs, sizeof(double) * 4 * (size_t)T * G) || h->ensure(h->err, 16) ||
+      h->ensure(h->flag, sizeof(int) * slots_cap) ||
+      h->ensure(h->plan, sizeof(TileInfo) * tiles_cap + sizeof(int2) * 2 * items_cap +
+                             sizeof(int) * 2 * slots_cap + 256) ||
+      h->ensure(h->jobtab, (sizeof(JobInit) + sizeof(JobOut)) * nj + 64))
     return SPC_ERR_ALLOC;
-  int* d_flag = (int*)h->flag.p;
   double2* d_psi = (double2*)h->psi.p;
   double2* d_Q = (double2*)h->Q.p;
   double2* d_P = (double2*)h->P.p;
@@ -753,40 +858,60 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   double2* d_E = (double2*)h->Aexp.p;
   double2* d_proj = (double2*)h->proj.p;
   double2* d_ppart = (double2*)h->projpart.p;
-  unsigned* d_combos = (unsigned*)((char*)h->projpart.p + sizeof(double2) * (size_t)nsplit * ld * ncombo);
+  unsigned* d_combos =
+      (unsigned*)((char*)h->projpart.p + sizeof(double2) * (size_t)nsplit_max * slots_cap * ncombo);
   double2* d_c = (double2*)h->cvec.p;
   double* d_t = (double*)h->tt.p;
   int* d_k = (int*)h->kk.p;
   int* d_done = (int*)h->done.p;
-  int* d_map = (int*)h->map.p;
   double* d_obs = (double*)h->obs.p;
   int* d_err = (int*)h->err.p;
   long long* d_nsteps = (long long*)((char*)h->err.p + 8);
+  int* d_flag = (int*)h->flag.p;
+  // per-round plan: tiles | pass items | SpMM items | map | scol
+  char* plan = (char*)h->plan.p;
+  TileInfo* d_tiles = (TileInfo*)plan;
+  int2* d_items_p = (int2*)(plan + sizeof(TileInfo) * tiles_cap);
+  int2* d_items_s = d_items_p + items_cap;
+  int* d_map = (int*)(d_items_s + items_cap);
+  int* d_scol = d_map + slots_cap;
+  JobInit* d_jinit = (JobInit*)h->jobtab.p;
+  JobOut* d_jout = (JobOut*)((char*)h->jobtab.p + sizeof(JobInit) * nj);
 
   int64_t launches0 = h->launches;
-  CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * tiles_max, st));
+  CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * tiles_cap, st));
   CK(cudaMemsetAsync(h->err.p, 0, 16, st));
-  CK(cudaMemsetAsync(d_obs, 0, sizeof(double) * 4 * (size_t)T * M, st));
-  if (ldp != M) CK(cudaMemsetAsync(d_psi, 0, sizeof(double2) * N * ldp, st));
+  CK(cudaMemsetAsync(d_obs, 0, sizeof(double) * 4 * (size_t)T * G, st));
+  CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * slots_cap, st));
+  CK(cudaMemsetAsync(d_psi, 0, sizeof(double2) * psi_total, st));
   {
     std::vector<unsigned> combos(ncombo);
     int id = 0;
     for (int t = 0; t < 4; ++t)
       for (int i = 0; i < m; ++i)
         for (int j = i; j < m; ++j) combos[id++] = ((unsigned)t << 16) | ((unsigned)i << 8) | (unsigned)j;
+    std::vector<JobInit> ji(nj);
+    std::vector<JobOut> jo(nj);
+    for (int k = 0; k < nj; ++k) {
+      ji[k] = JobInit{jobs[k].n / 4, psi_off[k], jobs[k].M, ldp[k], jobs[k].zk};
+      jo[k] = JobOut{base[k], jobs[k].M, jobs[k].out};
+    }
     CK(cudaMemcpyAsync(d_combos, combos.data(), sizeof(unsigned) * ncombo, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_jinit, ji.data(), sizeof(JobInit) * nj, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_jout, jo.data(), sizeof(JobOut) * nj, cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
   }
   Theta th;
   for (int e = 0; e < 4; ++e) th.v[e] = make_double2(theta[2 * e], theta[2 * e + 1]);
-  {
-    const int64_t tot = Z * (int64_t)M;
-    const int blocks = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)h->sm_count * 16);
-    k_kron_init<<<std::max(blocks, 1), 256, 0, st>>>(Z, M, ldp, th, (const double2*)zk_dev, d_psi);
+  for (int j0 = 0; j0 < nj; j0 += 65535) {
+    const int cnt = std::min(65535, nj - j0);
+    k_kron_init<<<dim3(std::max(1, h->sm_count * 8 / std::max(1, cnt)), cnt), 256, 0, st>>>(
+        d_jinit, j0, th, d_psi);
+    h->count_launch();
   }
-  k_obs_init<<<(M + 127) / 128, 128, 0, st>>>(M, T, init_pop[0], init_pop[1], init_pop[2],
+  k_obs_init<<<(G + 127) / 128, 128, 0, st>>>(G, T, init_pop[0], init_pop[1], init_pop[2],
                                                init_pop[3], d_obs, d_t, d_k, d_done);
-  h->count_launch(2);
+  h->count_launch();
   CK(cudaGetLastError());
 
   const size_t expm_smem = sizeof(double2) * 5 * mm;
@@ -796,7 +921,7 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   const void* proj_fn = maxc <= 8 ? (const void*)k_proj<8> : maxc <= 16 ? (const void*)k_proj<16>
                                                                          : (const void*)k_proj<24>;
   CK(cudaFuncSetAttribute(proj_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)proj_smem));
-  // resident CTAs per kernel: grids are sized to whole waves
+  // resident CTAs per kernel: item lists are sized to whole waves
   auto resident = [&](const void* fn, int threads, size_t smem) {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, threads, smem) != cudaSuccess) b = 1;
@@ -805,86 +930,130 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   const int res_spmm = resident((const void*)k_spmm, 256, 0);
   const int res_pass = std::min(resident((const void*)k_rowpass<PASS_AXPY_DOT>, 256, 0),
                                 resident((const void*)k_rowpass<PASS_AXPY_NORM>, 256, 0));
-  const int res_scale = resident((const void*)k_scale, 256, 0);
-  const int res_psi = resident((const void*)k_psi_update, 256, 0);
   const int res_proj = resident(proj_fn, 256, proj_smem);
 
   std::vector<int> active;
   if (0.0 < t_end)
-    for (int s = 0; s < M; ++s) active.push_back(s);
-  std::vector<int> done_h(M, 0), flag_h(ld, 0);
+    for (int g = 0; g < G; ++g) active.push_back(g);
+  std::vector<int> job_of(G);
+  for (int k = 0; k < nj; ++k)
+    for (int s = 0; s < jobs[k].M; ++s) job_of[base[k] + s] = k;
+  std::vector<int> done_h(G, 0), flag_h(slots_cap, 0);
   int64_t builds = 0, rounds = 0, fallbacks = 0;
   const dim3 blk(SPC_LANES, SPC_WARPS);
-  const bool use_lanczos = h->lanczos_active();
+  bool lanczos_ok = h->krylov_method == 1 || h->krylov_method == 2;
+  for (const JobSpec& j : jobs) lanczos_ok = lanczos_ok && j.herm_shift;
+  std::vector<char> hplan;
 
-  // One build round for the samples in `list`: Krylov basis (Lanczos or full
-  // MGS), expm, projectors; then the dt loop and psi = Q c for every sample
-  // whose basis passed the orthogonality check. Returns the samples that
-  // failed it (Lanczos only); their state is left untouched.
+  // One build round for the samples in `list` (global indices, job order):
+  // Krylov basis (Lanczos or full MGS), expm, projectors; then the dt loop and
+  // psi = Q c for every sample whose basis passed the orthogonality check.
+  // Returns the samples that failed it (Lanczos only); their state is left
+  // untouched.
   auto round = [&](const std::vector<int>& list, bool lanczos, std::vector<int>& failed) -> int {
     failed.clear();
-    const int Ma = (int)list.size();
-    const int tiles = (Ma + SPC_LANES - 1) / SPC_LANES;
-    int nrb, rpb, nrb_s, rpb_s, nrb_c, rpb_c, nrb_u, rpb_u;
-    geometry(N, tiles, res_pass, nrb, rpb);
-    geometry(N, tiles, res_spmm, nrb_s, rpb_s);
-    geometry(N, tiles, res_scale, nrb_c, rpb_c);
-    geometry(N, tiles, res_psi, nrb_u, rpb_u);
-    const dim3 grid(tiles, nrb), grid_s(tiles, nrb_s), grid_c(tiles, nrb_c), grid_u(tiles, nrb_u);
-    // projector split: the count in [1, nsplit_max] whose grid wastes the
-    // least of its last wave
-    int ns = 1;
-    {
-      double best = 1e30;
-      for (int c = 1; c <= nsplit_max; ++c) {
-        const double waves = (double)Ma * c / res_proj;
-        const double loss = std::ceil(waves) / waves - 1.0 + 0.002 * c;
-        if (loss < best) {
-          best = loss;
-          ns = c;
+    // tiles: each job's samples in this list, in groups of 32
+    std::vector<TileInfo> tiles;
+    std::vector<int> map, scol, tile_n;
+    int64_t qo = 0, po = 0;
+    size_t a = 0;
+    double elems = 0.0;
+    while (a < list.size()) {
+      const int k = job_of[list[a]];
+      size_t b = a;
+      while (b < list.size() && job_of[list[b]] == k) ++b;
+      for (size_t c = a; c < b; c += SPC_LANES) {
+        TileInfo ti{};
+        ti.job = k;
+        ti.n = jobs[k].n;
+        ti.ldp = ldp[k];
+        ti.q_off = qo;
+        ti.p_off = po;
+        ti.psi_off = psi_off[k];
+        ti.rowptr = jobs[k].rowptr;
+        ti.split = jobs[k].split;
+        ti.col = jobs[k].col;
+        ti.val = jobs[k].val;
+        qo += (int64_t)m * ti.n * SPC_LANES;
+        po += (int64_t)ti.n * SPC_LANES;
+        for (int l = 0; l < SPC_LANES; ++l) {
+          if (c + l < b) {
+            map.push_back(list[c + l]);
+            scol.push_back(list[c + l] - base[k]);
+          } else {
+            map.push_back(-1);
+            scol.push_back(-1);
+          }
         }
+        elems += (double)ti.n * (double)std::min<size_t>(SPC_LANES, b - c);
+        tiles.push_back(ti);
+        tile_n.push_back(ti.n);
       }
+      a = b;
     }
-    CK(cudaMemcpyAsync(d_map, list.data(), sizeof(int) * Ma, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(d_A, 0, sizeof(double2) * mm * Ma, st));
-    CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * ld, st));
-    PassArgs a{};
-    a.N = N;
-    a.ld = ld;
-    a.Ma = Ma;
-    a.rpb = rpb;
-    a.m = m;
-    a.map = d_map;
-    a.ldp = ldp;
-    a.coef = d_coef;
-    a.rbeta = d_rb;
-    a.Ahess = d_A;
-    a.cvec = d_c;
-    a.partial = d_part;
-    a.counters = d_cnt;
-    a.P = d_P;
-    a.lanczos = lanczos ? 1 : 0;
-    // c = ||psi|| e1 ; Q0 = psi/||psi||
-    a.X = d_psi;
-    const double elems = (double)N * Ma;
+    const int ntiles = (int)tiles.size();
+    const int nslots = ntiles * SPC_LANES;
+    std::vector<int> fp, cp, fs, cs;
+    std::vector<int2> items_p, items_s;
+    plan_items(tile_n, res_pass, fp, cp, items_p);
+    plan_items(tile_n, res_spmm, fs, cs, items_s);
+    for (int t = 0; t < ntiles; ++t) {
+      tiles[t].ip0 = fp[t];
+      tiles[t].nip = cp[t];
+      tiles[t].is0 = fs[t];
+      tiles[t].nis = cs[t];
+    }
+    const int nip = (int)items_p.size(), nis = (int)items_s.size();
+    if (nip > items_cap || nis > items_cap || ntiles > tiles_cap)
+      return set_error(SPC_ERR_ARG, "internal: work plan exceeds its buffer");
+    // one host->device copy of the plan
+    const size_t off_items_p = sizeof(TileInfo) * tiles_cap;
+    const size_t off_items_s = off_items_p + sizeof(int2) * items_cap;
+    const size_t off_map = off_items_s + sizeof(int2) * items_cap;
+    const size_t off_scol = off_map + sizeof(int) * slots_cap;
+    const size_t plan_bytes = off_scol + sizeof(int) * nslots;
+    hplan.resize(plan_bytes);
+    std::memcpy(hplan.data(), tiles.data(), sizeof(TileInfo) * ntiles);
+    std::memcpy(hplan.data() + off_items_p, items_p.data(), sizeof(int2) * nip);
+    std::memcpy(hplan.data() + off_items_s, items_s.data(), sizeof(int2) * nis);
+    std::memcpy(hplan.data() + off_map, map.data(), sizeof(int) * nslots);
+    std::memcpy(hplan.data() + off_scol, scol.data(), sizeof(int) * nslots);
+    CK(cudaMemcpyAsync(plan, hplan.data(), plan_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(d_A, 0, sizeof(double2) * mm * nslots, st));
+    CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * nslots, st));
+    PassArgs pa{};
+    pa.tiles = d_tiles;
+    pa.items = d_items_p;
+    pa.m = m;
+    pa.Q = d_Q;
+    pa.P = d_P;
+    pa.psi = d_psi;
+    pa.map = d_map;
+    pa.scol = d_scol;
+    pa.coef = d_coef;
+    pa.rbeta = d_rb;
+    pa.Ahess = d_A;
+    pa.cvec = d_c;
+    pa.partial = d_part;
+    pa.counters = d_cnt;
+    pa.lanczos = lanczos ? 1 : 0;
+    int64_t nnz_work = 0;
+    for (const TileInfo& ti : tiles) nnz_work += (int64_t)(jobs[ti.job].nnz);
     int pe = h->prof.begin(st);
-    k_rowpass<PASS_NORM_GATHER><<<grid, blk, 0, st>>>(a);
+    k_rowpass<PASS_NORM_GATHER><<<nip, blk, 0, st>>>(pa);
     h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
     pe = h->prof.begin(st);
-    k_scale<<<grid_c, blk, 0, st>>>(N, ld, Ma, rpb_c, d_psi, ldp, d_map, 1, d_rb, d_Q);
+    k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 1, 0, d_rb, d_Q);
     h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
     h->count_launch(2);
-    const size_t qs = (size_t)N * ld;
     for (int i = 0; i < m; ++i) {
-      const double2* Qi = d_Q + (size_t)i * qs;
       pe = h->prof.begin(st);
-      k_spmm<<<grid_s, blk, 0, st>>>(N, ld, Ma, rpb_s, h->d_rowptr, (const int*)h->xsplit.p,
-                                     (const int*)h->xcol.p, (const double2*)h->xval.p, Qi, d_P);
-      // algorithmic traffic: H once, X once, Y once
-      h->prof.end(st, pe, PK_SPMM, 8.0 * (double)h->nnz * Ma,
-                  20.0 * (double)h->nnz + 4.0 * (N + 1) + 32.0 * elems);
+      k_spmm<<<nis, blk, 0, st>>>(d_tiles, d_items_s, d_map, i, d_Q, d_P);
+      // algorithmic traffic: H once per tile, X once, Y once
+      h->prof.end(st, pe, PK_SPMM, 8.0 * (double)nnz_work * SPC_LANES,
+                  20.0 * (double)nnz_work + 32.0 * elems);
       h->count_launch();
-      a.col_i = i;
+      pa.col_i = i;
       // MGS (get_krylov :453-456) projects p on Q_0..Q_i in order. Lanczos
       // (H_eff Hermitian up to -i*kappa) needs only Q_{i-1} (coefficient
       // beta_{i-1}, already in coef) and Q_i.
@@ -892,72 +1061,90 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
       if (lanczos && i > 0) {
         j0 = i - 1;
       } else {
-        a.row_j = 0;
-        a.X = d_Q;
+        pa.row_j = 0;
+        pa.jx = 0;
         pe = h->prof.begin(st);
-        k_rowpass<PASS_DOT><<<grid, blk, 0, st>>>(a);
+        k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
         h->prof.end(st, pe, PK_DOT, 8.0 * elems, 32.0 * elems);
         h->count_launch();
       }
       for (int j = j0; j < i; ++j) {
-        a.Qj = d_Q + (size_t)j * qs;
-        a.Qn = d_Q + (size_t)(j + 1) * qs;
-        a.row_j = j + 1;
+        pa.jx = j;
+        pa.jn = j + 1;
+        pa.row_j = j + 1;
         pe = h->prof.begin(st);
-        k_rowpass<PASS_AXPY_DOT><<<grid, blk, 0, st>>>(a);
+        k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
         h->prof.end(st, pe, PK_AXPY_DOT, 16.0 * elems, 64.0 * elems);
         h->count_launch();
       }
       if (i < m - 1) {
-        a.Qj = Qi;
-        a.row_j = i + 1;
+        pa.jx = i;
+        pa.row_j = i + 1;
         pe = h->prof.begin(st);
-        k_rowpass<PASS_AXPY_NORM><<<grid, blk, 0, st>>>(a);
+        k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
         h->prof.end(st, pe, PK_AXPY_NORM, 12.0 * elems, 48.0 * elems);
         pe = h->prof.begin(st);
-        k_scale<<<grid_c, blk, 0, st>>>(N, ld, Ma, rpb_c, d_P, ldp, d_map, 0, d_rb,
-                                          d_Q + (size_t)(i + 1) * qs);
+        k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 0, i + 1, d_rb,
+                                     d_Q);
         h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
         h->count_launch(2);
       }
     }
+    double zsum = 0.0;  // sum over active slots of Z
+    for (size_t c = 0; c < map.size(); ++c)
+      if (map[c] >= 0) zsum += tiles[c / SPC_LANES].n / 4;
     pe = h->prof.begin(st);
-    k_expm<<<Ma, 128, expm_smem, st>>>(m, Ma, d_A, d_E, dt, d_err);
-    h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * Ma, 32.0 * (double)mm * Ma);
-    const dim3 pgrid(Ma, ns);
+    k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, d_map, d_A, d_E, dt, d_err);
+    h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * list.size(),
+                32.0 * (double)mm * list.size());
+    // projector split: the count in [1, nsplit_max] whose grid wastes the
+    // least of its last wave
+    int ns = 1;
+    {
+      double best = 1e30;
+      for (int c = 1; c <= nsplit_max; ++c) {
+        const double waves = (double)list.size() * c / res_proj;
+        const double loss = std::ceil(waves) / waves - 1.0 + 0.002 * c;
+        if (loss < best) {
+          best = loss;
+          ns = c;
+        }
+      }
+    }
+    const dim3 pgrid(nslots, ns);
     pe = h->prof.begin(st);
     if (maxc <= 8)
-      k_proj<8><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, ns, d_ppart);
+      k_proj<8><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, d_ppart);
     else if (maxc <= 16)
-      k_proj<16><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, ns, d_ppart);
+      k_proj<16><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, d_ppart);
     else
-      k_proj<24><<<pgrid, 256, proj_smem, st>>>(N, Z, ld, m, ncombo, d_combos, d_Q, ns, d_ppart);
-    h->prof.end(st, pe, PK_PROJ, 8.0 * (double)ncombo * Z * Ma + 4.0 * (double)m * Z * Ma,
-                16.0 * (double)m * N * Ma);
+      k_proj<24><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, d_ppart);
+    h->prof.end(st, pe, PK_PROJ, 8.0 * (double)ncombo * zsum + 4.0 * (double)m * zsum,
+                64.0 * (double)m * zsum);
     {
-      const int64_t tot = (int64_t)Ma * ncombo;
+      const int64_t tot = (int64_t)nslots * ncombo;
       pe = h->prof.begin(st);
-      k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(Ma, m, ncombo, ns, d_combos, d_ppart,
-                                                             d_proj);
+      k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(nslots, d_map, m, ncombo, ns, d_combos,
+                                                             d_ppart, d_proj);
       h->prof.end(st, pe, PK_PROJ_REDUCE, 2.0 * tot * ns, 16.0 * tot * (ns + 1));
       h->count_launch(3);
     }
     if (lanczos) {
       // G = Q^H Q = Tp + S + T0 + Tm; a basis that drifted from orthonormal
       // beyond ORTHO_TOL is rebuilt with full MGS
-      k_ortho_check<<<Ma, 128, 0, st>>>(m, Ma, d_proj, ORTHO_TOL, d_flag);
+      k_ortho_check<<<nslots, 128, 0, st>>>(m, d_map, d_proj, ORTHO_TOL, d_flag);
       h->count_launch();
-      CK(cudaMemcpyAsync(flag_h.data(), d_flag, sizeof(int) * Ma, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(flag_h.data(), d_flag, sizeof(int) * nslots, cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      for (int w = 0; w < Ma; ++w)
-        if (flag_h[w]) failed.push_back(list[w]);
+      for (int w = 0; w < nslots; ++w)
+        if (map[w] >= 0 && flag_h[w]) failed.push_back(map[w]);
     }
     pe = h->prof.begin(st);
-    k_dtloop<<<(Ma + 3) / 4, 128, 0, st>>>(m, Ma, T, d_map, d_flag, d_E, d_proj, d_c, d_t, d_k, d_done,
-                                           d_obs, dt, t_end, tol, d_nsteps, d_err);
+    k_dtloop<<<(nslots + 3) / 4, 128, 0, st>>>(m, nslots, T, d_map, d_flag, d_E, d_proj, d_c, d_t,
+                                               d_k, d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
     h->prof.end(st, pe, PK_DTLOOP, 0.0, 0.0);
     pe = h->prof.begin(st);
-    k_psi_update<<<grid_u, blk, 0, st>>>(N, ld, Ma, rpb_u, m, d_map, d_flag, ldp, d_Q, d_c, d_psi);
+    k_psi_update<<<nip, blk, 0, st>>>(d_tiles, d_items_p, m, d_map, d_scol, d_flag, d_Q, d_c, d_psi);
     h->prof.end(st, pe, PK_PSI, 8.0 * m * elems, 16.0 * (m + 1) * elems);
     h->count_launch(2);
     CK(cudaGetLastError());
@@ -966,7 +1153,7 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
 
   std::vector<int> failed, failed2;
   while (!active.empty()) {
-    int rc = round(active, use_lanczos, failed);
+    int rc = round(active, lanczos_ok, failed);
     if (rc) return rc;
     builds += (int64_t)active.size() - (int64_t)failed.size();
     if (!failed.empty()) {
@@ -975,18 +1162,21 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
       if (rc) return rc;
       builds += (int64_t)failed.size();
     }
-    CK(cudaMemcpyAsync(done_h.data(), d_done, sizeof(int) * M, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(done_h.data(), d_done, sizeof(int) * G, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     h->prof.collect();
     rounds++;
     std::vector<int> next;
     next.reserve(active.size());
-    for (int s : active)
-      if (!done_h[s]) next.push_back(s);
+    for (int g : active)
+      if (!done_h[g]) next.push_back(g);
     active.swap(next);
   }
-  k_average<<<(4 * T + 255) / 256, 256, 0, st>>>(M, T, d_obs, out_dev);
-  h->count_launch();
+  for (int j0 = 0; j0 < nj; j0 += 65535) {
+    const int cnt = std::min(65535, nj - j0);
+    k_average<<<dim3((4 * T + 255) / 256, cnt), 256, 0, st>>>(d_jout, j0, T, d_obs);
+    h->count_launch();
+  }
   CK(cudaGetLastError());
   int err_h[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(err_h, h->err.p, 16, cudaMemcpyDeviceToHost, st));
@@ -1005,6 +1195,23 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   if (err_h[0] == 2)
     return set_error(SPC_ERR_NUMERIC, "singular Pade denominator in expm");
   return SPC_OK;
+}
+
+// The single-Hamiltonian call: one job on the handle's Hamiltonian.
+int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev, int M,
+              double dt, double t_end, int m, double tol, double* out_dev, int T) {
+  JobSpec j{};
+  j.n = h->n;
+  j.nnz = h->nnz;
+  j.M = M;
+  j.rowptr = h->d_rowptr;
+  j.split = (const int*)h->xsplit.p;
+  j.col = (const int*)h->xcol.p;
+  j.val = (const double2*)h->xval.p;
+  j.zk = (const double2*)zk_dev;
+  j.out = out_dev;
+  j.herm_shift = h->herm_shift;
+  return propagate_batch(h, theta, init_pop, std::vector<JobSpec>{j}, dt, t_end, m, tol, T);
 }
 
 }  // namespace spc

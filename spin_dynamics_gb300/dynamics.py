@@ -198,6 +198,53 @@ class TraceSampler:
             self._h, _dptr(th), _dptr(pop), C.c_void_p(zkets_ptr), int(M), float(dt),
             float(t_end), int(m), float(tol), C.c_void_p(out_ptr), T))
 
+    # ---- batches ----
+    def build_h_batch(self, systems, fields, mode: str = "reference") -> list:
+        """Build one Hamiltonian per (system, field) pair and keep them as
+        the handle's batch. Returns the dimensions."""
+        m = {"reference": nat.SPC_H_REFERENCE, "general": nat.SPC_H_GENERAL}[mode]
+        structs, keep = [], []
+        for s, B in zip(systems, fields):
+            st, k = make_system(s, B)
+            structs.append(st)
+            keep.append(k)
+        arr = (nat.spc_system * len(structs))(*structs)
+        nat.check(nat.lib().spc_build_h_batch(self._h, len(structs), C.cast(arr, C.c_void_p), m))
+        return [4 * s.Z for s in systems]
+
+    def trace_sampling_batch(self, zkets_list, dt: float, t_end: float, m: int, tol: float,
+                             init_state: str = "singlet", job_sys=None) -> list:
+        """Propagate job k's M_k x Z_k vectors under batch system job_sys[k]
+        (default k) together; returns one Observables per job."""
+        M = np.array([z.shape[0] for z in zkets_list], np.int32)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(z, np.complex128).reshape(-1)
+                                                    for z in zkets_list]))
+        th, pop = init_el_state(init_state)
+        th = np.ascontiguousarray(th).view(np.float64)
+        T = max(num_time_points(dt, t_end), 1)
+        out = np.zeros(len(zkets_list) * 4 * T)
+        js = None if job_sys is None else np.ascontiguousarray(job_sys, np.int32)
+        nat.check(nat.lib().spc_trace_sampling_batch(
+            self._h, len(zkets_list), _dptr(js) if js is not None else None, _dptr(M), _dptr(th),
+            _dptr(pop), _dptr(flat.view(np.float64)), float(dt), float(t_end), int(m), float(tol),
+            _dptr(out), T))
+        out = out.reshape(len(zkets_list), 4, T)
+        return [Observables(o[0].copy(), o[1].copy(), o[2].copy(), o[3].copy()) for o in out]
+
+    def trace_sampling_batch_device(self, zk_ptr: int, M, dt: float, t_end: float, m: int,
+                                    tol: float, out_ptr: int, init_state: str = "singlet",
+                                    job_sys=None) -> None:
+        """Device-resident batch: zk_ptr -> the jobs' sample blocks back to
+        back, out_ptr -> n_jobs x 4 x T float64."""
+        M = np.ascontiguousarray(M, np.int32)
+        th, pop = init_el_state(init_state)
+        th = np.ascontiguousarray(th).view(np.float64)
+        T = num_time_points(dt, t_end)
+        js = None if job_sys is None else np.ascontiguousarray(job_sys, np.int32)
+        nat.check(nat.lib().spc_trace_sampling_batch_device(
+            self._h, len(M), _dptr(js) if js is not None else None, _dptr(M), _dptr(th), _dptr(pop),
+            C.c_void_p(zk_ptr), float(dt), float(t_end), int(m), float(tol), C.c_void_p(out_ptr), T))
+
     def stats(self) -> dict:
         s = nat.spc_stats()
         nat.check(nat.lib().spc_get_stats(self._h, C.byref(s)))

@@ -1,0 +1,92 @@
+"""Batched propagation of independent systems of uneven dimension (pairs,
+field orientations) in one call, against the oracle per job."""
+import numpy as np
+import pytest
+
+from conftest import general_csr, iso_csr
+from spin_dynamics_gb300 import workloads as W
+from spin_dynamics_gb300.spinsys import GAMMA_E
+
+ABS_TOL = 1e-10
+pytestmark = pytest.mark.gpu
+DT = 1.0 * GAMMA_E / 1000
+
+
+def fib_sphere(n, r=0.05):
+    i = np.arange(n) + 0.5
+    phi = np.arccos(1 - 2 * i / n)
+    th = np.pi * (1 + 5 ** 0.5) * i
+    return r * np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], 1)
+
+
+def _check(got, ref):
+    for k in ("P_S", "P_T0", "P_Tp", "P_Tm"):
+        assert np.max(np.abs(getattr(got, k) - ref[k])) <= ABS_TOL, k
+
+
+@pytest.mark.parametrize("method", ["mgs", "auto"])
+def test_uneven_pairs_in_one_batch(sampler, oracle, method):
+    iso_large, B = W.large_pair(isotropic=True)
+    systems = [W.notebook_pair(), W.small_pair(), iso_large, W.small_pair()]
+    fields = [0.2, 0.05, B[2], 0.3]
+    for s in systems:
+        s.kS = s.kT = 1.0 / GAMMA_E
+    Ms = [5, 40, 3, 33]
+    zks = [W.random_phase_samples(s.Z, M, seed=10 + i) for i, (s, M) in enumerate(zip(systems, Ms))]
+    t_end = 30 * DT
+    sampler.set_krylov(method)
+    try:
+        sampler.build_h_batch(systems, fields, "reference")
+        got = sampler.trace_sampling_batch(zks, DT, t_end, 12, 1e-6)
+    finally:
+        sampler.set_krylov("mgs")
+    for s, f, zk, g in zip(systems, fields, zks, got):
+        rp, col, val = iso_csr(oracle, s, f)
+        _check(g, oracle.trace_sampling(rp, col, val, zk, DT, t_end, 12, 1e-6))
+
+
+def test_orientation_scan_batch_equals_single_calls(sampler, oracle):
+    rng = np.random.default_rng(8)
+    s = W.small_pair()
+    for e in (s.e1, s.e2):
+        e.A = [(lambda R: R @ np.diag(rng.uniform(-2, 2, 3)) @ R.T)(W._haar_rotation(rng)) for _ in e.A]
+    s.J, s.D = 0.01, W.axial_dipolar(-0.4)
+    dirs = fib_sphere(6)
+    zk = W.random_phase_samples(s.Z, 32, seed=2)
+    t_end = 25 * DT
+    sampler.build_h_batch([s] * len(dirs), list(dirs), "general")
+    got = sampler.trace_sampling_batch([zk] * len(dirs), DT, t_end, 16, 1e-5)
+    for b, g in zip(dirs, got):
+        rp, col, val = general_csr(oracle, s, b)
+        _check(g, oracle.trace_sampling(rp, col, val, zk, DT, t_end, 16, 1e-5))
+        sampler.build_h(s, b, "general")
+        single = sampler.trace_sampling(zk, DT, t_end, 16, 1e-5)
+        for k in ("P_S", "P_Tm"):
+            assert np.max(np.abs(getattr(single, k) - getattr(g, k))) < 1e-13
+
+
+def test_jobs_sharing_a_system(sampler, oracle):
+    s = W.small_pair()
+    sampler.build_h_batch([s], [0.05], "reference")
+    za = W.random_phase_samples(s.Z, 7, seed=1)
+    zb = W.random_phase_samples(s.Z, 9, seed=2)
+    got = sampler.trace_sampling_batch([za, zb], DT, 20 * DT, 10, 1e-6, job_sys=[0, 0])
+    rp, col, val = iso_csr(oracle, s, 0.05)
+    _check(got[0], oracle.trace_sampling(rp, col, val, za, DT, 20 * DT, 10, 1e-6))
+    _check(got[1], oracle.trace_sampling(rp, col, val, zb, DT, 20 * DT, 10, 1e-6))
+
+
+def test_mixed_rates_batch_uses_mgs(sampler, oracle):
+    a, b = W.small_pair(), W.small_pair()
+    b.kT = b.kS * 0.2  # not Hermitian plus a scalar
+    zk = W.random_phase_samples(a.Z, 6, seed=3)
+    sampler.set_krylov("auto")
+    try:
+        sampler.build_h_batch([a, b], [0.05, 0.05], "reference")
+        got = sampler.trace_sampling_batch([zk, zk], DT, 15 * DT, 10, 1e-6)
+        assert sampler.stats()["lanczos_fallbacks"] == 0
+    finally:
+        sampler.set_krylov("mgs")
+    for s, g in ((a, got[0]), (b, got[1])):
+        rp, col, val = iso_csr(oracle, s, 0.05)
+        _check(g, oracle.trace_sampling(rp, col, val, zk, DT, 15 * DT, 10, 1e-6))
