@@ -59,6 +59,11 @@ def parse():
     p.add_argument("--cpu-samples", type=int, default=0, help="CPU sample size (0 = 12 x cores)")
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-batch", action="store_true", help="skip the batched uneven-set leg")
+    p.add_argument("--batch-pairs", type=int, default=16)
+    p.add_argument("--batch-orient", type=int, default=4)
+    p.add_argument("--batch-window-ns", type=float, default=20.0)
+    p.add_argument("--batch-krylov", type=int, default=20)
     return p.parse_args()
 
 
@@ -255,11 +260,72 @@ def run_ours(args, rank, world, local_rank):
         e2e = {"value": world * M * steps_per_sample / el, "unit": "sample-steps/s",
                "h2d_bytes_per_step": int(zk_host.nbytes), "d2h_bytes_per_step": int(4 * T * 8),
                "ms_per_step": el * 1e3}
+    batched = None if args.no_batch else batched_leg(args, sampler, local_rank)
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
-    return dict(ms=ms, value=value, e2e=e2e, prof=prof, clocks=clk.summary(), launches=launches,
+    return dict(ms=ms, value=value, e2e=e2e, batched=batched, prof=prof, clocks=clk.summary(), launches=launches,
                 builds=builds, fallbacks=fallbacks, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
                 sysp=sysp, B=B, sim=sim)
+
+
+def batched_leg(args, sampler, local_rank):
+    """The uneven set: pairs of dims 16..9216 x field orientations, every job
+    with its own Hamiltonian and 32-256 samples. Times one batched call
+    (spc_build_h_batch + spc_trace_sampling_batch_device) against the same
+    jobs as per-instance calls (spc_build_h + spc_trace_sampling_device)."""
+    import torch
+
+    from spin_dynamics_gb300.dynamics import num_time_points
+
+    pairs = W.uneven_pairs(args.batch_pairs)
+    dirs = W.fibonacci_sphere(args.batch_orient)
+    systems, fields, zks, Ms = [], [], [], []
+    for p, (s, M) in enumerate(pairs):
+        for d in dirs:
+            systems.append(s)
+            fields.append(d)
+            zks.append(W.random_phase_samples(s.Z, M, seed=100 + p))
+            Ms.append(M)
+    dt = 1.0 * 176.08596 / 1000
+    t_end = args.batch_window_ns * 176.08596 / 1000
+    m = args.batch_krylov
+    T = num_time_points(dt, t_end)
+    offs = np.cumsum([0] + [z.size for z in zks])
+    zk_dev = torch.from_numpy(np.concatenate([z.reshape(-1) for z in zks])).to(f"cuda:{local_rank}")
+    out_dev = torch.empty(len(zks) * 4 * T, dtype=torch.float64, device=f"cuda:{local_rank}")
+    stream = torch.cuda.current_stream()
+
+    def per_instance():
+        for k in range(len(zks)):
+            sampler.build_h(systems[k], fields[k], "general")
+            sampler.trace_sampling_device(zk_dev.data_ptr() + 16 * int(offs[k]), Ms[k], dt, t_end, m,
+                                          1e-5, out_dev.data_ptr() + 8 * k * 4 * T)
+
+    def batched():
+        sampler.build_h_batch(systems, fields, "general")
+        sampler.trace_sampling_batch_device(zk_dev.data_ptr(), Ms, dt, t_end, m, 1e-5, out_dev.data_ptr())
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    steps = int(round(t_end / dt))
+    work = sum(Ms) * steps
+    t_single = timed(per_instance)
+    t_batch = timed(batched)
+    dims = [4 * s.Z for s in systems]
+    return {"value": work / t_batch, "per_instance_value": work / t_single,
+            "ratio": t_single / t_batch, "unit": "sample-steps/s", "jobs": len(zks),
+            "pairs": len(pairs), "orientations": len(dirs), "dims": [min(dims), max(dims)],
+            "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m,
+            "workload": "uneven pairs (2-10 nuclei from 1H/14N, anisotropic) x Fibonacci-sphere "
+                        "orientations at 0.05 mT, own Hamiltonian per job"}
 
 
 def main():
@@ -331,7 +397,7 @@ def main():
                           "fp64": {"achieved_tflops": ach_tf, "peak_tflops": r["fp64_peak"] / 1e12,
                                    "frac": (ach_tf * 1e12 / r["fp64_peak"]) if ach_tf else None,
                                    "peak_source": "measured DFMA probe (spc_fp64_peak)"}},
-                kernel_share=share, cpu_baseline=cpu)
+                kernel_share=share, batched=r["batched"], cpu_baseline=cpu)
     print(json.dumps(line))
 
 

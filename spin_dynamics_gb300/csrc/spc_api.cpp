@@ -204,7 +204,6 @@ static int check_prop_args(spc_handle* h, const double* theta, const double* ini
   if (M < 1) return spc::set_error(SPC_ERR_ARG, "need at least one sample");
   if (!(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt must be positive");
   if (m < 1 || m > 48) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d outside [1, 48]", m);
-  if (m > h->h.n) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d exceeds the Hilbert dimension %d", m, h->h.n);
   if (T < 1) return spc::set_error(SPC_ERR_ARG, "need at least one output slot");
   return SPC_OK;
 }
@@ -337,8 +336,6 @@ int spc_trace_sampling_batch_device(spc_handle* h, int n_jobs, const int* job_sy
   std::vector<spc::JobSpec> jobs;
   int rc = batch_jobs(h, n_jobs, job_sys, M, (const double2*)zkets_dev, out_dev, T, jobs);
   if (rc) return rc;
-  for (const auto& j : jobs)
-    if (m > j.n) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d exceeds a job's dimension %d", m, j.n);
   return spc::propagate_batch(&h->h, theta, init_pop, jobs, dt, t_end, m, tol, T);
 }
 

@@ -47,7 +47,7 @@ struct TileInfo {
   int ldp;           // leading dimension of the job's psi block
   int ip0, nip;      // first pass item, pass items of this tile
   int is0, nis;      // first SpMM item, SpMM items of this tile
-  int pad;
+  int m;             // Krylov dimension of this tile's job: min(m, n)
   int64_t q_off;     // Q_t[j] = Q + q_off + j * n * 32
   int64_t p_off;     // P_t = P + p_off
   int64_t psi_off;   // job psi block
@@ -113,6 +113,9 @@ __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int2 it = a.items[blockIdx.x];
   const TileInfo& T = a.tiles[it.x];
+  // steps past this job's Krylov dimension (whole tile, so whole CTA)
+  if (KIND != PASS_NORM_GATHER && (a.col_i >= T.m || (KIND == PASS_AXPY_NORM && a.col_i >= T.m - 1)))
+    return;
   const int w = it.x * SPC_LANES + tx;
   const bool act = a.map[w] >= 0;
   const int n = T.n;
@@ -192,6 +195,7 @@ __global__ void __launch_bounds__(256)
             const double* __restrict__ rbeta, double2* __restrict__ Q) {
   const int2 it = items[blockIdx.x];
   const TileInfo& T = tiles[it.x];
+  if (!gather && jd >= T.m) return;
   const int tx = threadIdx.x;
   const int w = it.x * SPC_LANES + tx;
   if (map[w] < 0) return;
@@ -224,6 +228,7 @@ __global__ void __launch_bounds__(256)
            double2* __restrict__ Pout) {
   const int2 it = items[blockIdx.x];
   const TileInfo& T = tiles[it.x];
+  if (i >= T.m) return;
   const int tx = threadIdx.x;
   const bool act = map[it.x * SPC_LANES + tx] >= 0;
   const int n = T.n;
@@ -332,25 +337,28 @@ __device__ void smem_matmul(int m, const double2* A, const double2* B, double2* 
 }
 
 __global__ void __launch_bounds__(128)
-    k_expm(int m, int nslots, const int* __restrict__ map, const double2* __restrict__ Ahess,
-           double2* __restrict__ Aexp, double dt, int* __restrict__ err) {
+    k_expm(int mld, int nslots, const TileInfo* __restrict__ tiles, const int* __restrict__ map,
+           const double2* __restrict__ Ahess, double2* __restrict__ Aexp, double dt,
+           int* __restrict__ err) {
   extern __shared__ double2 sm[];
   __shared__ double rowsum[SPC_MAX_M];
   __shared__ int piv[SPC_MAX_M];
   __shared__ int s_sh, p_sh;
-  const int mm = m * m;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int w = blockIdx.x;
   if (w >= nslots || map[w] < 0) return;
+  // working dimension m <= mld (the storage leading dimension)
+  const int m = tiles[w / SPC_LANES].m;
+  const int mm = m * m;
   double2* A2 = sm;
   double2* X = A2 + mm;
   double2* E = X + mm;
   double2* D = E + mm;
   double2* T = D + mm;
-  const double2* Ain = Ahess + (size_t)w * mm;
+  const double2* Ain = Ahess + (size_t)w * mld * mld;
   // (0,-1)*dt*A
   for (int i = tid; i < mm; i += nt) {
-    double2 a = Ain[i];
+    double2 a = Ain[(i % m) + (size_t)(i / m) * mld];
     A2[i] = make_double2(dt * a.y, -dt * a.x);
   }
   __syncthreads();
@@ -481,8 +489,8 @@ __global__ void __launch_bounds__(128)
     for (int i = tid; i < mm; i += nt) E[i] = X[i];
     __syncthreads();
   }
-  double2* out = Aexp + (size_t)w * mm;
-  for (int i = tid; i < mm; i += nt) out[i] = E[i];
+  double2* out = Aexp + (size_t)w * mld * mld;
+  for (int i = tid; i < mm; i += nt) out[(i % m) + (size_t)(i / m) * mld] = E[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -502,6 +510,7 @@ __global__ void __launch_bounds__(256)
   const int w = blockIdx.x;
   if (map[w] < 0) return;
   const TileInfo& Ti = tiles[w / SPC_LANES];
+  const int me = Ti.m;
   const int lane = w % SPC_LANES;
   const int split = blockIdx.y;
   const int tid = threadIdx.x;
@@ -531,7 +540,7 @@ __global__ void __launch_bounds__(256)
     for (int idx = tid; idx < m * PROJ_NC; idx += 256) {
       const int j = idx / PROJ_NC, nn = idx % PROJ_NC;
       double2 q1 = cz(), q2 = cz(), q3 = cz(), q4 = cz();
-      if (nn < len) {
+      if (nn < len && j < me) {
         const double2* base = Qt + (size_t)j * vs;
         const int64_t n = c0 + nn;
         q1 = base[(size_t)n * SPC_LANES];
@@ -582,17 +591,20 @@ __global__ void k_proj_reduce(int nslots, const int* __restrict__ map, int m, in
 // max_ij |(Tp + S + T0 + Tm)_ij - delta_ij| > tol flags the slot.
 #define ORTHO_TOL 1e-12
 __global__ void __launch_bounds__(128)
-    k_ortho_check(int m, const int* __restrict__ map, const double2* __restrict__ proj, double tol,
-                  int* __restrict__ flag) {
+    k_ortho_check(int m, const TileInfo* __restrict__ tiles, const int* __restrict__ map,
+                  const double2* __restrict__ proj, double tol, int* __restrict__ flag) {
   __shared__ double red[128];
   const int w = blockIdx.x;
   if (map[w] < 0) return;
   const size_t mm = (size_t)m * m;
   const double2* P = proj + (size_t)w * 4 * mm;
+  const int me = tiles[w / SPC_LANES].m;
   double mx = 0.0;
-  for (int idx = threadIdx.x; idx < (int)mm; idx += blockDim.x) {
+  for (int id = threadIdx.x; id < me * me; id += blockDim.x) {
+    const int i = id % me, j = id / me;
+    const size_t idx = (size_t)i + (size_t)j * m;
     const double2 g = cadd(cadd(P[idx], P[mm + idx]), cadd(P[2 * mm + idx], P[3 * mm + idx]));
-    const double d = (idx % (m + 1) == 0) ? 1.0 : 0.0;
+    const double d = (i == j) ? 1.0 : 0.0;
     const double e = fmax(fabs(g.x - d), fabs(g.y));
     mx = (e > mx || e != e) ? e : mx;  // NaN flags too
   }
@@ -612,7 +624,8 @@ __global__ void __launch_bounds__(128)
 // dt loop (src/qm_dynamics.f90:348-364), one warp per slot. Projector types
 // in `proj`: 0 Tp, 1 S, 2 T0, 3 Tm; obs slots per sample: 0 S, 1 T0, 2 Tp, 3 Tm.
 __global__ void __launch_bounds__(128)
-    k_dtloop(int m, int nslots, int T, const int* __restrict__ map, const int* __restrict__ skip,
+    k_dtloop(int m, int nslots, int T, const TileInfo* __restrict__ tiles,
+             const int* __restrict__ map, const int* __restrict__ skip,
              const double2* __restrict__ Aexp, const double2* __restrict__ proj,
              double2* __restrict__ cvec, double* __restrict__ tt, int* __restrict__ kk,
              int* __restrict__ done, double* __restrict__ obs, double dt, double t_end, double tol,
@@ -626,7 +639,8 @@ __global__ void __launch_bounds__(128)
   const double2* E = Aexp + (size_t)w * mm;
   const double2* PX = proj + (size_t)w * 4 * mm;
   double2* c = cs[warp];
-  const bool l0 = lane < m, l1 = lane + 32 < m;
+  const int me = tiles[w / SPC_LANES].m;  // this job's Krylov dimension
+  const bool l0 = lane < me, l1 = lane + 32 < me;
   if (l0) c[lane] = cvec[(size_t)w * m + lane];
   if (l1) c[lane + 32] = cvec[(size_t)w * m + lane + 32];
   __syncwarp();
@@ -638,7 +652,7 @@ __global__ void __launch_bounds__(128)
   long long steps = 0;
   while (cm2 <= tol * c2 && t < t_end) {
     double2 n0 = cz(), n1 = cz();
-    for (int j = 0; j < m; ++j) {
+    for (int j = 0; j < me; ++j) {
       const double2 cj = c[j];
       if (l0) n0 = cfma(E[lane + j * m], cj, n0);
       if (l1) n1 = cfma(E[lane + 32 + j * m], cj, n1);
@@ -654,7 +668,7 @@ __global__ void __launch_bounds__(128)
     for (int ty = 0; ty < 4; ++ty) {
       const double2* P = PX + ty * mm;
       double2 v0 = cz(), v1 = cz();
-      for (int j = 0; j < m; ++j) {
+      for (int j = 0; j < me; ++j) {
         const double2 cj = c[j];
         if (l0) v0 = cfma(P[lane + j * m], cj, v0);
         if (l1) v1 = cfma(P[lane + 32 + j * m], cj, v1);
@@ -669,7 +683,7 @@ __global__ void __launch_bounds__(128)
     if (l0) nn = fma(n0.x, n0.x, n0.y * n0.y);
     if (l1) nn += fma(n1.x, n1.x, n1.y * n1.y);
     c2 = warp_sum(nn);
-    const double2 cmv = c[m - 1];
+    const double2 cmv = c[me - 1];
     cm2 = cmv.x * cmv.x + cmv.y * cmv.y;
     t = t + dt;
     k = k + 1;
@@ -698,7 +712,8 @@ __global__ void __launch_bounds__(256)
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int w = it.x * SPC_LANES + tx;
   const bool act = map[w] >= 0 && !skip[w];
-  for (int j = ty; j < m; j += SPC_WARPS) cs[j][tx] = act ? cvec[(size_t)w * m + j] : cz();
+  const int me = T.m;
+  for (int j = ty; j < me; j += SPC_WARPS) cs[j][tx] = act ? cvec[(size_t)w * m + j] : cz();
   __syncthreads();
   if (!act) return;
   const int n = T.n;
@@ -709,7 +724,7 @@ __global__ void __launch_bounds__(256)
   for (int r = it.y * SPC_WARPS + ty; r < n; r += stride) {
     double2 acc = cz();
     const double2* qr = q + (size_t)r * SPC_LANES;
-    for (int j = 0; j < m; ++j) acc = cfma(qr[(size_t)j * vs], cs[j][tx], acc);
+    for (int j = 0; j < me; ++j) acc = cfma(qr[(size_t)j * vs], cs[j][tx], acc);
     dst[(size_t)r * T.ldp] = acc;
   }
 }
@@ -974,6 +989,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
         ti.split = jobs[k].split;
         ti.col = jobs[k].col;
         ti.val = jobs[k].val;
+        ti.m = std::min(m, ti.n);
         qo += (int64_t)m * ti.n * SPC_LANES;
         po += (int64_t)ti.n * SPC_LANES;
         for (int l = 0; l < SPC_LANES; ++l) {
@@ -1094,7 +1110,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     for (size_t c = 0; c < map.size(); ++c)
       if (map[c] >= 0) zsum += tiles[c / SPC_LANES].n / 4;
     pe = h->prof.begin(st);
-    k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, d_map, d_A, d_E, dt, d_err);
+    k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, d_tiles, d_map, d_A, d_E, dt, d_err);
     h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * list.size(),
                 32.0 * (double)mm * list.size());
     // projector split: the count in [1, nsplit_max] whose grid wastes the
@@ -1132,7 +1148,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     if (lanczos) {
       // G = Q^H Q = Tp + S + T0 + Tm; a basis that drifted from orthonormal
       // beyond ORTHO_TOL is rebuilt with full MGS
-      k_ortho_check<<<nslots, 128, 0, st>>>(m, d_map, d_proj, ORTHO_TOL, d_flag);
+      k_ortho_check<<<nslots, 128, 0, st>>>(m, d_tiles, d_map, d_proj, ORTHO_TOL, d_flag);
       h->count_launch();
       CK(cudaMemcpyAsync(flag_h.data(), d_flag, sizeof(int) * nslots, cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
@@ -1140,7 +1156,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
         if (map[w] >= 0 && flag_h[w]) failed.push_back(map[w]);
     }
     pe = h->prof.begin(st);
-    k_dtloop<<<(nslots + 3) / 4, 128, 0, st>>>(m, nslots, T, d_map, d_flag, d_E, d_proj, d_c, d_t,
+    k_dtloop<<<(nslots + 3) / 4, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj, d_c, d_t,
                                                d_k, d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
     h->prof.end(st, pe, PK_DTLOOP, 0.0, 0.0);
     pe = h->prof.begin(st);

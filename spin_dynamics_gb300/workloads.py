@@ -81,6 +81,39 @@ def notebook_pair() -> SysParam:
                                      J=0.1, D=np.zeros((3, 3)), kS_per_us=0.0, kT_per_us=0.0)
 
 
+def fibonacci_sphere(n: int, radius: float = 0.05) -> np.ndarray:
+    """n field vectors of length `radius` (mT) on a Fibonacci sphere."""
+    i = np.arange(n) + 0.5
+    phi = np.arccos(1.0 - 2.0 * i / n)
+    th = np.pi * (1.0 + 5.0 ** 0.5) * i
+    return radius * np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], 1)
+
+
+def uneven_pairs(n_pairs: int = 256, seed: int = 3) -> list:
+    """The batched uneven set: independent pairs with 2-10 nuclei drawn from
+    {1H, 14N} (14N with probability 0.3), split at random between the two
+    radicals, Hilbert dimensions 16 ... 4*3^2*2^8 = 9216; couplings as in the
+    large pair (anisotropic, principal values in [-2, 2] mT); J = 0.01 mT,
+    D = -0.4 mT axial, kS = kT = 1/us; 32-256 samples each.
+    Returns [(SysParam, n_samples)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n_pairs:
+        nn = int(rng.integers(2, 11))
+        g = [3 if rng.random() < 0.3 else 2 for _ in range(nn)]
+        if 4 * int(np.prod(g)) > 9216:
+            continue
+        side = rng.random(nn) < 0.5
+        g1 = [x for x, s in zip(g, side) if s]
+        g2 = [x for x, s in zip(g, side) if not s]
+        A1 = _tensors(rng, len(g1), -2.0, 2.0, True)
+        A2 = _tensors(rng, len(g2), -2.0, 2.0, True)
+        sys_ = SysParam.from_input_units(Electron(g_I=g1, A=A1), Electron(g_I=g2, A=A2), J=0.01,
+                                         D=axial_dipolar(-0.4), kS_per_us=1.0, kT_per_us=1.0)
+        out.append((sys_, int(rng.integers(32, 257))))
+    return out
+
+
 def random_phase_samples(Z: int, M: int, seed: int = 7) -> np.ndarray:
     """M normalised random-phase vectors e^{i phi}/sqrt(Z), phi ~ U[0, 2 pi)."""
     rng = np.random.default_rng(seed)

@@ -90,3 +90,24 @@ def test_mixed_rates_batch_uses_mgs(sampler, oracle):
     for s, g in ((a, got[0]), (b, got[1])):
         rp, col, val = iso_csr(oracle, s, 0.05)
         _check(g, oracle.trace_sampling(rp, col, val, zk, DT, 15 * DT, 10, 1e-6))
+
+
+def test_krylov_dimension_capped_at_job_dimension(sampler, oracle):
+    """A 16-dim job at m = 20 runs with m = 16 (its whole space): exact."""
+    import dense
+    from spin_dynamics_gb300.spinsys import Electron, SysParam
+    tiny = SysParam(e1=Electron(g_I=[2], A=[np.eye(3) * 0.6]), e2=Electron(g_I=[2], A=[np.eye(3) * 0.3]),
+                    J=0.02, kS=1.0 / GAMMA_E, kT=1.0 / GAMMA_E)
+    big = W.small_pair()
+    zt = np.eye(tiny.Z, dtype=complex)
+    zb = W.random_phase_samples(big.Z, 8, seed=4)
+    t_end = 20 * DT
+    sampler.build_h_batch([tiny, big], [0.1, 0.1], "reference")
+    got = sampler.trace_sampling_batch([zt, zb], DT, t_end, 20, 1e-6)
+    n = int(np.ceil(t_end / DT)) + 1
+    H = dense.hamiltonian(tiny.e1.g_I, tiny.e1.A, tiny.e2.g_I, tiny.e2.A, [0, 0, 0.1], tiny.J, tiny.D,
+                          tiny.kS, tiny.kT)
+    PS = dense.trace_sampled_populations(H, zt, np.arange(n) * DT)[0]
+    assert np.max(np.abs(got[0].P_S[:n] - PS)) < 1e-12
+    rp, col, val = iso_csr(oracle, big, 0.1)
+    _check(got[1], oracle.trace_sampling(rp, col, val, zb, DT, t_end, 20, 1e-6))
