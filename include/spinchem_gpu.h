@@ -209,6 +209,43 @@ int spc_trace_sampling_batch_device(spc_handle* h, int n_jobs, const int* job_sy
                                     const double* zkets_dev, double dt, double t_end, int m,
                                     double tol, double* out_dev, int T);
 
+/* ---- yield gradient (no counterpart in the reference) ---------------- */
+
+/* Entries of the gradient spc_yield_gradient writes for `sys`:
+ * 15 + 9 * (n_nuc1 + n_nuc2), or -1 for a bad argument. */
+int spc_yield_gradient_size(const spc_system* sys);
+
+/* Singlet and triplet yields and the gradient of wS*Phi_S + wT*Phi_T with
+ * respect to every parameter of `sys`, by the discrete adjoint of a stepwise
+ * propagation. The reference computes the yields only (get_kinetics,
+ * src/observables.f90:74-101, on the populations of trace_sampling_para,
+ * src/qm_dynamics.f90:257-384); it has no derivatives.
+ * Model: every sample psi = theta (x) z is propagated by
+ * psi_{k+1} = exp(-i H dt) psi_k with one Krylov basis of dimension m per
+ * step (full MGS; the three-term recurrence only under SPC_KRYLOV_LANCZOS,
+ * which needs kS == kT and is not Gram-checked here), the
+ * Hamiltonian of SPC_H_GENERAL, populations averaged over the M samples, and
+ * Phi_X = k_X * the Simpson sum of get_kinetics over the
+ * spc_num_time_points(dt, t_end) grid (its last value).
+ *   zkets            M x Z complex, host memory, sample-major
+ *   n_quad           Gauss-Legendre nodes per step for the derivative of
+ *                    exp(-i H dt) (1..16; 6 gives ~1e-8 relative error at
+ *                    ||H|| dt ~ 5)
+ *   checkpoint_every forward states kept every this many steps (0 = about
+ *                    sqrt(steps / (1 + n_quad)), the least device memory)
+ *   yields           2 doubles: Phi_S, Phi_T
+ *   grad             spc_yield_gradient_size(sys) doubles:
+ *                    dB[3], dJ, dD[9] (column-major as spc_system.D), dkS, dkT,
+ *                    then 9 per nucleus (radical 1's, then radical 2's),
+ *                    column-major as spc_system.A1/A2
+ * Device memory: about (m + 4 + n_steps/K + (1 + n_quad) K) states of
+ * 16 * n * ceil(M/32)*32 bytes. Nuclei of multiplicity above 3 return
+ * SPC_ERR_UNSUPPORTED. The handle's Hamiltonian and batch are replaced by H
+ * and H^H. Cost: three Krylov builds per sample and step. */
+int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta,
+                       const double* zkets, int M, double dt, double t_end, int m, int n_quad,
+                       int checkpoint_every, double wS, double wT, double* yields, double* grad);
+
 /* Select the Krylov orthogonalisation (SPC_KRYLOV_*). In exact arithmetic
  * Lanczos and MGS give the same basis when H_eff = Hermitian - i*kappa; the
  * Lanczos path skips the O(m^2 n) re-orthogonalisation and verifies the

@@ -112,3 +112,33 @@ def trace_sampled_populations(H, zkets, times, which="singlet"):
     ps = propagate(H, psi0, times)
     PS, PT0, PTp, PTm = populations(ps, Z)
     return PS.mean(1), PT0.mean(1), PTp.mean(1), PTm.mean(1)
+
+
+def simpson_weights(T, dt):
+    """Weights c_k with Phi_X = k_X sum_k c_k P_X(k) equal to the last value
+    get_kinetics returns over T points (src/observables.f90:74-101): panels
+    (2i-2, 2i-1, 2i) for i = 1 .. T//2 - 1, each dt/3 (1, 4, 1)."""
+    w = np.zeros(T)
+    for i in range(1, T // 2):
+        w[2 * i - 2] += dt / 3.0
+        w[2 * i - 1] += 4.0 * dt / 3.0
+        w[2 * i] += dt / 3.0
+    return w
+
+
+def stepwise_yields(H, zkets, dt, T, kS, kT, which="singlet"):
+    """(Phi_S, Phi_T) of psi_{k+1} = expm(-i H dt) psi_k, sample-averaged
+    populations and get_kinetics' Simpson rule over T points."""
+    from scipy.linalg import expm
+    Z = zkets.shape[1]
+    U = expm(-1j * dt * H)
+    psi = np.stack([np.kron(theta(which), z) for z in zkets])
+    w = simpson_weights(T, dt)
+    aS = aT = 0.0
+    for k in range(T):
+        if w[k] != 0.0:
+            PS, PT0, PTp, PTm = populations(psi, Z)
+            aS += w[k] * PS.mean()
+            aT += w[k] * (PT0 + PTp + PTm).mean()
+        psi = psi @ U.T
+    return kS * aS, kT * aT

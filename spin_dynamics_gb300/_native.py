@@ -80,6 +80,9 @@ SIGNATURES = {
     "spc_build_h_batch": (_I, [_P, _I, _P, _I]),
     "spc_trace_sampling_batch": (_I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _I, _D, _P, _I]),
     "spc_trace_sampling_batch_device": (_I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _I, _D, _P, _I]),
+    "spc_yield_gradient_size": (_I, [C.POINTER(spc_system)]),
+    "spc_yield_gradient": (_I, [_P, C.POINTER(spc_system), _P, _P, _I, _D, _D, _I, _I, _I, _D, _D, _P,
+                                _P]),
     "spc_set_profiling": (_I, [_P, _I]),
     "spc_get_profile": (_I, [_P, _I, C.POINTER(_D), C.POINTER(C.c_int64), C.POINTER(_D),
                              C.POINTER(_D)]),

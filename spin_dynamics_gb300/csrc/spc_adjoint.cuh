@@ -1,0 +1,453 @@
+// Adjoint gradient of the radical-pair yields (spc_yield_gradient). Included
+// at the end of spc_propagate.cu, inside namespace spc, so that it reuses the
+// Krylov kernels defined there.
+//
+// Model: the stepwise propagation psi_{k+1} = exp(-i H dt) psi_k of every
+// sample (a fresh Krylov basis each dt step, no data-dependent basis reuse,
+// so the objective is a smooth function of the parameters), populations
+// P_X(k) = <psi_k|Pi_X|psi_k> averaged over the samples, and the yields of
+// get_kinetics (src/observables.f90:74-101): Phi_X = k_X sum_k c_k P_X(k)
+// with Simpson weights c_k = dt/3 {1, 4, 2, ..., 4, 1} on the reference's time
+// grid. The objective is wS Phi_S + wT Phi_T.
+//
+// Discrete adjoint with O = wS kS Pi_S + wT kT Pi_T:
+//   lambda_N = c_N O psi_N,  lambda_k = c_k O psi_k + U^H lambda_{k+1},
+//   dObj/dp = sum_k 2 Re <lambda_{k+1}| dU/dp |psi_k>  (+ explicit k_X terms)
+//   <lambda| dU |psi> = -i int_0^dt <exp(i H^H (dt-tau)) lambda| dH/dp |exp(-i H tau) psi> dtau
+// with the integral by Gauss-Legendre nodes. H^H = H_eff(-kS, -kT), so
+// exp(i H^H s) lambda is a Krylov step of lambda under that Hamiltonian with a
+// negative time step. Every dH/dp is an electron operator times at most one
+// nuclear operator, so all of them are read off reduced matrices
+// R[a][b] = sum_rest conj(mu_a) nu_b of the electron pair (4 x 4) and of each
+// (electron spin, nucleus) pair (2g x 2g), accumulated on the device over the
+// nodes and steps.
+//
+// Schedule: forward sweep with checkpoints every K steps; the backward sweep
+// recomputes each segment from its checkpoint, and the Krylov basis built at
+// psi_k for psi_{k+1} also gives the node states exp(-i H x_q dt) psi_k, kept
+// for the segment. Per step: three Krylov builds (forward, recompute, costate)
+// and 2*nq + 2 basis applications.
+
+#define CON_MAXG 6
+
+// R[a][b] += w * sum_o conj(mu_row(a,o)) nu_row(b,o) for one (tile, slot);
+// one warp per CTA, lanes = samples, the `o` range split into nch chunks;
+// the last CTA of each (tile, slot) adds the chunk partials in chunk order.
+template <int G>
+__global__ void __launch_bounds__(32)
+    k_contract(const TileInfo* __restrict__ tiles, const int* __restrict__ map,
+               const int* __restrict__ scol, const GradSlot* __restrict__ slots, int nsl, int nch,
+               const double2* __restrict__ mu, const double2* __restrict__ nu, double w,
+               double2* __restrict__ partial, unsigned* __restrict__ counters,
+               double2* __restrict__ racc) {
+  const int b = blockIdx.x;
+  const int pair = b / nch, ch = b % nch;
+  const int t = pair / nsl, js = pair % nsl;
+  const GradSlot S = slots[js];
+  if (S.G != G) return;  // launched once per G; slots of the other size leave at once
+  const TileInfo& T = tiles[t];
+  const int lane = threadIdx.x;
+  const int wslot = t * SPC_LANES + lane;
+  const bool act = map[wslot] >= 0;
+  const int64_t Z = T.n / 4;
+  const int64_t L = S.owner < 0 ? Z : 2 * Z / S.g;
+  const int64_t per = (L + nch - 1) / nch;
+  const int64_t o0 = (int64_t)ch * per, o1 = min(L, o0 + per);
+  double2 acc[G * G];
+#pragma unroll
+  for (int i = 0; i < G * G; ++i) acc[i] = cz();
+  if (act) {
+    const int64_t ld = T.ldp;
+    const double2* Mu = mu + T.psi_off + scol[wslot];
+    const double2* Nu = nu + T.psi_off + scol[wslot];
+    const int64_t zg = S.owner < 0 ? Z : Z / S.g;
+    for (int64_t o = o0; o < o1; ++o) {
+      double2 a[G], v[G];
+      if (S.owner < 0) {
+#pragma unroll
+        for (int c = 0; c < G; ++c) {
+          const int64_t row = (int64_t)c * Z + o;
+          a[c] = Mu[row * ld];
+          v[c] = Nu[row * ld];
+        }
+      } else {
+        // o = (spin of the other electron, nuclear index without nucleus j)
+        const int so = (int)(o / zg);
+        const int64_t rem = o - (int64_t)so * zg;
+        const int64_t hi = rem / S.stride, lo = rem - hi * S.stride;
+        const int64_t nbase = hi * S.g * S.stride + lo;
+#pragma unroll
+        for (int c = 0; c < G; ++c) {
+          const int sk = c / (G / 2), mm = c % (G / 2);
+          const int e = S.owner == 0 ? (sk * 2 + so) : (so * 2 + sk);
+          const int64_t row = (int64_t)e * Z + nbase + (int64_t)mm * S.stride;
+          a[c] = Mu[row * ld];
+          v[c] = Nu[row * ld];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < G; ++i)
+#pragma unroll
+        for (int j = 0; j < G; ++j) acc[i * G + j] = cjfma(a[i], v[j], acc[i * G + j]);
+    }
+  }
+  double2* P = partial + (size_t)b * CON_MAXG * CON_MAXG * SPC_LANES + lane;
+#pragma unroll
+  for (int i = 0; i < G * G; ++i) P[(size_t)i * SPC_LANES] = acc[i];
+  __threadfence();
+  __shared__ bool am_last;
+  if (lane == 0) am_last = atomicAdd(&counters[pair], 1u) == (unsigned)nch - 1;
+  __syncwarp();
+  if (!am_last) return;
+  __threadfence();
+  if (act) {
+    double2* R = racc + ((size_t)wslot * nsl + js) * CON_MAXG * CON_MAXG;
+    const double2* base = partial + (size_t)pair * nch * CON_MAXG * CON_MAXG * SPC_LANES + lane;
+    for (int i = 0; i < G * G; ++i) {
+      double2 s = cz();
+      for (int c = 0; c < nch; ++c)
+        s = cadd(s, __ldcg(base + ((size_t)c * CON_MAXG * CON_MAXG + i) * SPC_LANES));
+      R[i] = make_double2(fma(w, s.x, R[i].x), fma(w, s.y, R[i].y));
+    }
+  }
+  if (lane == 0) counters[pair] = 0u;
+}
+
+// Krylov coordinates of y = exp(-i tau A) (beta e1): beta * E[:, 0] per slot,
+// beta = ||x|| as the norm pass left it in cvec[w][0].
+__global__ void k_first_col(int nslots, const TileInfo* __restrict__ tiles, const int* __restrict__ map,
+                            int m, const double2* __restrict__ Aexp, const double2* __restrict__ cvec,
+                            double2* __restrict__ cout) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nslots || map[w] < 0) return;
+  const int me = tiles[w / SPC_LANES].m;
+  const double beta = cvec[(size_t)w * m].x;
+  const double2* E = Aexp + (size_t)w * m * m;
+  for (int j = 0; j < m; ++j) cout[(size_t)w * m + j] = j < me ? cscale(beta, E[j]) : cz();
+}
+
+// lam = ulam + cI psi + cP Pi_S psi, Pi_S = |S><S| on the electron pair,
+// |S> = (|ab> - |ba>)/sqrt(2); grid (tiles, row blocks), block (32, SPC_WARPS).
+__global__ void __launch_bounds__(256)
+    k_costate(const TileInfo* __restrict__ tiles, const int* __restrict__ map,
+              const int* __restrict__ scol, const double2* __restrict__ psi,
+              const double2* __restrict__ ulam, double cI, double cP, double2* __restrict__ lam) {
+  const TileInfo& T = tiles[blockIdx.x];
+  const int w = blockIdx.x * SPC_LANES + threadIdx.x;
+  if (map[w] < 0) return;
+  const int64_t Z = T.n / 4;
+  const int64_t ld = T.ldp;
+  const size_t base = T.psi_off + scol[w];
+  for (int64_t r = (int64_t)blockIdx.y * SPC_WARPS + threadIdx.y; r < 4 * Z;
+       r += (int64_t)gridDim.y * SPC_WARPS) {
+    const int e = (int)(r / Z);
+    const int64_t n = r - e * Z;
+    double2 v = ulam[base + r * ld];
+    const double2 x = psi[base + r * ld];
+    v = make_double2(fma(cI, x.x, v.x), fma(cI, x.y, v.y));
+    if (e == 1 || e == 2) {
+      const double2 ab = psi[base + (Z + n) * ld], ba = psi[base + (2 * Z + n) * ld];
+      const double2 d = cscale(e == 1 ? 0.5 * cP : -0.5 * cP, csub(ab, ba));
+      v = cadd(v, d);
+    }
+    lam[base + r * ld] = v;
+  }
+}
+
+// Gauss-Legendre nodes and weights on [0, 1] (Newton on P_n from the
+// Tricomi initial guesses).
+static void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      // p1 = P_n(z), p0 = P_{n-1}(z)
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    x[i] = 0.5 * (1.0 - z);
+    w[i] = 1.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int M,
+                       const std::vector<GradSlot>& cs, double dt, int nsteps,
+                       const std::vector<double>& cw, double cI, double cP, int m, int nq, int K,
+                       std::vector<double2>& racc_h, std::vector<double2>& facc_h) {
+  auto t_start = std::chrono::steady_clock::now();
+  cudaStream_t st = h->stream;
+  const auto& HB = h->hb;
+  const int n = HB.n[0];
+  const int64_t Z = n / 4;
+  const int ldp = (M + SPC_LANES - 1) / SPC_LANES * SPC_LANES;
+  const int ntiles = ldp / SPC_LANES, nslots = ldp;
+  const int nsl = (int)cs.size();
+  const size_t S = (size_t)n * ldp;  // one state of all samples (psi layout)
+  const int nck = nsteps / K + 1;
+  const int a_last = ((nsteps - 1) / K) * K;  // first step of the last segment
+  const size_t mm = (size_t)m * m;
+  // chunks per (tile, slot): about two waves of one-warp CTAs
+  const int nch = (int)std::max<int64_t>(
+      1, std::min<int64_t>(Z, (int64_t)h->sm_count * 32 / std::max(1, ntiles * nsl)));
+  const size_t npairs = (size_t)ntiles * nsl;
+  const int items_cap = h->sm_count * 32 + ntiles;
+  const size_t con = (size_t)CON_MAXG * CON_MAXG;
+  if (h->ensure(h->gck, sizeof(double2) * S * nck) || h->ensure(h->gseg, sizeof(double2) * S * (K + 1)) ||
+      h->ensure(h->gnu, sizeof(double2) * S * K * nq) || h->ensure(h->gmu, sizeof(double2) * S) ||
+      h->ensure(h->glam, sizeof(double2) * S * 2) || h->ensure(h->Q, sizeof(double2) * m * S) ||
+      h->ensure(h->P, sizeof(double2) * S) ||
+      h->ensure(h->partial, sizeof(double2) * std::max<size_t>((size_t)items_cap * SPC_LANES,
+                                                               npairs * nch * con * SPC_LANES)) ||
+      h->ensure(h->counters, sizeof(unsigned) * std::max<size_t>(ntiles, npairs)) ||
+      h->ensure(h->coef, sizeof(double2) * nslots) || h->ensure(h->rbeta, sizeof(double) * nslots) ||
+      h->ensure(h->Ahess, sizeof(double2) * mm * nslots) || h->ensure(h->Aexp, sizeof(double2) * mm * nslots) ||
+      h->ensure(h->cvec, sizeof(double2) * m * nslots) || h->ensure(h->cvec2, sizeof(double2) * m * nslots) ||
+      h->ensure(h->flag, sizeof(int) * nslots) || h->ensure(h->err, 16) ||
+      h->ensure(h->gslots, sizeof(GradSlot) * nsl) || h->ensure(h->gracc, sizeof(double2) * nslots * nsl * con) ||
+      h->ensure(h->gfacc, sizeof(double2) * nslots * con) ||
+      h->ensure(h->plan, 2 * sizeof(TileInfo) * ntiles + sizeof(int2) * 2 * items_cap + sizeof(int) * 2 * nslots) ||
+      h->ensure(h->jobtab, sizeof(JobInit)))
+    return SPC_ERR_ALLOC;
+  double2 *ck = (double2*)h->gck.p, *seg = (double2*)h->gseg.p, *gnu = (double2*)h->gnu.p;
+  double2 *gmu = (double2*)h->gmu.p, *lam = (double2*)h->glam.p, *ulam = lam + S;
+  double2 *d_Q = (double2*)h->Q.p, *d_P = (double2*)h->P.p, *d_part = (double2*)h->partial.p;
+  unsigned* d_cnt = (unsigned*)h->counters.p;
+  double2 *d_A = (double2*)h->Ahess.p, *d_E = (double2*)h->Aexp.p, *d_c = (double2*)h->cvec.p;
+  double2* d_c2 = (double2*)h->cvec2.p;
+  int* d_flag = (int*)h->flag.p;
+  int* d_err = (int*)h->err.p;
+  GradSlot* d_slots = (GradSlot*)h->gslots.p;
+  double2 *d_racc = (double2*)h->gracc.p, *d_facc = (double2*)h->gfacc.p;
+  char* plan = (char*)h->plan.p;
+  TileInfo* d_tf = (TileInfo*)plan;
+  TileInfo* d_tb = d_tf + ntiles;
+  int2* d_items = (int2*)(plan + 2 * sizeof(TileInfo) * ntiles);
+  int2* d_items_s = d_items + items_cap;
+  int* d_map = (int*)(d_items_s + items_cap);
+  int* d_scol = d_map + nslots;
+  int64_t launches0 = h->launches;
+
+  // static tiles (every sample takes every step) for H (tf) and H^H (tb)
+  auto resident = [&](const void* fn) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 256, 0) != cudaSuccess) b = 1;
+    return std::max(1, b) * h->sm_count;
+  };
+  std::vector<int> tile_n(ntiles, n), fp, cp, fs, csn;
+  std::vector<int2> items_p, items_s;
+  plan_items(tile_n, std::min(resident((const void*)k_rowpass<PASS_AXPY_DOT>),
+                              resident((const void*)k_rowpass<PASS_AXPY_NORM>)), fp, cp, items_p);
+  plan_items(tile_n, resident((const void*)k_spmm), fs, csn, items_s);
+  const int nip = (int)items_p.size(), nis = (int)items_s.size();
+  if (nip > items_cap || nis > items_cap) return set_error(SPC_ERR_ARG, "internal: work plan exceeds its buffer");
+  std::vector<TileInfo> tf(ntiles), tb(ntiles);
+  std::vector<int> map(nslots), scol(nslots);
+  for (int t = 0; t < ntiles; ++t) {
+    TileInfo ti{};
+    ti.job = 0;
+    ti.n = n;
+    ti.ldp = ldp;
+    ti.m = std::min(m, n);
+    ti.q_off = (int64_t)t * m * n * SPC_LANES;
+    ti.p_off = (int64_t)t * n * SPC_LANES;
+    ti.psi_off = 0;
+    ti.ip0 = fp[t];
+    ti.nip = cp[t];
+    ti.is0 = fs[t];
+    ti.nis = csn[t];
+    tf[t] = tb[t] = ti;
+    for (int e = 0; e < 2; ++e) {
+      TileInfo& x = e == 0 ? tf[t] : tb[t];
+      x.rowptr = (const int*)HB.rowptr.p + HB.rp_off[e];
+      x.split = (const int*)HB.split.p + HB.rp_off[e];
+      x.col = (const int*)HB.col.p + HB.nz_off[e];
+      x.val = (const double2*)HB.val.p + HB.nz_off[e];
+    }
+    for (int l = 0; l < SPC_LANES; ++l) {
+      const int s = t * SPC_LANES + l;
+      map[s] = scol[s] = s < M ? s : -1;
+    }
+  }
+  CK(cudaMemcpyAsync(d_tf, tf.data(), sizeof(TileInfo) * ntiles, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_tb, tb.data(), sizeof(TileInfo) * ntiles, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_items, items_p.data(), sizeof(int2) * nip, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_items_s, items_s.data(), sizeof(int2) * nis, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_map, map.data(), sizeof(int) * nslots, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_scol, scol.data(), sizeof(int) * nslots, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_slots, cs.data(), sizeof(GradSlot) * nsl, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * std::max<size_t>(ntiles, npairs), st));
+  CK(cudaMemsetAsync(d_racc, 0, sizeof(double2) * nslots * nsl * con, st));
+  CK(cudaMemsetAsync(d_facc, 0, sizeof(double2) * nslots * con, st));
+  CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * nslots, st));
+  CK(cudaMemsetAsync(h->err.p, 0, 16, st));
+  // psi_0 = theta (x) z: into the last segment's buffer when it is the only one
+  double2* psi0 = a_last == 0 ? seg : ck;
+  CK(cudaMemsetAsync(psi0, 0, sizeof(double2) * S, st));
+  {
+    JobInit ji{Z, 0, M, ldp, (const double2*)zk_dev};
+    CK(cudaMemcpyAsync(h->jobtab.p, &ji, sizeof(JobInit), cudaMemcpyHostToDevice, st));
+    Theta th;
+    for (int e = 0; e < 4; ++e) th.v[e] = make_double2(theta[2 * e], theta[2 * e + 1]);
+    k_kron_init<<<dim3(h->sm_count * 8, 1), 256, 0, st>>>((const JobInit*)h->jobtab.p, 0, th, psi0);
+    h->count_launch();
+  }
+  const size_t expm_smem = sizeof(double2) * 5 * mm;
+  CK(cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expm_smem));
+  const dim3 blk(SPC_LANES, SPC_WARPS);
+  // the three-term recurrence only on explicit request: no projector Gram
+  // verifies these bases (the trace-sampling path checks its own)
+  const bool lanczos = h->krylov_method == 1 && HB.herm[0] && HB.herm[1];
+  std::vector<double> xq, wq;
+  gauss_legendre01(nq, xq, wq);
+  int64_t builds = 0;
+
+  // Krylov basis of the states `x` (psi layout) under the tiles' Hamiltonian
+  auto build = [&](const double2* x, const TileInfo* tiles) {
+    CK(cudaMemsetAsync(d_A, 0, sizeof(double2) * mm * nslots, st));
+    PassArgs pa{};
+    pa.tiles = tiles;
+    pa.items = d_items;
+    pa.m = m;
+    pa.Q = d_Q;
+    pa.P = d_P;
+    pa.psi = x;
+    pa.map = d_map;
+    pa.scol = d_scol;
+    pa.coef = (double2*)h->coef.p;
+    pa.rbeta = (double*)h->rbeta.p;
+    pa.Ahess = d_A;
+    pa.cvec = d_c;
+    pa.partial = d_part;
+    pa.counters = d_cnt;
+    pa.lanczos = lanczos ? 1 : 0;
+    k_rowpass<PASS_NORM_GATHER><<<nip, blk, 0, st>>>(pa);
+    k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 1, 0, pa.rbeta, d_Q);
+    h->count_launch(2);
+    for (int i = 0; i < m; ++i) {
+      k_spmm<<<nis, blk, 0, st>>>(tiles, d_items_s, d_map, i, d_Q, d_P);
+      h->count_launch();
+      pa.col_i = i;
+      int j0 = 0;
+      if (lanczos && i > 0) {
+        j0 = i - 1;
+      } else {
+        pa.row_j = 0;
+        pa.jx = 0;
+        k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
+        h->count_launch();
+      }
+      for (int j = j0; j < i; ++j) {
+        pa.jx = j;
+        pa.jn = j + 1;
+        pa.row_j = j + 1;
+        k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
+        h->count_launch();
+      }
+      if (i < m - 1) {
+        pa.jx = i;
+        pa.row_j = i + 1;
+        k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
+        k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 0, i + 1, pa.rbeta, d_Q);
+        h->count_launch(2);
+      }
+    }
+    builds += M;
+    return SPC_OK;
+  };
+  // y = exp(-i tau H) x from the current basis (tau < 0 runs backwards)
+  auto apply = [&](double tau, const TileInfo* tiles, double2* y) {
+    k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, tiles, d_map, d_A, d_E, tau, d_err);
+    k_first_col<<<(nslots + 127) / 128, 128, 0, st>>>(nslots, tiles, d_map, m, d_E, d_c, d_c2);
+    k_psi_update<<<nip, blk, 0, st>>>(tiles, d_items, m, d_map, d_scol, d_flag, d_Q, d_c2, y);
+    h->count_launch(3);
+  };
+  // acc += w * reduced matrices of (mu, nu); nsl_ = 1 takes the electron pair only
+  auto contract = [&](const double2* mu, const double2* nu, double w, int nsl_, double2* acc) {
+    const int nb = ntiles * nsl_ * nch;
+    k_contract<4><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, nsl_, nch, mu, nu, w, d_part, d_cnt, acc);
+    h->count_launch();
+    if (nsl_ > 1) {
+      k_contract<6><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, nsl_, nch, mu, nu, w, d_part, d_cnt, acc);
+      h->count_launch();
+    }
+  };
+  // basis at psi_k under H: node states nu_q and psi_{k+1}
+  auto step_forward = [&](const double2* x, double2* nodes, double2* y) {
+    int rc = build(x, d_tf);
+    if (rc) return rc;
+    if (nodes)
+      for (int q = 0; q < nq; ++q) apply(dt * xq[q], d_tf, nodes + S * q);
+    apply(dt, d_tf, y);
+    return SPC_OK;
+  };
+  const dim3 lgrid(ntiles, std::max(1, h->sm_count * 4 / ntiles));
+
+  // forward sweep: checkpoints, the last segment's states and node states,
+  // and F = sum_k c_k (electron-pair reduced matrix of psi_k)
+  double2* cur = psi0;
+  for (int k = 0; k < nsteps; ++k) {
+    if (cw[k] != 0.0) contract(cur, cur, cw[k], 1, d_facc);
+    double2* nxt;
+    if (k + 1 >= a_last)
+      nxt = seg + S * (k + 1 - a_last);
+    else if ((k + 1) % K == 0)
+      nxt = ck + S * ((k + 1) / K);
+    else
+      nxt = cur == gmu ? ulam : gmu;
+    int rc = step_forward(cur, k >= a_last ? gnu + S * nq * (k - a_last) : nullptr, nxt);
+    if (rc) return rc;
+    cur = nxt;
+  }
+  if (cw[nsteps] != 0.0) contract(cur, cur, cw[nsteps], 1, d_facc);
+  // backward sweep
+  CK(cudaMemsetAsync(lam, 0, sizeof(double2) * S, st));
+  k_costate<<<lgrid, blk, 0, st>>>(d_tf, d_map, d_scol, cur, lam, cw[nsteps] * cI, cw[nsteps] * cP, lam);
+  h->count_launch();
+  for (int a = a_last; a >= 0; a -= K) {
+    const int b = std::min(nsteps, a + K);
+    if (a != a_last) {
+      CK(cudaMemcpyAsync(seg, ck + S * (a / K), sizeof(double2) * S, cudaMemcpyDeviceToDevice, st));
+      for (int k = a; k < b; ++k) {
+        int rc = step_forward(seg + S * (k - a), gnu + S * nq * (k - a), seg + S * (k - a + 1));
+        if (rc) return rc;
+      }
+    }
+    for (int k = b - 1; k >= a; --k) {
+      int rc = build(lam, d_tb);
+      if (rc) return rc;
+      for (int q = 0; q < nq; ++q) {
+        apply(-dt * (1.0 - xq[q]), d_tb, gmu);
+        contract(gmu, gnu + S * (nq * (k - a) + q), wq[q] * dt, nsl, d_racc);
+      }
+      apply(-dt, d_tb, ulam);
+      k_costate<<<lgrid, blk, 0, st>>>(d_tf, d_map, d_scol, seg + S * (k - a), ulam, cw[k] * cI,
+                                       cw[k] * cP, lam);
+      h->count_launch();
+    }
+  }
+  CK(cudaGetLastError());
+  racc_h.resize((size_t)nslots * nsl * con);
+  facc_h.resize((size_t)nslots * con);
+  CK(cudaMemcpyAsync(racc_h.data(), d_racc, sizeof(double2) * racc_h.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(facc_h.data(), d_facc, sizeof(double2) * facc_h.size(), cudaMemcpyDeviceToHost, st));
+  int err_h[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(err_h, h->err.p, 16, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  h->stats.krylov_builds = builds;
+  h->stats.lanczos_fallbacks = 0;
+  h->stats.rounds = 0;
+  h->stats.sample_steps = (int64_t)nsteps * M;
+  h->stats.kernel_launches = h->launches - launches0;
+  h->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  if (err_h[0] == 2) return set_error(SPC_ERR_NUMERIC, "singular Pade denominator in expm");
+  return SPC_OK;
+}

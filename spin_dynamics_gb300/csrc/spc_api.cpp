@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -386,6 +387,199 @@ int spc_get_profile(const spc_handle* h, int kind, double* ms, int64_t* launches
 int spc_get_stats(const spc_handle* h, spc_stats* out) {
   if (!h || !out) return spc::set_error(SPC_ERR_ARG, "null pointer");
   *out = h->h.stats;
+  return SPC_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// yield gradient: host side (operators dH/dp and the contraction with the
+// device's reduced matrices)
+namespace {
+using cplx = std::complex<double>;
+using Mat = std::vector<cplx>;  // row-major square
+
+// Sx, Sy, Sz of multiplicity g in the basis m = S, S-1, ..., -S
+void spin_ops(int g, Mat out[3]) {
+  const double S = 0.5 * (g - 1);
+  for (int c = 0; c < 3; ++c) out[c].assign((size_t)g * g, 0.0);
+  for (int i = 0; i < g; ++i) out[2][(size_t)i * g + i] = S - i;
+  for (int i = 1; i < g; ++i) {
+    const double sp = std::sqrt(S * (S + 1) - (S - i) * (S - i + 1));  // <m_{i-1}|S+|m_i>
+    out[0][(size_t)(i - 1) * g + i] += 0.5 * sp;
+    out[0][(size_t)i * g + i - 1] += 0.5 * sp;
+    out[1][(size_t)(i - 1) * g + i] += cplx(0.0, -0.5 * sp);
+    out[1][(size_t)i * g + i - 1] += cplx(0.0, 0.5 * sp);
+  }
+}
+Mat kron(const Mat& A, int p, const Mat& B, int q) {
+  Mat C((size_t)p * q * p * q);
+  for (int i = 0; i < p; ++i)
+    for (int j = 0; j < p; ++j)
+      for (int k = 0; k < q; ++k)
+        for (int l = 0; l < q; ++l) C[(size_t)(i * q + k) * p * q + j * q + l] = A[i * p + j] * B[k * q + l];
+  return C;
+}
+Mat matmul(const Mat& A, const Mat& B, int n) {
+  Mat C((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j) C[i * n + j] += A[i * n + k] * B[k * n + j];
+  return C;
+}
+Mat eye(int n) {
+  Mat I((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) I[i * n + i] = 1.0;
+  return I;
+}
+// sum_ab O[a][b] R[a][b]
+cplx contract_op(const Mat& O, const cplx* R, int G) {
+  cplx s = 0.0;
+  for (int i = 0; i < G * G; ++i) s += O[i] * R[i];
+  return s;
+}
+}  // namespace
+
+extern "C" {
+
+int spc_yield_gradient_size(const spc_system* sys) {
+  if (!sys || sys->n_nuc1 < 0 || sys->n_nuc2 < 0) return -1;
+  return 15 + 9 * (sys->n_nuc1 + sys->n_nuc2);
+}
+
+int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta, const double* zkets,
+                       int M, double dt, double t_end, int m, int n_quad, int checkpoint_every,
+                       double wS, double wT, double* yields, double* grad) {
+  if (!h || !sys || !theta || !zkets || !yields || !grad)
+    return spc::set_error(SPC_ERR_ARG, "spc_yield_gradient: null argument");
+  if (M < 1) return spc::set_error(SPC_ERR_ARG, "M must be positive");
+  if (!(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt must be positive");
+  if (m < 1 || m > 48) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d outside [1, 48]", m);
+  if (n_quad < 1 || n_quad > 16) return spc::set_error(SPC_ERR_ARG, "n_quad %d outside [1, 16]", n_quad);
+  if (checkpoint_every < 0) return spc::set_error(SPC_ERR_ARG, "checkpoint_every must be >= 0");
+  spc::HostSystem hs;
+  int rc = spc::make_host_system(sys, SPC_H_GENERAL, hs);
+  if (rc) return rc;
+  if (h->h.krylov_method == SPC_KRYLOV_LANCZOS && !hs.herm_shift)
+    return spc::set_error(SPC_ERR_ARG, "Lanczos needs H_eff = Hermitian - i*kappa (kS == kT)");
+  for (const spc::NucInfo& q : hs.nuc)
+    if (q.g > 3)
+      return spc::set_error(SPC_ERR_UNSUPPORTED, "the yield gradient takes nuclei of multiplicity <= 3");
+  CKR(cudaSetDevice(h->h.device));
+  spc::Handle& H = h->h;
+  const int nn = (int)hs.nuc.size();
+  const int npar = 15 + 9 * nn;
+  std::fill(grad, grad + npar, 0.0);
+  yields[0] = yields[1] = 0.0;
+  const int T = spc::num_time_points(dt, t_end);
+  const int nh = T / 2;
+  if (nh < 2) return SPC_OK;  // get_kinetics adds no Simpson panel
+  const int nsteps = 2 * nh - 2;
+  std::vector<double> cw(nsteps + 1);
+  for (int k = 0; k <= nsteps; ++k)
+    cw[k] = (dt / 3.0) * ((k == 0 || k == nsteps) ? 1.0 : (k % 2 ? 4.0 : 2.0));
+  int K = checkpoint_every;
+  if (K == 0) K = (int)std::lround(std::sqrt((double)nsteps / (1.0 + n_quad)));
+  K = std::max(1, std::min(K, nsteps));
+  // H and H^H = H_eff(-kS, -kT) as batch systems 0 and 1
+  spc_system pair[2] = {*sys, *sys};
+  pair[1].kS = -sys->kS;
+  pair[1].kT = -sys->kT;
+  rc = spc_build_h_batch(h, 2, pair, SPC_H_GENERAL);
+  if (rc) return rc;
+  const int64_t Z = hs.Z;
+  if (H.ensure(H.zk, sizeof(double) * 2 * Z * M)) return SPC_ERR_ALLOC;
+  CKR(cudaMemcpyAsync(H.zk.p, zkets, sizeof(double) * 2 * Z * M, cudaMemcpyHostToDevice, H.stream));
+  std::vector<spc::GradSlot> slots;
+  slots.push_back({4, -1, 1, 0, 1});
+  std::vector<int> slot_of(nn, -1);
+  for (int j = 0; j < nn; ++j)
+    if (hs.nuc[j].g >= 2) {
+      slot_of[j] = (int)slots.size();
+      slots.push_back({2 * hs.nuc[j].g, hs.nuc[j].owner, hs.nuc[j].g, 0, hs.nuc[j].stride});
+    }
+  const double cI = wT * sys->kT, cP = wS * sys->kS - wT * sys->kT;
+  std::vector<double2> racc, facc;
+  rc = spc::yield_gradient_run(&H, theta, (const double*)H.zk.p, M, slots, dt, nsteps, cw, cI, cP, m,
+                               n_quad, K, racc, facc);
+  if (rc) return rc;
+  // sample sums in sample order
+  const int nsl = (int)slots.size();
+  const size_t con = 36;
+  std::vector<cplx> R(nsl * con, 0.0), F(con, 0.0);
+  for (int s = 0; s < M; ++s) {
+    for (int js = 0; js < nsl; ++js)
+      for (size_t i = 0; i < con; ++i) {
+        const double2 v = racc[((size_t)s * nsl + js) * con + i];
+        R[js * con + i] += cplx(v.x, v.y);
+      }
+    for (size_t i = 0; i < con; ++i) F[i] += cplx(facc[(size_t)s * con + i].x, facc[(size_t)s * con + i].y);
+  }
+  Mat s2[3], I2 = eye(2), S1[3], S2[3];
+  spin_ops(2, s2);
+  for (int r = 0; r < 3; ++r) {
+    S1[r] = kron(s2[r], 2, I2, 2);
+    S2[r] = kron(I2, 2, s2[r], 2);
+  }
+  Mat S1S2(16, 0.0);
+  for (int r = 0; r < 3; ++r) {
+    const Mat p = matmul(S1[r], S2[r], 4);
+    for (int i = 0; i < 16; ++i) S1S2[i] += p[i];
+  }
+  Mat PS(16), PT(16);
+  for (int i = 0; i < 16; ++i) {
+    const double d = (i % 5 == 0) ? 1.0 : 0.0;
+    PS[i] = 0.25 * d - S1S2[i];
+    PT[i] = 0.75 * d + S1S2[i];
+  }
+  const double inv_m = 1.0 / M;
+  // d/dp: (2/M) Im(sum_ab O_p R); the pair slot is slot 0
+  auto dpair = [&](const Mat& O) { return 2.0 * inv_m * contract_op(O, &R[0], 4).imag(); };
+  const double ps_int = contract_op(PS, F.data(), 4).real() * inv_m;
+  const double pt_int = contract_op(PT, F.data(), 4).real() * inv_m;
+  yields[0] = sys->kS * ps_int;
+  yields[1] = sys->kT * pt_int;
+  for (int c = 0; c < 3; ++c) {
+    Mat O(16);
+    for (int i = 0; i < 16; ++i) O[i] = -(S1[c][i] + S2[c][i]);
+    double g = dpair(O);
+    for (int j = 0; j < nn; ++j) {
+      if (slot_of[j] < 0) continue;
+      const int gj = hs.nuc[j].g;
+      Mat I[3];
+      spin_ops(gj, I);
+      const Mat Oj = kron(I2, 2, I[c], gj);
+      g += hs.nuc[j].gratio * 2.0 * inv_m * contract_op(Oj, &R[slot_of[j] * con], 2 * gj).imag();
+    }
+    grad[c] = g;
+  }
+  {
+    Mat O(16);
+    for (int i = 0; i < 16; ++i) O[i] = 2.0 * S1S2[i];
+    grad[3] = dpair(O);
+  }
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) grad[4 + r + 3 * c] = dpair(matmul(S1[r], S2[c], 4));
+  {
+    Mat OS(16), OT(16);
+    for (int i = 0; i < 16; ++i) {
+      OS[i] = cplx(0.0, -0.5) * PS[i];
+      OT[i] = cplx(0.0, -0.5) * PT[i];
+    }
+    grad[13] = dpair(OS) + wS * ps_int;
+    grad[14] = dpair(OT) + wT * pt_int;
+  }
+  for (int j = 0; j < nn; ++j) {
+    if (slot_of[j] < 0) continue;
+    const int gj = hs.nuc[j].g;
+    Mat I[3];
+    spin_ops(gj, I);
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        const Mat O = kron(s2[r], 2, I[c], gj);
+        grad[15 + 9 * j + r + 3 * c] = 2.0 * inv_m * contract_op(O, &R[slot_of[j] * con], 2 * gj).imag();
+      }
+  }
   return SPC_OK;
 }
 

@@ -67,7 +67,8 @@ int Handle::ensure_h_entries(size_t count) {
 Handle::~Handle() {
   Buf* all[] = {&psi, &Q,  &P,    &partial, &counters, &coef, &rbeta, &Ahess, &Aexp, &proj, &projpart,
                 &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag, &xcol, &xval, &xsplit, &plan, &jobtab,
-                &hb.rowptr, &hb.split, &hb.col, &hb.val};
+                &hb.rowptr, &hb.split, &hb.col, &hb.val, &gck, &gseg, &gnu, &gmu, &glam, &cvec2,
+                &gslots, &gracc, &gfacc};
   for (Buf* b : all)
     if (b->p) cudaFree(b->p);
   if (d_rowptr) cudaFree(d_rowptr);
@@ -143,6 +144,7 @@ int make_host_system(const spc_system* sys, int mode, HostSystem& hs) {
       const double w = -sys->B[2];
       q.zf = -(w * gm / GAMMA_E);
       for (int c = 0; c < 3; ++c) q.zeta[c] = (gm / GAMMA_E) * sys->B[c];
+      q.gratio = gm / GAMMA_E;
       hs.nuc.push_back(q);
       Z *= g;
       if (Z > (int64_t)1 << 29) return set_error(SPC_ERR_ARG, "nuclear space too large");

@@ -20,6 +20,7 @@ struct NucInfo {
   double zf;        // nuclear Zeeman factor -w*gamma/gamma_e (reference builder)
   double A[9];      // full tensor, A[r*3+c] (general builder)
   double zeta[3];   // (gamma/gamma_e) * B_c (general builder)
+  double gratio;    // gamma/gamma_e
 };
 
 // Electronic 4x4 pieces of getHiso_sp, rounded as the reference rounds them.
@@ -102,6 +103,9 @@ struct Handle {
   };
   Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
       map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit, plan, jobtab;
+  // yield-gradient workspace: checkpoints, segment states, node states,
+  // costate pair, second coordinate vector, slot table, accumulators
+  Buf gck, gseg, gnu, gmu, glam, cvec2, gslots, gracc, gfacc;
   // Hamiltonians of a batch (spc_build_h_batch): execution-order CSRs back to back
   struct HBatch {
     std::vector<int> n;
@@ -144,6 +148,17 @@ struct JobSpec {
   bool herm_shift = false;
 };
 
+// One reduced-matrix slot of the yield gradient: the electron pair (G = 4,
+// owner = -1) or (spin of electron `owner`, nucleus of multiplicity g) with
+// G = 2g classes; stride is the nucleus' stride in the nuclear index.
+struct GradSlot {
+  int G;
+  int owner;
+  int g;
+  int pad;
+  int64_t stride;
+};
+
 int set_error(int code, const char* fmt, ...);
 int build_h_device(Handle* h, const HostSystem& hs, int mode);
 int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev,
@@ -151,6 +166,14 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
 int propagate_batch(Handle* h, const double* theta, const double* init_pop,
                     const std::vector<JobSpec>& jobs, double dt, double t_end, int m, double tol,
                     int T);
+// Adjoint sweep of spc_yield_gradient on the batch store's systems 0 (H) and
+// 1 (H^H): per-sample reduced matrices racc (slots x cs.size() x 36 complex)
+// of the gradient integrals and facc (slots x 36) of sum_k cw[k] psi_k psi_k^H
+// on the electron pair.
+int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int M,
+                       const std::vector<GradSlot>& cs, double dt, int nsteps,
+                       const std::vector<double>& cw, double cI, double cP, int m, int nq, int K,
+                       std::vector<double2>& racc_h, std::vector<double2>& facc_h);
 // Nonzero count spc_build_h produces for a system (closed form per mode).
 int64_t predict_nnz(const HostSystem& hs, int mode);
 int num_time_points(double dt, double t_end);

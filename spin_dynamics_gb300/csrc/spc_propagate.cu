@@ -1230,4 +1230,6 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   return propagate_batch(h, theta, init_pop, std::vector<JobSpec>{j}, dt, t_end, m, tol, T);
 }
 
+#include "spc_adjoint.cuh"
+
 }  // namespace spc

@@ -13,6 +13,7 @@ sets per field (app/main.f90:53-54), exactly as in the reference.
 from __future__ import annotations
 
 import ctypes as C
+from dataclasses import dataclass
 from typing import Optional, Sequence
 
 import numpy as np
@@ -93,6 +94,29 @@ def seeded_samples(seed: Sequence[int], Z: int, M: int, serial: bool = False) ->
     s1 = s1 - 2**64 if s1 >= 2**63 else s1
     nat.check(nat.lib().spc_seeded_samples(s0, s1, Z, M, 1 if serial else 0, _dptr(out)))
     return out.view(np.complex128).reshape(M, Z)
+
+
+@dataclass
+class YieldGradient:
+    """Yields and gradient of spc_yield_gradient. Tensors are (row, col)
+    matrices; `raw` is the C layout (column-major tensors)."""
+    Phi_S: float
+    Phi_T: float
+    B: np.ndarray
+    J: float
+    D: np.ndarray
+    kS: float
+    kT: float
+    A1: list
+    A2: list
+    raw: np.ndarray
+
+    @staticmethod
+    def unpack(y, g, n1: int, n2: int) -> "YieldGradient":
+        mat = lambda v: np.asarray(v).reshape(3, 3).T.copy()
+        A = [mat(g[15 + 9 * j:24 + 9 * j]) for j in range(n1 + n2)]
+        return YieldGradient(float(y[0]), float(y[1]), g[0:3].copy(), float(g[3]), mat(g[4:13]),
+                             float(g[13]), float(g[14]), A[:n1], A[n1:], g.copy())
 
 
 class TraceSampler:
@@ -244,6 +268,26 @@ class TraceSampler:
         nat.check(nat.lib().spc_trace_sampling_batch_device(
             self._h, len(M), _dptr(js) if js is not None else None, _dptr(M), _dptr(th), _dptr(pop),
             C.c_void_p(zk_ptr), float(dt), float(t_end), int(m), float(tol), C.c_void_p(out_ptr), T))
+
+    def yield_gradient(self, sys: SysParam, B, zkets, dt: float, t_end: float, m: int,
+                       n_quad: int = 6, checkpoint_every: int = 0, wS: float = 1.0, wT: float = 0.0,
+                       init_state: str = "singlet") -> "YieldGradient":
+        """Yields (Phi_S, Phi_T) of the stepwise propagation and the gradient
+        of wS*Phi_S + wT*Phi_T with respect to every parameter of the system
+        (internal units: mT for B, J, D, A; kS, kT as stored), by the discrete
+        adjoint; the general Hamiltonian (anisotropic A, field vector)."""
+        st, keep = make_system(sys, B)
+        npar = nat.lib().spc_yield_gradient_size(C.byref(st))
+        zk = np.ascontiguousarray(zkets, np.complex128)
+        th, _ = init_el_state(init_state)
+        th = np.ascontiguousarray(th).view(np.float64)
+        y = np.zeros(2)
+        g = np.zeros(npar)
+        nat.check(nat.lib().spc_yield_gradient(
+            self._h, C.byref(st), _dptr(th), _dptr(zk.view(np.float64)), zk.shape[0], float(dt),
+            float(t_end), int(m), int(n_quad), int(checkpoint_every), float(wS), float(wT), _dptr(y),
+            _dptr(g)))
+        return YieldGradient.unpack(y, g, len(sys.e1.g_I), len(sys.e2.g_I))
 
     def stats(self) -> dict:
         s = nat.spc_stats()

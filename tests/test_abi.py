@@ -73,3 +73,12 @@ def test_time_points_and_initial_states(oracle):
         th2, pop2 = oracle.init_el_state(s)
         assert np.array_equal(th, th2) and np.array_equal(pop, pop2)
     assert nat.lib().spc_num_time_points(0.0, 1.0) == -1
+
+
+def test_yield_gradient_size_is_host_only():
+    from spin_dynamics_gb300 import workloads as W
+    from spin_dynamics_gb300.dynamics import make_system
+    s = W.small_pair()
+    st, keep = make_system(s, 0.05)
+    assert nat.lib().spc_yield_gradient_size(C.byref(st)) == 15 + 9 * 5
+    assert nat.lib().spc_yield_gradient_size(None) == -1

@@ -1,0 +1,130 @@
+"""Adjoint gradient of the yields (spc_yield_gradient) against central finite
+differences of the dense stepwise model, plus its schedule invariances."""
+import numpy as np
+import pytest
+
+import dense
+from spin_dynamics_gb300 import workloads as W
+from spin_dynamics_gb300.dynamics import num_time_points
+from spin_dynamics_gb300.spinsys import GAMMA_E, Electron, SysParam
+
+pytestmark = pytest.mark.gpu
+DT = 1.0 * GAMMA_E / 1000
+# gradient entries: |g - g_fd| <= GRAD_RTOL * max|g_fd| (central differences of
+# the dense model carry ~1e-9 relative error; the Gauss-Legendre rule with 8
+# nodes and exact Krylov spaces are far below that)
+GRAD_RTOL = 2e-7
+
+
+def aniso_pair(g1, g2, seed, kS, kT):
+    rng = np.random.default_rng(seed)
+    t = lambda: (lambda R: R @ np.diag(rng.uniform(-1.5, 1.5, 3)) @ R.T)(W._haar_rotation(rng))
+    return SysParam(e1=Electron(g_I=list(g1), A=[t() for _ in g1]),
+                    e2=Electron(g_I=list(g2), A=[t() for _ in g2]),
+                    J=0.03, D=W.axial_dipolar(-0.3) + 0.05 * np.eye(3)[[1, 0, 2]],
+                    kS=kS, kT=kT)
+
+
+def pack(s, B):
+    A = [a.reshape(3, 3).T.reshape(9) for a in list(s.e1.A) + list(s.e2.A)]
+    return np.concatenate([np.asarray(B, float), [s.J], np.asarray(s.D).T.reshape(9), [s.kS, s.kT]]
+                          + A)
+
+
+def dense_objective(s, v, zk, t_end, wS, wT):
+    n1 = len(s.e1.g_I)
+    A = [v[15 + 9 * j:24 + 9 * j].reshape(3, 3).T for j in range(len(s.e1.g_I) + len(s.e2.g_I))]
+    H = dense.hamiltonian(s.e1.g_I, A[:n1], s.e2.g_I, A[n1:], v[0:3], v[3], v[4:13].reshape(3, 3).T,
+                          v[13], v[14])
+    T = num_time_points(DT, t_end)
+    PhiS, PhiT = dense.stepwise_yields(H, zk, DT, T, v[13], v[14])
+    return wS * PhiS + wT * PhiT, (PhiS, PhiT)
+
+
+def fd_gradient(s, B, zk, t_end, wS, wT, h=1e-5):
+    v0 = pack(s, B)
+    g = np.zeros_like(v0)
+    for i in range(v0.size):
+        vp, vm = v0.copy(), v0.copy()
+        vp[i] += h
+        vm[i] -= h
+        g[i] = (dense_objective(s, vp, zk, t_end, wS, wT)[0] -
+                dense_objective(s, vm, zk, t_end, wS, wT)[0]) / (2 * h)
+    return g
+
+
+@pytest.mark.parametrize("rates", [(1.3, 0.4), (0.8, 0.8)], ids=["unequal", "equal"])
+def test_gradient_matches_dense_finite_differences(sampler, rates):
+    kS, kT = rates[0] / GAMMA_E * 50, rates[1] / GAMMA_E * 50
+    s = aniso_pair([2], [2, 3], seed=5, kS=kS, kT=kT)  # dim 48
+    B = np.array([0.11, -0.07, 0.2])
+    zk = W.random_phase_samples(s.Z, 5, seed=9)
+    t_end = 12 * DT
+    got = sampler.yield_gradient(s, B, zk, DT, t_end, m=48, n_quad=8)
+    _, (PhiS, PhiT) = dense_objective(s, pack(s, B), zk, t_end, 1.0, 0.0)
+    assert abs(got.Phi_S - PhiS) <= 1e-12 * max(1.0, abs(PhiS))
+    assert abs(got.Phi_T - PhiT) <= 1e-12 * max(1.0, abs(PhiT))
+    ref = fd_gradient(s, B, zk, t_end, 1.0, 0.0)
+    scale = np.max(np.abs(ref))
+    err = np.abs(got.raw - ref)
+    assert np.max(err) <= GRAD_RTOL * scale, (np.argmax(err), got.raw[np.argmax(err)], ref[np.argmax(err)])
+
+
+def test_triplet_objective_and_truncated_krylov(sampler):
+    """wT Phi_T at dim 288 with a Krylov dimension below the space (m = 28)."""
+    s = W.small_pair()
+    rng = np.random.default_rng(3)
+    for e in (s.e1, s.e2):
+        e.A = [(lambda R: R @ np.diag(rng.uniform(-1, 1, 3)) @ R.T)(W._haar_rotation(rng)) for _ in e.A]
+    s.J, s.D = 0.02, W.axial_dipolar(-0.2)
+    s.kS, s.kT = 20.0 / GAMMA_E, 5.0 / GAMMA_E
+    B = np.array([0.0, 0.03, 0.05])
+    zk = W.random_phase_samples(s.Z, 3, seed=4)
+    t_end = 8 * DT
+    got = sampler.yield_gradient(s, B, zk, DT, t_end, m=28, n_quad=8, wS=0.0, wT=1.0)
+    ref = fd_gradient(s, B, zk, t_end, 0.0, 1.0)
+    err = np.abs(got.raw - ref)
+    assert np.max(err) <= 1e-6 * np.max(np.abs(ref)), (np.argmax(err), got.raw[np.argmax(err)], ref[np.argmax(err)])
+
+
+def test_lanczos_matches_mgs_and_finite_differences(sampler):
+    """kS == kT at dim 288 with m = 24: the three-term recurrence (explicit
+    SPC_KRYLOV_LANCZOS) against full MGS and the dense model."""
+    s = W.small_pair()
+    rng = np.random.default_rng(11)
+    for e in (s.e1, s.e2):
+        e.A = [(lambda R: R @ np.diag(rng.uniform(-1, 1, 3)) @ R.T)(W._haar_rotation(rng)) for _ in e.A]
+    s.J, s.D = 0.02, W.axial_dipolar(-0.2)
+    s.kS = s.kT = 10.0 / GAMMA_E
+    B = np.array([0.02, 0.0, 0.06])
+    zk = W.random_phase_samples(s.Z, 4, seed=6)
+    t_end = 9 * DT
+    mgs = sampler.yield_gradient(s, B, zk, DT, t_end, m=24, n_quad=8)
+    sampler.set_krylov("lanczos")
+    try:
+        lz = sampler.yield_gradient(s, B, zk, DT, t_end, m=24, n_quad=8)
+    finally:
+        sampler.set_krylov("mgs")
+    scale = np.max(np.abs(mgs.raw))
+    assert np.max(np.abs(lz.raw - mgs.raw)) <= 1e-10 * scale
+    ref = fd_gradient(s, B, zk, t_end, 1.0, 0.0)
+    assert np.max(np.abs(mgs.raw - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+def test_checkpoint_spacing_does_not_change_results(sampler):
+    s = aniso_pair([2, 2], [3], seed=2, kS=0.02, kT=0.01)
+    B = np.array([0.05, 0.0, 0.1])
+    zk = W.random_phase_samples(s.Z, 40, seed=1)  # two tiles, one partial
+    t_end = 13 * DT
+    runs = [sampler.yield_gradient(s, B, zk, DT, t_end, m=20, n_quad=4, checkpoint_every=K)
+            for K in (0, 1, 3, 100)]
+    for r in runs[1:]:
+        assert np.array_equal(r.raw, runs[0].raw)
+        assert r.Phi_S == runs[0].Phi_S
+
+
+def test_short_window_has_zero_yield(sampler):
+    s = W.notebook_pair()
+    zk = W.random_phase_samples(s.Z, 2, seed=1)
+    got = sampler.yield_gradient(s, 0.05, zk, DT, 0.5 * DT, m=8)  # T = 3: no Simpson panel
+    assert got.Phi_S == 0.0 and not np.any(got.raw)
