@@ -64,6 +64,11 @@ def parse():
     p.add_argument("--batch-orient", type=int, default=4)
     p.add_argument("--batch-window-ns", type=float, default=20.0)
     p.add_argument("--batch-krylov", type=int, default=20)
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient leg")
+    p.add_argument("--adjoint-samples", type=int, default=256)
+    p.add_argument("--adjoint-window-ns", type=float, default=20.0)
+    p.add_argument("--adjoint-checkpoint", type=int, default=10)
+    p.add_argument("--adjoint-quad", type=int, default=6)
     return p.parse_args()
 
 
@@ -261,9 +266,10 @@ def run_ours(args, rank, world, local_rank):
                "h2d_bytes_per_step": int(zk_host.nbytes), "d2h_bytes_per_step": int(4 * T * 8),
                "ms_per_step": el * 1e3}
     batched = None if args.no_batch else batched_leg(args, sampler, local_rank)
+    adjoint = None if args.no_adjoint else adjoint_leg(args, sampler, value / world)
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
-    return dict(ms=ms, value=value, e2e=e2e, batched=batched, prof=prof, clocks=clk.summary(), launches=launches,
+    return dict(ms=ms, value=value, e2e=e2e, batched=batched, adjoint=adjoint, prof=prof, clocks=clk.summary(), launches=launches,
                 builds=builds, fallbacks=fallbacks, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
                 sysp=sysp, B=B, sim=sim)
 
@@ -326,6 +332,68 @@ def batched_leg(args, sampler, local_rank):
             "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m,
             "workload": "uneven pairs (2-10 nuclei from 1H/14N, anisotropic) x Fibonacci-sphere "
                         "orientations at 0.05 mT, own Hamiltonian per job"}
+
+
+def adjoint_leg(args, sampler, plain_value):
+    """Yields and their gradient with respect to all 15 + 9*12 parameters of
+    the large pair (spc_yield_gradient, host sample vectors in, gradient out)
+    against the stepwise forward it differentiates and the plain Krylov-reuse
+    forward of the headline measurement."""
+    import torch
+
+    sysp, B = W.large_pair()
+    dt = 1.0 * 176.08596 / 1000
+    t_end = args.adjoint_window_ns * 176.08596 / 1000
+    M, m = args.adjoint_samples, args.krylov
+    zk = W.random_phase_samples(sysp.Z, M, seed=11)
+    method = "lanczos" if args.method in ("auto", "lanczos") and sysp.kS == sysp.kT else "mgs"
+    sampler.set_krylov(method)
+    try:
+        def grad():
+            return sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=args.adjoint_quad,
+                                          checkpoint_every=args.adjoint_checkpoint)
+
+        def fwd():
+            return sampler.stepwise_yields(sysp, B, zk, dt, t_end, m)
+
+        def timed(fn):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = fn()
+            torch.cuda.synchronize()
+            return r, time.perf_counter() - t0
+
+        # untimed first call (allocation, page-in) with per-kernel-class timing
+        import ctypes as C
+        from spin_dynamics_gb300 import _native as nat
+        nat.check(nat.lib().spc_set_profiling(sampler.handle, 1))
+        grad()
+        breakdown = {}
+        for k in range(nat.SPC_KERNEL_KINDS):
+            a, n, f, b = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
+            nat.lib().spc_get_profile(sampler.handle, k, C.byref(a), C.byref(n), C.byref(f), C.byref(b))
+            if n.value:
+                breakdown[nat.lib().spc_kernel_kind_name(k).decode()] = {
+                    "ms": round(a.value, 3), "launches": n.value,
+                    "tflops": round(f.value / (a.value / 1e3) / 1e12, 4) if a.value else None}
+        nat.check(nat.lib().spc_set_profiling(sampler.handle, 0))
+        g, t_grad = timed(grad)
+        st = sampler.stats()
+        y, t_fwd = timed(fwd)
+    finally:
+        sampler.set_krylov(args.method)
+    steps = st["sample_steps"] // M
+    work = M * steps
+    return {"value": work / t_grad, "unit": "sample-steps/s", "seconds": t_grad,
+            "stepwise_forward_value": work / t_fwd, "cost_vs_stepwise_forward": t_grad / t_fwd,
+            "cost_vs_plain_forward": t_grad / (work / plain_value),
+            "params": int(g.raw.size), "samples": M, "dt_steps": int(steps), "krylov": m,
+            "krylov_method": method, "quadrature_nodes": args.adjoint_quad,
+            "checkpoint_every": args.adjoint_checkpoint, "node_states_kept": bool(st["rounds"]),
+            "krylov_builds": int(st["krylov_builds"]), "kernel_launches": int(st["kernel_launches"]),
+            "Phi_S": g.Phi_S, "Phi_S_forward_only": y[0], "kernel_breakdown": breakdown,
+            "workload": "large pair dim 55296 (anisotropic), gradient of Phi_S over B, J, D, kS, kT "
+                        "and every hyperfine tensor element; h2d of the sample vectors inside"}
 
 
 def main():
@@ -397,7 +465,7 @@ def main():
                           "fp64": {"achieved_tflops": ach_tf, "peak_tflops": r["fp64_peak"] / 1e12,
                                    "frac": (ach_tf * 1e12 / r["fp64_peak"]) if ach_tf else None,
                                    "peak_source": "measured DFMA probe (spc_fp64_peak)"}},
-                kernel_share=share, batched=r["batched"], cpu_baseline=cpu)
+                kernel_share=share, batched=r["batched"], adjoint=r["adjoint"], cpu_baseline=cpu)
     print(json.dumps(line))
 
 

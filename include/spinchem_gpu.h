@@ -231,17 +231,22 @@ int spc_yield_gradient_size(const spc_system* sys);
  *   n_quad           Gauss-Legendre nodes per step for the derivative of
  *                    exp(-i H dt) (1..16; 6 gives ~1e-8 relative error at
  *                    ||H|| dt ~ 5)
- *   checkpoint_every forward states kept every this many steps (0 = about
- *                    sqrt(steps / (1 + n_quad)), the least device memory)
+ *   checkpoint_every forward states kept every this many steps (0 = the
+ *                    largest spacing that fits in device memory: the fewest
+ *                    recomputed steps)
  *   yields           2 doubles: Phi_S, Phi_T
- *   grad             spc_yield_gradient_size(sys) doubles:
+ *   grad             NULL: yields only (the forward sweep, one Krylov build
+ *                    per sample and step); else spc_yield_gradient_size(sys) doubles:
  *                    dB[3], dJ, dD[9] (column-major as spc_system.D), dkS, dkT,
  *                    then 9 per nucleus (radical 1's, then radical 2's),
  *                    column-major as spc_system.A1/A2
- * Device memory: about (m + 4 + n_steps/K + (1 + n_quad) K) states of
- * 16 * n * ceil(M/32)*32 bytes. Nuclei of multiplicity above 3 return
- * SPC_ERR_UNSUPPORTED. The handle's Hamiltonian and batch are replaced by H
- * and H^H. Cost: three Krylov builds per sample and step. */
+ * Device memory: about (m + 6 + n_steps/K + (1 + n_quad) K) states of
+ * 16 * n * ceil(M/32)*32 bytes, or (m + 6 + n_steps/K + K + n_quad) when that
+ * does not fit (node states rebuilt per step); SPC_ERR_ALLOC when neither
+ * fits. Nuclei of multiplicity above 3 return SPC_ERR_UNSUPPORTED. The
+ * handle's Hamiltonian and batch are replaced by H and H^H. Cost: three
+ * Krylov builds per sample and step (four when node states are rebuilt);
+ * spc_get_stats reports rounds = 1 when node states were kept. */
 int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta,
                        const double* zkets, int M, double dt, double t_end, int m, int n_quad,
                        int checkpoint_every, double wS, double wT, double* yields, double* grad);
@@ -290,7 +295,7 @@ int spc_set_profiling(spc_handle* h, int enable);
 /* Accumulated time (ms), launches, and the algorithmic FLOPs and bytes of
  * kernel class `kind` (0 <= kind < SPC_KERNEL_KINDS) since profiling was
  * enabled. */
-#define SPC_KERNEL_KINDS 11
+#define SPC_KERNEL_KINDS 13
 int spc_get_profile(const spc_handle* h, int kind, double* ms, int64_t* launches, double* flops,
                     double* bytes);
 

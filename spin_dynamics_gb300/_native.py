@@ -89,7 +89,7 @@ SIGNATURES = {
     "spc_kernel_kind_name": (C.c_char_p, [_I]),
     "spc_fp64_peak": (_I, [_I, C.POINTER(_D)]),
 }
-SPC_KERNEL_KINDS = 11
+SPC_KERNEL_KINDS = 13
 
 _LIB: C.CDLL | None = None
 

@@ -26,7 +26,9 @@
 // recomputes each segment from its checkpoint, and the Krylov basis built at
 // psi_k for psi_{k+1} also gives the node states exp(-i H x_q dt) psi_k, kept
 // for the segment. Per step: three Krylov builds (forward, recompute, costate)
-// and 2*nq + 2 basis applications.
+// and 2*nq + 2 basis applications. When a segment's node states do not fit in
+// device memory they are rebuilt per step instead (four builds per step).
+// Without a gradient only the forward sweep runs (one build per step).
 
 #define CON_MAXG 6
 
@@ -182,7 +184,7 @@ static void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>&
 int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int M,
                        const std::vector<GradSlot>& cs, double dt, int nsteps,
                        const std::vector<double>& cw, double cI, double cP, int m, int nq, int K,
-                       std::vector<double2>& racc_h, std::vector<double2>& facc_h) {
+                       bool want_grad, std::vector<double2>& racc_h, std::vector<double2>& facc_h) {
   auto t_start = std::chrono::steady_clock::now();
   cudaStream_t st = h->stream;
   const auto& HB = h->hb;
@@ -192,8 +194,6 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   const int ntiles = ldp / SPC_LANES, nslots = ldp;
   const int nsl = (int)cs.size();
   const size_t S = (size_t)n * ldp;  // one state of all samples (psi layout)
-  const int nck = nsteps / K + 1;
-  const int a_last = ((nsteps - 1) / K) * K;  // first step of the last segment
   const size_t mm = (size_t)m * m;
   // chunks per (tile, slot): about two waves of one-warp CTAs
   const int nch = (int)std::max<int64_t>(
@@ -201,8 +201,47 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   const size_t npairs = (size_t)ntiles * nsl;
   const int items_cap = h->sm_count * 32 + ntiles;
   const size_t con = (size_t)CON_MAXG * CON_MAXG;
-  if (h->ensure(h->gck, sizeof(double2) * S * nck) || h->ensure(h->gseg, sizeof(double2) * S * (K + 1)) ||
-      h->ensure(h->gnu, sizeof(double2) * S * K * nq) || h->ensure(h->gmu, sizeof(double2) * S) ||
+  const double elems = (double)n * M;  // vector entries of one state over the samples
+  // Node states of a whole segment are kept (one Krylov build per step saved)
+  // when they fit in device memory; otherwise they are rebuilt per step.
+  // Checkpoint spacing K and whether a segment's node states are kept (one
+  // Krylov build per step saved). K = 0 picks the largest spacing whose
+  // states fit in device memory (fewest recomputed segments), else the
+  // spacing of least memory with node states rebuilt per step.
+  bool cache = false;
+  if (want_grad) {
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const double held = (double)h->gck.bytes + h->gseg.bytes + h->gnu.bytes + h->Q.bytes + h->gmu.bytes +
+                        h->glam.bytes + h->P.bytes;
+    const double avail = 0.85 * ((double)free_b + held) - (double)(1 << 28);
+    const double st = sizeof(double2) * (double)S;
+    auto need = [&](int k, bool keep) {
+      return st * ((double)m + 4.0 + (nsteps / k + 1) + k + 1.0 + (keep ? (double)k * nq : (double)nq));
+    };
+    if (K == 0) {
+      for (int k = nsteps; k >= 1 && K == 0; --k)
+        if (need(k, true) <= avail) K = k;
+      if (K) {
+        cache = true;
+      } else {
+        K = std::max(1, (int)std::lround(std::sqrt((double)nsteps)));
+      }
+    } else {
+      cache = need(K, true) <= avail;
+    }
+    if (!cache && need(K, false) > avail)
+      return set_error(SPC_ERR_ALLOC,
+                       "yield gradient needs %.1f GB of device memory at checkpoint spacing %d (%.1f GB free)",
+                       need(K, false) / 1e9, K, free_b / 1e9);
+  }
+  if (K < 1) K = 1;
+  const int nck = nsteps / K + 1;
+  const int a_last = ((nsteps - 1) / K) * K;  // first step of the last segment
+  const size_t n_ck = want_grad ? nck : 0, n_seg = want_grad ? K + 1 : 0;
+  const size_t n_nu = want_grad ? (cache ? (size_t)K * nq : (size_t)nq) : 0;
+  if (h->ensure(h->gck, sizeof(double2) * S * n_ck) || h->ensure(h->gseg, sizeof(double2) * S * n_seg) ||
+      h->ensure(h->gnu, sizeof(double2) * S * n_nu) || h->ensure(h->gmu, sizeof(double2) * S) ||
       h->ensure(h->glam, sizeof(double2) * S * 2) || h->ensure(h->Q, sizeof(double2) * m * S) ||
       h->ensure(h->P, sizeof(double2) * S) ||
       h->ensure(h->partial, sizeof(double2) * std::max<size_t>((size_t)items_cap * SPC_LANES,
@@ -290,7 +329,7 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * nslots, st));
   CK(cudaMemsetAsync(h->err.p, 0, 16, st));
   // psi_0 = theta (x) z: into the last segment's buffer when it is the only one
-  double2* psi0 = a_last == 0 ? seg : ck;
+  double2* psi0 = !want_grad ? lam : a_last == 0 ? seg : ck;
   CK(cudaMemsetAsync(psi0, 0, sizeof(double2) * S, st));
   {
     JobInit ji{Z, 0, M, ldp, (const double2*)zk_dev};
@@ -329,11 +368,17 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
     pa.partial = d_part;
     pa.counters = d_cnt;
     pa.lanczos = lanczos ? 1 : 0;
+    int pe = h->prof.begin(st);
     k_rowpass<PASS_NORM_GATHER><<<nip, blk, 0, st>>>(pa);
+    h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
+    pe = h->prof.begin(st);
     k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 1, 0, pa.rbeta, d_Q);
+    h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
     h->count_launch(2);
     for (int i = 0; i < m; ++i) {
+      pe = h->prof.begin(st);
       k_spmm<<<nis, blk, 0, st>>>(tiles, d_items_s, d_map, i, d_Q, d_P);
+      h->prof.end(st, pe, PK_SPMM, 8.0 * (double)HB.nnz[0] * nslots, 20.0 * (double)HB.nnz[0] * ntiles + 32.0 * elems);
       h->count_launch();
       pa.col_i = i;
       int j0 = 0;
@@ -342,21 +387,29 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
       } else {
         pa.row_j = 0;
         pa.jx = 0;
+        pe = h->prof.begin(st);
         k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
+        h->prof.end(st, pe, PK_DOT, 8.0 * elems, 32.0 * elems);
         h->count_launch();
       }
       for (int j = j0; j < i; ++j) {
         pa.jx = j;
         pa.jn = j + 1;
         pa.row_j = j + 1;
+        pe = h->prof.begin(st);
         k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
+        h->prof.end(st, pe, PK_AXPY_DOT, 16.0 * elems, 64.0 * elems);
         h->count_launch();
       }
       if (i < m - 1) {
         pa.jx = i;
         pa.row_j = i + 1;
+        pe = h->prof.begin(st);
         k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
+        h->prof.end(st, pe, PK_AXPY_NORM, 12.0 * elems, 48.0 * elems);
+        pe = h->prof.begin(st);
         k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 0, i + 1, pa.rbeta, d_Q);
+        h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
         h->count_launch(2);
       }
     }
@@ -365,20 +418,38 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   };
   // y = exp(-i tau H) x from the current basis (tau < 0 runs backwards)
   auto apply = [&](double tau, const TileInfo* tiles, double2* y) {
+    int pe = h->prof.begin(st);
     k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, tiles, d_map, d_A, d_E, tau, d_err);
+    h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * M, 32.0 * (double)mm * M);
+    pe = h->prof.begin(st);
     k_first_col<<<(nslots + 127) / 128, 128, 0, st>>>(nslots, tiles, d_map, m, d_E, d_c, d_c2);
+    h->prof.end(st, pe, PK_SETUP, 2.0 * m * M, 32.0 * m * M);
+    pe = h->prof.begin(st);
     k_psi_update<<<nip, blk, 0, st>>>(tiles, d_items, m, d_map, d_scol, d_flag, d_Q, d_c2, y);
+    h->prof.end(st, pe, PK_PSI, 8.0 * m * elems, 16.0 * (m + 1) * elems);
     h->count_launch(3);
   };
   // acc += w * reduced matrices of (mu, nu); nsl_ = 1 takes the electron pair only
+  // algorithmic FLOPs and bytes of one contraction over the first nsl_ slots
+  auto con_cost = [&](int nsl_, double& f, double& by) {
+    f = by = 0.0;
+    for (int j = 0; j < nsl_; ++j) {
+      const double L = cs[j].owner < 0 ? (double)Z : 2.0 * Z / cs[j].g;
+      f += 8.0 * cs[j].G * cs[j].G * L * M;
+    }
+    by = 32.0 * elems;
+  };
+  double con_f1, con_b1, con_fn, con_bn;
+  con_cost(1, con_f1, con_b1);
+  con_cost(nsl, con_fn, con_bn);
   auto contract = [&](const double2* mu, const double2* nu, double w, int nsl_, double2* acc) {
     const int nb = ntiles * nsl_ * nch;
+    int pe = h->prof.begin(st);
     k_contract<4><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, nsl_, nch, mu, nu, w, d_part, d_cnt, acc);
-    h->count_launch();
-    if (nsl_ > 1) {
+    if (nsl_ > 1)
       k_contract<6><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, nsl_, nch, mu, nu, w, d_part, d_cnt, acc);
-      h->count_launch();
-    }
+    h->prof.end(st, pe, PK_CONTRACT, nsl_ > 1 ? con_fn : con_f1, nsl_ > 1 ? con_bn : con_b1);
+    h->count_launch(nsl_ > 1 ? 2 : 1);
   };
   // basis at psi_k under H: node states nu_q and psi_{k+1}
   auto step_forward = [&](const double2* x, double2* nodes, double2* y) {
@@ -397,40 +468,52 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   for (int k = 0; k < nsteps; ++k) {
     if (cw[k] != 0.0) contract(cur, cur, cw[k], 1, d_facc);
     double2* nxt;
-    if (k + 1 >= a_last)
+    if (want_grad && k + 1 >= a_last)
       nxt = seg + S * (k + 1 - a_last);
-    else if ((k + 1) % K == 0)
+    else if (want_grad && (k + 1) % K == 0)
       nxt = ck + S * ((k + 1) / K);
     else
       nxt = cur == gmu ? ulam : gmu;
-    int rc = step_forward(cur, k >= a_last ? gnu + S * nq * (k - a_last) : nullptr, nxt);
+    int rc = step_forward(cur, want_grad && cache && k >= a_last ? gnu + S * nq * (k - a_last) : nullptr, nxt);
     if (rc) return rc;
     cur = nxt;
   }
   if (cw[nsteps] != 0.0) contract(cur, cur, cw[nsteps], 1, d_facc);
   // backward sweep
-  CK(cudaMemsetAsync(lam, 0, sizeof(double2) * S, st));
-  k_costate<<<lgrid, blk, 0, st>>>(d_tf, d_map, d_scol, cur, lam, cw[nsteps] * cI, cw[nsteps] * cP, lam);
-  h->count_launch();
-  for (int a = a_last; a >= 0; a -= K) {
+  if (want_grad) {
+    CK(cudaMemsetAsync(lam, 0, sizeof(double2) * S, st));
+    int pe = h->prof.begin(st);
+    k_costate<<<lgrid, blk, 0, st>>>(d_tf, d_map, d_scol, cur, lam, cw[nsteps] * cI, cw[nsteps] * cP, lam);
+    h->prof.end(st, pe, PK_COSTATE, 6.0 * elems, 48.0 * elems);
+    h->count_launch();
+  }
+  for (int a = want_grad ? a_last : -1; a >= 0; a -= K) {
     const int b = std::min(nsteps, a + K);
     if (a != a_last) {
       CK(cudaMemcpyAsync(seg, ck + S * (a / K), sizeof(double2) * S, cudaMemcpyDeviceToDevice, st));
       for (int k = a; k < b; ++k) {
-        int rc = step_forward(seg + S * (k - a), gnu + S * nq * (k - a), seg + S * (k - a + 1));
+        int rc = step_forward(seg + S * (k - a), cache ? gnu + S * nq * (k - a) : nullptr, seg + S * (k - a + 1));
         if (rc) return rc;
       }
     }
     for (int k = b - 1; k >= a; --k) {
+      double2* nodes = gnu + S * nq * (cache ? k - a : 0);
+      if (!cache) {
+        int rc = build(seg + S * (k - a), d_tf);
+        if (rc) return rc;
+        for (int q = 0; q < nq; ++q) apply(dt * xq[q], d_tf, nodes + S * q);
+      }
       int rc = build(lam, d_tb);
       if (rc) return rc;
       for (int q = 0; q < nq; ++q) {
         apply(-dt * (1.0 - xq[q]), d_tb, gmu);
-        contract(gmu, gnu + S * (nq * (k - a) + q), wq[q] * dt, nsl, d_racc);
+        contract(gmu, nodes + S * q, wq[q] * dt, nsl, d_racc);
       }
       apply(-dt, d_tb, ulam);
+      int pe = h->prof.begin(st);
       k_costate<<<lgrid, blk, 0, st>>>(d_tf, d_map, d_scol, seg + S * (k - a), ulam, cw[k] * cI,
                                        cw[k] * cP, lam);
+      h->prof.end(st, pe, PK_COSTATE, 6.0 * elems, 48.0 * elems);
       h->count_launch();
     }
   }
@@ -442,10 +525,11 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   int err_h[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(err_h, h->err.p, 16, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  h->prof.collect();
   h->stats.krylov_builds = builds;
   h->stats.lanczos_fallbacks = 0;
-  h->stats.rounds = 0;
-  h->stats.sample_steps = (int64_t)nsteps * M;
+  h->stats.sample_steps = (int64_t)(cw.size() - 1) * M;
+  h->stats.rounds = cache ? 1 : 0;  // 1: node states kept per segment
   h->stats.kernel_launches = h->launches - launches0;
   h->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   if (err_h[0] == 2) return set_error(SPC_ERR_NUMERIC, "singular Pade denominator in expm");

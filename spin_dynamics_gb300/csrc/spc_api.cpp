@@ -450,7 +450,7 @@ int spc_yield_gradient_size(const spc_system* sys) {
 int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta, const double* zkets,
                        int M, double dt, double t_end, int m, int n_quad, int checkpoint_every,
                        double wS, double wT, double* yields, double* grad) {
-  if (!h || !sys || !theta || !zkets || !yields || !grad)
+  if (!h || !sys || !theta || !zkets || !yields)
     return spc::set_error(SPC_ERR_ARG, "spc_yield_gradient: null argument");
   if (M < 1) return spc::set_error(SPC_ERR_ARG, "M must be positive");
   if (!(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt must be positive");
@@ -469,7 +469,7 @@ int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta
   spc::Handle& H = h->h;
   const int nn = (int)hs.nuc.size();
   const int npar = 15 + 9 * nn;
-  std::fill(grad, grad + npar, 0.0);
+  if (grad) std::fill(grad, grad + npar, 0.0);
   yields[0] = yields[1] = 0.0;
   const int T = spc::num_time_points(dt, t_end);
   const int nh = T / 2;
@@ -478,9 +478,7 @@ int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta
   std::vector<double> cw(nsteps + 1);
   for (int k = 0; k <= nsteps; ++k)
     cw[k] = (dt / 3.0) * ((k == 0 || k == nsteps) ? 1.0 : (k % 2 ? 4.0 : 2.0));
-  int K = checkpoint_every;
-  if (K == 0) K = (int)std::lround(std::sqrt((double)nsteps / (1.0 + n_quad)));
-  K = std::max(1, std::min(K, nsteps));
+  const int K = std::min(checkpoint_every, nsteps);  // 0: chosen by device memory
   // H and H^H = H_eff(-kS, -kT) as batch systems 0 and 1
   spc_system pair[2] = {*sys, *sys};
   pair[1].kS = -sys->kS;
@@ -501,7 +499,7 @@ int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta
   const double cI = wT * sys->kT, cP = wS * sys->kS - wT * sys->kT;
   std::vector<double2> racc, facc;
   rc = spc::yield_gradient_run(&H, theta, (const double*)H.zk.p, M, slots, dt, nsteps, cw, cI, cP, m,
-                               n_quad, K, racc, facc);
+                               n_quad, K, grad != nullptr, racc, facc);
   if (rc) return rc;
   // sample sums in sample order
   const int nsl = (int)slots.size();
@@ -539,6 +537,7 @@ int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta
   const double pt_int = contract_op(PT, F.data(), 4).real() * inv_m;
   yields[0] = sys->kS * ps_int;
   yields[1] = sys->kT * pt_int;
+  if (!grad) return SPC_OK;
   for (int c = 0; c < 3; ++c) {
     Mat O(16);
     for (int i = 0; i < 16; ++i) O[i] = -(S1[c][i] + S2[c][i]);

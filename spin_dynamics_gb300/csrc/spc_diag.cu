@@ -10,7 +10,8 @@ namespace spc {
 
 static const char* kKindNames[PROF_KINDS] = {"spmm",   "mgs_dot",    "mgs_axpy_dot", "mgs_axpy_norm",
                                              "scale",  "expm",       "projectors",   "proj_reduce",
-                                             "dtloop", "psi_update", "setup"};
+                                             "dtloop", "psi_update", "setup",        "contract",
+                                             "costate"};
 
 const char* prof_kind_name(int k) { return (k >= 0 && k < PROF_KINDS) ? kKindNames[k] : ""; }
 

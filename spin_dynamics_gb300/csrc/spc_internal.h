@@ -59,6 +59,8 @@ enum ProfKind {
   PK_DTLOOP,
   PK_PSI,
   PK_SETUP,
+  PK_CONTRACT,
+  PK_COSTATE,
   PROF_KINDS
 };
 const char* prof_kind_name(int k);
@@ -169,11 +171,11 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
 // Adjoint sweep of spc_yield_gradient on the batch store's systems 0 (H) and
 // 1 (H^H): per-sample reduced matrices racc (slots x cs.size() x 36 complex)
 // of the gradient integrals and facc (slots x 36) of sum_k cw[k] psi_k psi_k^H
-// on the electron pair.
+// on the electron pair. want_grad = false runs the forward sweep only.
 int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int M,
                        const std::vector<GradSlot>& cs, double dt, int nsteps,
                        const std::vector<double>& cw, double cI, double cP, int m, int nq, int K,
-                       std::vector<double2>& racc_h, std::vector<double2>& facc_h);
+                       bool want_grad, std::vector<double2>& racc_h, std::vector<double2>& facc_h);
 // Nonzero count spc_build_h produces for a system (closed form per mode).
 int64_t predict_nnz(const HostSystem& hs, int mode);
 int num_time_points(double dt, double t_end);

@@ -111,6 +111,20 @@ class YieldGradient:
     A2: list
     raw: np.ndarray
 
+    def symmetric_A(self) -> list:
+        """Derivatives with respect to the 6 independent elements (xx, xy, xz,
+        yy, yz, zz) of each hyperfine tensor taken as symmetric."""
+        out = []
+        for a in self.A1 + self.A2:
+            out.append(np.array([a[0, 0], a[0, 1] + a[1, 0], a[0, 2] + a[2, 0], a[1, 1],
+                                 a[1, 2] + a[2, 1], a[2, 2]]))
+        return out
+
+    def axial_D(self) -> float:
+        """Derivative with respect to the scalar D of the axial tensor
+        2/3 D diag(-1, -1, 2)."""
+        return float(np.sum(self.D * (2.0 / 3.0) * np.diag([-1.0, -1.0, 2.0])))
+
     @staticmethod
     def unpack(y, g, n1: int, n2: int) -> "YieldGradient":
         mat = lambda v: np.asarray(v).reshape(3, 3).T.copy()
@@ -288,6 +302,20 @@ class TraceSampler:
             float(t_end), int(m), int(n_quad), int(checkpoint_every), float(wS), float(wT), _dptr(y),
             _dptr(g)))
         return YieldGradient.unpack(y, g, len(sys.e1.g_I), len(sys.e2.g_I))
+
+    def stepwise_yields(self, sys: SysParam, B, zkets, dt: float, t_end: float, m: int,
+                        init_state: str = "singlet") -> tuple:
+        """(Phi_S, Phi_T) of the stepwise propagation spc_yield_gradient
+        differentiates: its forward sweep alone."""
+        st, keep = make_system(sys, B)
+        zk = np.ascontiguousarray(zkets, np.complex128)
+        th, _ = init_el_state(init_state)
+        th = np.ascontiguousarray(th).view(np.float64)
+        y = np.zeros(2)
+        nat.check(nat.lib().spc_yield_gradient(
+            self._h, C.byref(st), _dptr(th), _dptr(zk.view(np.float64)), zk.shape[0], float(dt),
+            float(t_end), int(m), 1, 0, 1.0, 0.0, _dptr(y), None))
+        return float(y[0]), float(y[1])
 
     def stats(self) -> dict:
         s = nat.spc_stats()

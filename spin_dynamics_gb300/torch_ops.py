@@ -1,0 +1,77 @@
+"""torch.autograd binding of the radical-pair yields.
+
+`yield_objective(params, ...)` returns wS*Phi_S + wT*Phi_T of the stepwise
+trace-sampling propagation as a 0-d float64 tensor whose backward is the
+adjoint gradient of spc_yield_gradient (no finite differences, no tape). The
+parameter vector uses the C layout of spc_yield_gradient:
+
+    [Bx, By, Bz, J, D (9, column-major), kS, kT, A (9 per nucleus, column-major)]
+
+in internal units (mT; kS, kT in 1/us divided by gamma_e). `pack_params` and
+`unpack_params` convert to and from a SysParam and a field vector.
+"""
+from __future__ import annotations
+
+import copy
+
+import numpy as np
+import torch
+
+from .dynamics import TraceSampler
+from .spinsys import SysParam
+
+
+def pack_params(sys: SysParam, B) -> torch.Tensor:
+    Bv = np.array([0.0, 0.0, float(B)]) if np.isscalar(B) else np.asarray(B, np.float64).reshape(3)
+    A = [np.asarray(a, np.float64).reshape(3, 3).T.reshape(9) for a in list(sys.e1.A) + list(sys.e2.A)]
+    v = np.concatenate([Bv, [sys.J], np.asarray(sys.D, np.float64).reshape(3, 3).T.reshape(9),
+                        [sys.kS, sys.kT]] + A)
+    return torch.from_numpy(v)
+
+
+def unpack_params(template: SysParam, v) -> tuple:
+    v = np.asarray(v, np.float64)
+    n1 = len(template.e1.g_I)
+    nn = n1 + len(template.e2.g_I)
+    if v.size != 15 + 9 * nn:
+        raise ValueError(f"parameter vector has {v.size} entries, the system needs {15 + 9 * nn}")
+    s = copy.deepcopy(template)
+    A = [v[15 + 9 * j:24 + 9 * j].reshape(3, 3).T.copy() for j in range(nn)]
+    s.e1.A, s.e2.A = A[:n1], A[n1:]
+    s.J = float(v[3])
+    s.D = v[4:13].reshape(3, 3).T.copy()
+    s.kS, s.kT = float(v[13]), float(v[14])
+    return s, v[0:3].copy()
+
+
+class _Yield(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, params, sampler, template, zkets, dt, t_end, m, n_quad, checkpoint_every, wS, wT):
+        s, B = unpack_params(template, params.detach().cpu().numpy())
+        if ctx.needs_input_grad[0]:
+            g = sampler.yield_gradient(s, B, zkets, dt, t_end, m, n_quad=n_quad,
+                                       checkpoint_every=checkpoint_every, wS=wS, wT=wT)
+            ctx.save_for_backward(torch.from_numpy(g.raw).to(params))
+            val = wS * g.Phi_S + wT * g.Phi_T
+        else:
+            PhiS, PhiT = sampler.stepwise_yields(s, B, zkets, dt, t_end, m)
+            val = wS * PhiS + wT * PhiT
+        return params.new_tensor(val)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (g,) = ctx.saved_tensors
+        return (grad_out * g,) + (None,) * 10
+
+
+def yield_objective(params: torch.Tensor, sampler: TraceSampler, template: SysParam, zkets,
+                    dt: float, t_end: float, m: int, n_quad: int = 6, checkpoint_every: int = 0,
+                    wS: float = 1.0, wT: float = 0.0) -> torch.Tensor:
+    """wS*Phi_S + wT*Phi_T at `params` (float64, C layout); differentiable
+    with respect to params through the adjoint sweep."""
+    if params.dtype != torch.float64:
+        raise TypeError("params must be float64")
+    return _Yield.apply(params, sampler, template, zkets, dt, t_end, m, n_quad, checkpoint_every, wS, wT)
+
+
+__all__ = ["pack_params", "unpack_params", "yield_objective"]

@@ -128,3 +128,53 @@ def test_short_window_has_zero_yield(sampler):
     zk = W.random_phase_samples(s.Z, 2, seed=1)
     got = sampler.yield_gradient(s, 0.05, zk, DT, 0.5 * DT, m=8)  # T = 3: no Simpson panel
     assert got.Phi_S == 0.0 and not np.any(got.raw)
+
+
+def test_full_size_directional_derivatives(sampler):
+    """dim 55296 (the large anisotropic pair): the adjoint gradient against
+    central differences (h = 1e-6 relative) of the GPU's own stepwise yields
+    along single parameters and a random direction."""
+    from spin_dynamics_gb300.torch_ops import pack_params, unpack_params
+    s, B = W.large_pair()
+    s.kS, s.kT = 20.0 / GAMMA_E, 20.0 / GAMMA_E
+    zk = W.random_phase_samples(s.Z, 2, seed=3)
+    t_end = 6 * DT
+    g = sampler.yield_gradient(s, B, zk, DT, t_end, m=30, n_quad=6, checkpoint_every=2)
+    v0 = pack_params(s, B).numpy()
+    rng = np.random.default_rng(1)
+    dirs = {"Bx": 0, "J": 3, "kS": 13, "A0_xy": 15 + 3}
+    cases = [(k, np.eye(v0.size)[i]) for k, i in dirs.items()]
+    cases.append(("random", rng.normal(size=v0.size) * np.abs(v0).clip(1e-3)))
+    for name, d in cases:
+        h = 1e-6 * max(np.abs(v0 @ d) / np.linalg.norm(d), 1.0) / np.linalg.norm(d)
+        sp, Bp = unpack_params(s, v0 + h * d)
+        sm, Bm = unpack_params(s, v0 - h * d)
+        fd = (sampler.stepwise_yields(sp, Bp, zk, DT, t_end, 30)[0] -
+              sampler.stepwise_yields(sm, Bm, zk, DT, t_end, 30)[0]) / (2 * h)
+        ad = g.raw @ d
+        # 1e-6 of the gradient scale |g| |d|: a central difference of yields
+        # evaluated to ~1e-15 carries ~1e-10 of rounding noise at h = 1e-6,
+        # which is 1e-5 relative for the smallest entries (dPhi/dBx ~ 8e-6)
+        assert abs(ad - fd) <= 1e-6 * np.linalg.norm(g.raw) * np.linalg.norm(d), (name, ad, fd)
+
+
+def test_torch_autograd_matches_adjoint(sampler):
+    import torch
+    from spin_dynamics_gb300.torch_ops import pack_params, yield_objective
+    s = aniso_pair([2], [2, 2], seed=8, kS=0.02, kT=0.005)
+    B = np.array([0.0, 0.04, 0.03])
+    zk = W.random_phase_samples(s.Z, 6, seed=2)
+    t_end = 10 * DT
+    p = pack_params(s, B).clone().requires_grad_(True)
+    val = yield_objective(p, sampler, s, zk, DT, t_end, 32, n_quad=8)
+    val.backward()
+    g = sampler.yield_gradient(s, B, zk, DT, t_end, 32, n_quad=8)
+    assert val.item() == g.Phi_S
+    assert torch.equal(p.grad, torch.from_numpy(g.raw))
+    with torch.no_grad():
+        v2 = yield_objective(p.detach(), sampler, s, zk, DT, t_end, 32)
+    assert abs(v2.item() - g.Phi_S) <= 1e-14 * abs(g.Phi_S)
+    ok = torch.autograd.gradcheck(
+        lambda q: yield_objective(q, sampler, s, zk, DT, t_end, 32, n_quad=8),
+        (p.detach().clone().requires_grad_(True),), eps=1e-6, atol=1e-8, rtol=1e-5)
+    assert ok
