@@ -251,6 +251,23 @@ int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta
                        const double* zkets, int M, double dt, double t_end, int m, int n_quad,
                        int checkpoint_every, double wS, double wT, double* yields, double* grad);
 
+/* Gradient sets for spc_yield_gradient_batch. */
+#define SPC_GRAD_ALL 0    /* every parameter (nuclei of multiplicity <= 3) */
+#define SPC_GRAD_FIELD 1  /* B, J, D, kS, kT; hyperfine entries left 0 (nuclei of
+                             multiplicity <= 6, e.g. symmetry blocks) */
+
+/* spc_yield_gradient for n_jobs systems of any dimensions in one sweep
+ * (field orientations, radical pairs, symmetry blocks): job k propagates
+ * M[k] vectors under systems[k]; zkets holds the jobs' M[k] x Z_k blocks back
+ * to back. yields: n_jobs x (Phi_S, Phi_T); grad (NULL: yields only): the
+ * jobs' spc_yield_gradient_size(systems[k]) blocks back to back. Every build,
+ * contraction and costate step of all jobs shares one set of launches. The
+ * handle's Hamiltonian and batch are replaced by H_k and H_k^H. */
+int spc_yield_gradient_batch(spc_handle* h, int n_jobs, const spc_system* systems, const int* M,
+                             const double* theta, const double* zkets, double dt, double t_end, int m,
+                             int n_quad, int checkpoint_every, double wS, double wT, int which,
+                             double* yields, double* grad);
+
 /* Select the Krylov orthogonalisation (SPC_KRYLOV_*). In exact arithmetic
  * Lanczos and MGS give the same basis when H_eff = Hermitian - i*kappa; the
  * Lanczos path skips the O(m^2 n) re-orthogonalisation and verifies the

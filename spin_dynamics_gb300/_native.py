@@ -19,6 +19,8 @@ SPC_ERR_NUMERIC = 5
 SPC_ERR_STATE = 6
 SPC_H_REFERENCE = 0
 SPC_H_GENERAL = 1
+SPC_GRAD_ALL = 0
+SPC_GRAD_FIELD = 1
 SPC_KRYLOV_MGS = 0
 SPC_KRYLOV_LANCZOS = 1
 SPC_KRYLOV_AUTO = 2
@@ -83,6 +85,7 @@ SIGNATURES = {
     "spc_yield_gradient_size": (_I, [C.POINTER(spc_system)]),
     "spc_yield_gradient": (_I, [_P, C.POINTER(spc_system), _P, _P, _I, _D, _D, _I, _I, _I, _D, _D, _P,
                                 _P]),
+    "spc_yield_gradient_batch": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _I, _I, _I, _D, _D, _I, _P, _P]),
     "spc_set_profiling": (_I, [_P, _I]),
     "spc_get_profile": (_I, [_P, _I, C.POINTER(_D), C.POINTER(C.c_int64), C.POINTER(_D),
                              C.POINTER(_D)]),

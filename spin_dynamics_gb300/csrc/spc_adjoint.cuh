@@ -1,4 +1,5 @@
-// Adjoint gradient of the radical-pair yields (spc_yield_gradient). Included
+// Adjoint gradient of the radical-pair yields (spc_yield_gradient and
+// spc_yield_gradient_batch: many systems of uneven dimension in one sweep). Included
 // at the end of spc_propagate.cu, inside namespace spc, so that it reuses the
 // Krylov kernels defined there.
 //
@@ -32,27 +33,34 @@
 
 #define CON_MAXG 6
 
-// R[a][b] += w * sum_o conj(mu_row(a,o)) nu_row(b,o) for one (tile, slot);
-// one warp per CTA, lanes = samples, the `o` range split into nch chunks;
-// the last CTA of each (tile, slot) adds the chunk partials in chunk order.
+// One (tile, slot) of a contraction launch; roff is the accumulator offset
+// (in 36-entry blocks) of the tile's lane 0, nsl its job's slot count.
+struct ConPair {
+  int t, js, jl, nsl;
+  int64_t roff;
+};
+
+// R[a][b] += w * sum_o conj(mu_row(a,o)) nu_row(b,o) for the (tile, slot)
+// pairs [p0, p0 + gridDim.x / nch), all of slot size G; one warp per CTA,
+// lanes = samples, the `o` range split into nch chunks; the last CTA of each
+// pair adds the chunk partials in chunk order.
 template <int G>
 __global__ void __launch_bounds__(32)
     k_contract(const TileInfo* __restrict__ tiles, const int* __restrict__ map,
-               const int* __restrict__ scol, const GradSlot* __restrict__ slots, int nsl, int nch,
-               const double2* __restrict__ mu, const double2* __restrict__ nu, double w,
-               double2* __restrict__ partial, unsigned* __restrict__ counters,
-               double2* __restrict__ racc) {
+               const int* __restrict__ scol, const GradSlot* __restrict__ slots,
+               const ConPair* __restrict__ pairs, int p0, int nch, const double2* __restrict__ mu,
+               const double2* __restrict__ nu, double w, double2* __restrict__ partial,
+               unsigned* __restrict__ counters, double2* __restrict__ racc) {
   const int b = blockIdx.x;
-  const int pair = b / nch, ch = b % nch;
-  const int t = pair / nsl, js = pair % nsl;
-  const GradSlot S = slots[js];
-  if (S.G != G) return;  // launched once per G; slots of the other size leave at once
-  const TileInfo& T = tiles[t];
+  const int pl = b / nch, ch = b % nch;
+  const ConPair PR = pairs[p0 + pl];
+  const GradSlot S = slots[PR.js];
+  const TileInfo& T = tiles[PR.t];
   const int lane = threadIdx.x;
-  const int wslot = t * SPC_LANES + lane;
+  const int wslot = PR.t * SPC_LANES + lane;
   const bool act = map[wslot] >= 0;
   const int64_t Z = T.n / 4;
-  const int64_t L = S.owner < 0 ? Z : 2 * Z / S.g;
+  const int64_t L = S.owner == -1 ? Z : (S.owner == -2 ? 4 * Z / S.g : 2 * Z / S.g);
   const int64_t per = (L + nch - 1) / nch;
   const int64_t o0 = (int64_t)ch * per, o1 = min(L, o0 + per);
   double2 acc[G * G];
@@ -62,10 +70,11 @@ __global__ void __launch_bounds__(32)
     const int64_t ld = T.ldp;
     const double2* Mu = mu + T.psi_off + scol[wslot];
     const double2* Nu = nu + T.psi_off + scol[wslot];
-    const int64_t zg = S.owner < 0 ? Z : Z / S.g;
+    const int64_t zg = S.owner == -1 ? Z : Z / S.g;
     for (int64_t o = o0; o < o1; ++o) {
       double2 a[G], v[G];
-      if (S.owner < 0) {
+      if (S.owner == -1) {
+        // electron pair: o = nuclear index
 #pragma unroll
         for (int c = 0; c < G; ++c) {
           const int64_t row = (int64_t)c * Z + o;
@@ -73,15 +82,23 @@ __global__ void __launch_bounds__(32)
           v[c] = Nu[row * ld];
         }
       } else {
-        // o = (spin of the other electron, nuclear index without nucleus j)
+        // o = (electron state or spin of the other electron, nuclear index
+        // without nucleus j)
         const int so = (int)(o / zg);
         const int64_t rem = o - (int64_t)so * zg;
         const int64_t hi = rem / S.stride, lo = rem - hi * S.stride;
         const int64_t nbase = hi * S.g * S.stride + lo;
 #pragma unroll
         for (int c = 0; c < G; ++c) {
-          const int sk = c / (G / 2), mm = c % (G / 2);
-          const int e = S.owner == 0 ? (sk * 2 + so) : (so * 2 + sk);
+          int e, mm;
+          if (S.owner == -2) {
+            e = so;
+            mm = c;
+          } else {
+            const int sk = c / (G / 2);
+            mm = c % (G / 2);
+            e = S.owner == 0 ? (sk * 2 + so) : (so * 2 + sk);
+          }
           const int64_t row = (int64_t)e * Z + nbase + (int64_t)mm * S.stride;
           a[c] = Mu[row * ld];
           v[c] = Nu[row * ld];
@@ -93,26 +110,25 @@ __global__ void __launch_bounds__(32)
         for (int j = 0; j < G; ++j) acc[i * G + j] = cjfma(a[i], v[j], acc[i * G + j]);
     }
   }
-  double2* P = partial + (size_t)b * CON_MAXG * CON_MAXG * SPC_LANES + lane;
+  double2* P = partial + (size_t)b * G * G * SPC_LANES + lane;
 #pragma unroll
   for (int i = 0; i < G * G; ++i) P[(size_t)i * SPC_LANES] = acc[i];
   __threadfence();
   __shared__ bool am_last;
-  if (lane == 0) am_last = atomicAdd(&counters[pair], 1u) == (unsigned)nch - 1;
+  if (lane == 0) am_last = atomicAdd(&counters[p0 + pl], 1u) == (unsigned)nch - 1;
   __syncwarp();
   if (!am_last) return;
   __threadfence();
   if (act) {
-    double2* R = racc + ((size_t)wslot * nsl + js) * CON_MAXG * CON_MAXG;
-    const double2* base = partial + (size_t)pair * nch * CON_MAXG * CON_MAXG * SPC_LANES + lane;
+    double2* R = racc + ((size_t)PR.roff + (size_t)lane * PR.nsl + PR.jl) * CON_MAXG * CON_MAXG;
+    const double2* base = partial + (size_t)pl * nch * G * G * SPC_LANES + lane;
     for (int i = 0; i < G * G; ++i) {
       double2 s = cz();
-      for (int c = 0; c < nch; ++c)
-        s = cadd(s, __ldcg(base + ((size_t)c * CON_MAXG * CON_MAXG + i) * SPC_LANES));
+      for (int c = 0; c < nch; ++c) s = cadd(s, __ldcg(base + ((size_t)c * G * G + i) * SPC_LANES));
       R[i] = make_double2(fma(w, s.x, R[i].x), fma(w, s.y, R[i].y));
     }
   }
-  if (lane == 0) counters[pair] = 0u;
+  if (lane == 0) counters[p0 + pl] = 0u;
 }
 
 // Krylov coordinates of y = exp(-i tau A) (beta e1): beta * E[:, 0] per slot,
@@ -128,15 +144,18 @@ __global__ void k_first_col(int nslots, const TileInfo* __restrict__ tiles, cons
   for (int j = 0; j < m; ++j) cout[(size_t)w * m + j] = j < me ? cscale(beta, E[j]) : cz();
 }
 
-// lam = ulam + cI psi + cP Pi_S psi, Pi_S = |S><S| on the electron pair,
-// |S> = (|ab> - |ba>)/sqrt(2); grid (tiles, row blocks), block (32, SPC_WARPS).
+// lam = ulam + c (cI psi + cP Pi_S psi) with (cI, cP) per tile, Pi_S = |S><S|
+// on the electron pair, |S> = (|ab> - |ba>)/sqrt(2); grid (tiles, row
+// blocks), block (32, SPC_WARPS).
 __global__ void __launch_bounds__(256)
     k_costate(const TileInfo* __restrict__ tiles, const int* __restrict__ map,
-              const int* __restrict__ scol, const double2* __restrict__ psi,
-              const double2* __restrict__ ulam, double cI, double cP, double2* __restrict__ lam) {
+              const int* __restrict__ scol, const double2* __restrict__ coefs, double c,
+              const double2* __restrict__ psi, const double2* __restrict__ ulam,
+              double2* __restrict__ lam) {
   const TileInfo& T = tiles[blockIdx.x];
   const int w = blockIdx.x * SPC_LANES + threadIdx.x;
   if (map[w] < 0) return;
+  const double cI = c * coefs[blockIdx.x].x, cP = c * coefs[blockIdx.x].y;
   const int64_t Z = T.n / 4;
   const int64_t ld = T.ldp;
   const size_t base = T.psi_off + scol[w];
@@ -181,30 +200,108 @@ static void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>&
   }
 }
 
-int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int M,
+int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob>& jobs,
                        const std::vector<GradSlot>& cs, double dt, int nsteps,
-                       const std::vector<double>& cw, double cI, double cP, int m, int nq, int K,
-                       bool want_grad, std::vector<double2>& racc_h, std::vector<double2>& facc_h) {
+                       const std::vector<double>& cw, int m, int nq, int K, bool want_grad,
+                       std::vector<std::vector<double2>>& rsum, std::vector<std::vector<double2>>& fsum) {
   auto t_start = std::chrono::steady_clock::now();
   cudaStream_t st = h->stream;
   const auto& HB = h->hb;
-  const int n = HB.n[0];
-  const int64_t Z = n / 4;
-  const int ldp = (M + SPC_LANES - 1) / SPC_LANES * SPC_LANES;
-  const int ntiles = ldp / SPC_LANES, nslots = ldp;
-  const int nsl = (int)cs.size();
-  const size_t S = (size_t)n * ldp;  // one state of all samples (psi layout)
+  const int nj = (int)jobs.size();
+  // job layout: state blocks [rows][ldp] back to back, 32-sample tiles
+  std::vector<int> ldp(nj), nrow(nj), tile0(nj);
+  std::vector<int64_t> psi_off(nj);
+  size_t S = 0;  // entries of one state of all samples of all jobs
+  int ntiles = 0, Mtot = 0;
+  for (int k = 0; k < nj; ++k) {
+    nrow[k] = HB.n[jobs[k].sys];
+    ldp[k] = (jobs[k].M + SPC_LANES - 1) / SPC_LANES * SPC_LANES;
+    psi_off[k] = (int64_t)S;
+    S += (size_t)nrow[k] * ldp[k];
+    tile0[k] = ntiles;
+    ntiles += ldp[k] / SPC_LANES;
+    Mtot += jobs[k].M;
+  }
+  const int nslots = ntiles * SPC_LANES;
   const size_t mm = (size_t)m * m;
-  // chunks per (tile, slot): about two waves of one-warp CTAs
-  const int nch = (int)std::max<int64_t>(
-      1, std::min<int64_t>(Z, (int64_t)h->sm_count * 32 / std::max(1, ntiles * nsl)));
-  const size_t npairs = (size_t)ntiles * nsl;
-  const int items_cap = h->sm_count * 32 + ntiles;
   const size_t con = (size_t)CON_MAXG * CON_MAXG;
-  const double elems = (double)n * M;  // vector entries of one state over the samples
-  // Node states of a whole segment are kept (one Krylov build per step saved)
-  // when they fit in device memory; otherwise they are rebuilt per step.
-  // Checkpoint spacing K and whether a segment's node states are kept (one
+  const double elems = [&] {
+    double e = 0.0;
+    for (int k = 0; k < nj; ++k) e += (double)nrow[k] * jobs[k].M;
+    return e;
+  }();
+  const int items_cap = h->sm_count * 32 + ntiles;
+
+  // tiles, slot maps, costate coefficients
+  std::vector<TileInfo> tf(ntiles), tb(ntiles);
+  std::vector<int> map(nslots), scol(nslots), tile_n(ntiles), tile_job(ntiles);
+  std::vector<double2> coefs(ntiles);
+  {
+    int t = 0;
+    int64_t qo = 0, po = 0;
+    for (int k = 0; k < nj; ++k) {
+      for (int c = 0; c < ldp[k] / SPC_LANES; ++c, ++t) {
+        TileInfo ti{};
+        ti.job = k;
+        ti.n = nrow[k];
+        ti.ldp = ldp[k];
+        ti.m = std::min(m, nrow[k]);
+        ti.q_off = qo;
+        ti.p_off = po;
+        ti.psi_off = psi_off[k];
+        qo += (int64_t)m * nrow[k] * SPC_LANES;
+        po += (int64_t)nrow[k] * SPC_LANES;
+        tf[t] = tb[t] = ti;
+        for (int e = 0; e < 2; ++e) {
+          TileInfo& x = e == 0 ? tf[t] : tb[t];
+          const int sy = jobs[k].sys + e;
+          x.rowptr = (const int*)HB.rowptr.p + HB.rp_off[sy];
+          x.split = (const int*)HB.split.p + HB.rp_off[sy];
+          x.col = (const int*)HB.col.p + HB.nz_off[sy];
+          x.val = (const double2*)HB.val.p + HB.nz_off[sy];
+        }
+        for (int l = 0; l < SPC_LANES; ++l) {
+          const int s = c * SPC_LANES + l;
+          map[t * SPC_LANES + l] = s < jobs[k].M ? tile0[k] * SPC_LANES + s : -1;
+          scol[t * SPC_LANES + l] = s < jobs[k].M ? s : -1;
+        }
+        tile_n[t] = nrow[k];
+        tile_job[t] = k;
+        coefs[t] = make_double2(jobs[k].cI, jobs[k].cP);
+      }
+    }
+  }
+  // contraction pair tables: gradient pairs grouped by slot size, and the
+  // electron-pair slot of every tile for the forward sum F
+  std::vector<int64_t> roff(ntiles);
+  int64_t rtot = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    roff[t] = rtot;
+    rtot += (int64_t)SPC_LANES * jobs[tile_job[t]].nslot;
+  }
+  std::vector<ConPair> pairs;
+  std::vector<int> grp_G, grp_p0, grp_cnt;
+  for (int Gv = 2; Gv <= CON_MAXG; ++Gv) {
+    const int p0 = (int)pairs.size();
+    for (int t = 0; t < ntiles; ++t) {
+      const GradJob& J = jobs[tile_job[t]];
+      for (int jl = 0; jl < J.nslot; ++jl)
+        if (cs[J.slot0 + jl].G == Gv) pairs.push_back(ConPair{t, J.slot0 + jl, jl, J.nslot, roff[t]});
+    }
+    if ((int)pairs.size() > p0) {
+      grp_G.push_back(Gv);
+      grp_p0.push_back(p0);
+      grp_cnt.push_back((int)pairs.size() - p0);
+    }
+  }
+  const int pf0 = (int)pairs.size();
+  for (int t = 0; t < ntiles; ++t)
+    pairs.push_back(ConPair{t, jobs[tile_job[t]].slot0, 0, 1, (int64_t)t * SPC_LANES});
+  const int npairs = (int)pairs.size();
+  auto chunks = [&](int cnt) { return std::max(1, h->sm_count * 32 / std::max(1, cnt)); };
+  const size_t part_cap = (size_t)std::max(npairs, h->sm_count * 64) * con * SPC_LANES;
+
+  // checkpoint spacing K and whether a segment's node states are kept (one
   // Krylov build per step saved). K = 0 picks the largest spacing whose
   // states fit in device memory (fewest recomputed segments), else the
   // spacing of least memory with node states rebuilt per step.
@@ -215,18 +312,17 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
     const double held = (double)h->gck.bytes + h->gseg.bytes + h->gnu.bytes + h->Q.bytes + h->gmu.bytes +
                         h->glam.bytes + h->P.bytes;
     const double avail = 0.85 * ((double)free_b + held) - (double)(1 << 28);
-    const double st = sizeof(double2) * (double)S;
+    const double sb = sizeof(double2) * (double)S;
     auto need = [&](int k, bool keep) {
-      return st * ((double)m + 4.0 + (nsteps / k + 1) + k + 1.0 + (keep ? (double)k * nq : (double)nq));
+      return sb * ((double)m + 4.0 + (nsteps / k + 1) + k + 1.0 + (keep ? (double)k * nq : (double)nq));
     };
     if (K == 0) {
       for (int k = nsteps; k >= 1 && K == 0; --k)
         if (need(k, true) <= avail) K = k;
-      if (K) {
+      if (K)
         cache = true;
-      } else {
+      else
         K = std::max(1, (int)std::lround(std::sqrt((double)nsteps)));
-      }
     } else {
       cache = need(K, true) <= avail;
     }
@@ -240,21 +336,22 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   const int a_last = ((nsteps - 1) / K) * K;  // first step of the last segment
   const size_t n_ck = want_grad ? nck : 0, n_seg = want_grad ? K + 1 : 0;
   const size_t n_nu = want_grad ? (cache ? (size_t)K * nq : (size_t)nq) : 0;
+  const size_t plan_bytes = 2 * sizeof(TileInfo) * ntiles + sizeof(int2) * 2 * items_cap +
+                            sizeof(int) * 2 * nslots + sizeof(double2) * ntiles + 64;
   if (h->ensure(h->gck, sizeof(double2) * S * n_ck) || h->ensure(h->gseg, sizeof(double2) * S * n_seg) ||
       h->ensure(h->gnu, sizeof(double2) * S * n_nu) || h->ensure(h->gmu, sizeof(double2) * S) ||
       h->ensure(h->glam, sizeof(double2) * S * 2) || h->ensure(h->Q, sizeof(double2) * m * S) ||
       h->ensure(h->P, sizeof(double2) * S) ||
-      h->ensure(h->partial, sizeof(double2) * std::max<size_t>((size_t)items_cap * SPC_LANES,
-                                                               npairs * nch * con * SPC_LANES)) ||
+      h->ensure(h->partial, sizeof(double2) * std::max<size_t>((size_t)items_cap * SPC_LANES, part_cap)) ||
       h->ensure(h->counters, sizeof(unsigned) * std::max<size_t>(ntiles, npairs)) ||
       h->ensure(h->coef, sizeof(double2) * nslots) || h->ensure(h->rbeta, sizeof(double) * nslots) ||
       h->ensure(h->Ahess, sizeof(double2) * mm * nslots) || h->ensure(h->Aexp, sizeof(double2) * mm * nslots) ||
       h->ensure(h->cvec, sizeof(double2) * m * nslots) || h->ensure(h->cvec2, sizeof(double2) * m * nslots) ||
       h->ensure(h->flag, sizeof(int) * nslots) || h->ensure(h->err, 16) ||
-      h->ensure(h->gslots, sizeof(GradSlot) * nsl) || h->ensure(h->gracc, sizeof(double2) * nslots * nsl * con) ||
-      h->ensure(h->gfacc, sizeof(double2) * nslots * con) ||
-      h->ensure(h->plan, 2 * sizeof(TileInfo) * ntiles + sizeof(int2) * 2 * items_cap + sizeof(int) * 2 * nslots) ||
-      h->ensure(h->jobtab, sizeof(JobInit)))
+      h->ensure(h->gslots, sizeof(GradSlot) * cs.size() + sizeof(ConPair) * npairs) ||
+      h->ensure(h->gracc, sizeof(double2) * std::max<int64_t>(rtot, 1) * con) ||
+      h->ensure(h->gfacc, sizeof(double2) * nslots * con) || h->ensure(h->plan, plan_bytes) ||
+      h->ensure(h->jobtab, sizeof(JobInit) * nj))
     return SPC_ERR_ALLOC;
   double2 *ck = (double2*)h->gck.p, *seg = (double2*)h->gseg.p, *gnu = (double2*)h->gnu.p;
   double2 *gmu = (double2*)h->gmu.p, *lam = (double2*)h->glam.p, *ulam = lam + S;
@@ -265,6 +362,7 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   int* d_flag = (int*)h->flag.p;
   int* d_err = (int*)h->err.p;
   GradSlot* d_slots = (GradSlot*)h->gslots.p;
+  ConPair* d_pairs = (ConPair*)((char*)h->gslots.p + sizeof(GradSlot) * cs.size());
   double2 *d_racc = (double2*)h->gracc.p, *d_facc = (double2*)h->gfacc.p;
   char* plan = (char*)h->plan.p;
   TileInfo* d_tf = (TileInfo*)plan;
@@ -273,48 +371,28 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   int2* d_items_s = d_items + items_cap;
   int* d_map = (int*)(d_items_s + items_cap);
   int* d_scol = d_map + nslots;
+  double2* d_coefs = (double2*)(((uintptr_t)(d_scol + nslots) + 15) & ~(uintptr_t)15);
   int64_t launches0 = h->launches;
 
-  // static tiles (every sample takes every step) for H (tf) and H^H (tb)
   auto resident = [&](const void* fn) {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 256, 0) != cudaSuccess) b = 1;
     return std::max(1, b) * h->sm_count;
   };
-  std::vector<int> tile_n(ntiles, n), fp, cp, fs, csn;
+  std::vector<int> fp, cp, fs, csn;
   std::vector<int2> items_p, items_s;
   plan_items(tile_n, std::min(resident((const void*)k_rowpass<PASS_AXPY_DOT>),
                               resident((const void*)k_rowpass<PASS_AXPY_NORM>)), fp, cp, items_p);
   plan_items(tile_n, resident((const void*)k_spmm), fs, csn, items_s);
   const int nip = (int)items_p.size(), nis = (int)items_s.size();
   if (nip > items_cap || nis > items_cap) return set_error(SPC_ERR_ARG, "internal: work plan exceeds its buffer");
-  std::vector<TileInfo> tf(ntiles), tb(ntiles);
-  std::vector<int> map(nslots), scol(nslots);
+  int64_t nnz_tiles = 0;
   for (int t = 0; t < ntiles; ++t) {
-    TileInfo ti{};
-    ti.job = 0;
-    ti.n = n;
-    ti.ldp = ldp;
-    ti.m = std::min(m, n);
-    ti.q_off = (int64_t)t * m * n * SPC_LANES;
-    ti.p_off = (int64_t)t * n * SPC_LANES;
-    ti.psi_off = 0;
-    ti.ip0 = fp[t];
-    ti.nip = cp[t];
-    ti.is0 = fs[t];
-    ti.nis = csn[t];
-    tf[t] = tb[t] = ti;
-    for (int e = 0; e < 2; ++e) {
-      TileInfo& x = e == 0 ? tf[t] : tb[t];
-      x.rowptr = (const int*)HB.rowptr.p + HB.rp_off[e];
-      x.split = (const int*)HB.split.p + HB.rp_off[e];
-      x.col = (const int*)HB.col.p + HB.nz_off[e];
-      x.val = (const double2*)HB.val.p + HB.nz_off[e];
-    }
-    for (int l = 0; l < SPC_LANES; ++l) {
-      const int s = t * SPC_LANES + l;
-      map[s] = scol[s] = s < M ? s : -1;
-    }
+    tf[t].ip0 = tb[t].ip0 = fp[t];
+    tf[t].nip = tb[t].nip = cp[t];
+    tf[t].is0 = tb[t].is0 = fs[t];
+    tf[t].nis = tb[t].nis = csn[t];
+    nnz_tiles += HB.nnz[jobs[tile_job[t]].sys];
   }
   CK(cudaMemcpyAsync(d_tf, tf.data(), sizeof(TileInfo) * ntiles, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d_tb, tb.data(), sizeof(TileInfo) * ntiles, cudaMemcpyHostToDevice, st));
@@ -322,9 +400,11 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   CK(cudaMemcpyAsync(d_items_s, items_s.data(), sizeof(int2) * nis, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d_map, map.data(), sizeof(int) * nslots, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d_scol, scol.data(), sizeof(int) * nslots, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d_slots, cs.data(), sizeof(GradSlot) * nsl, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_coefs, coefs.data(), sizeof(double2) * ntiles, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_slots, cs.data(), sizeof(GradSlot) * cs.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_pairs, pairs.data(), sizeof(ConPair) * npairs, cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * std::max<size_t>(ntiles, npairs), st));
-  CK(cudaMemsetAsync(d_racc, 0, sizeof(double2) * nslots * nsl * con, st));
+  CK(cudaMemsetAsync(d_racc, 0, sizeof(double2) * std::max<int64_t>(rtot, 1) * con, st));
   CK(cudaMemsetAsync(d_facc, 0, sizeof(double2) * nslots * con, st));
   CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * nslots, st));
   CK(cudaMemsetAsync(h->err.p, 0, 16, st));
@@ -332,24 +412,30 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
   double2* psi0 = !want_grad ? lam : a_last == 0 ? seg : ck;
   CK(cudaMemsetAsync(psi0, 0, sizeof(double2) * S, st));
   {
-    JobInit ji{Z, 0, M, ldp, (const double2*)zk_dev};
-    CK(cudaMemcpyAsync(h->jobtab.p, &ji, sizeof(JobInit), cudaMemcpyHostToDevice, st));
+    std::vector<JobInit> ji(nj);
+    for (int k = 0; k < nj; ++k) ji[k] = JobInit{nrow[k] / 4, psi_off[k], jobs[k].M, ldp[k], jobs[k].zk};
+    CK(cudaMemcpyAsync(h->jobtab.p, ji.data(), sizeof(JobInit) * nj, cudaMemcpyHostToDevice, st));
     Theta th;
     for (int e = 0; e < 4; ++e) th.v[e] = make_double2(theta[2 * e], theta[2 * e + 1]);
-    k_kron_init<<<dim3(h->sm_count * 8, 1), 256, 0, st>>>((const JobInit*)h->jobtab.p, 0, th, psi0);
-    h->count_launch();
+    for (int j0 = 0; j0 < nj; j0 += 65535) {
+      const int cnt = std::min(65535, nj - j0);
+      k_kron_init<<<dim3(std::max(1, h->sm_count * 8 / cnt), cnt), 256, 0, st>>>((const JobInit*)h->jobtab.p,
+                                                                                 j0, th, psi0);
+      h->count_launch();
+    }
   }
   const size_t expm_smem = sizeof(double2) * 5 * mm;
   CK(cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expm_smem));
   const dim3 blk(SPC_LANES, SPC_WARPS);
   // the three-term recurrence only on explicit request: no projector Gram
   // verifies these bases (the trace-sampling path checks its own)
-  const bool lanczos = h->krylov_method == 1 && HB.herm[0] && HB.herm[1];
+  bool lanczos = h->krylov_method == 1;
+  for (const GradJob& J : jobs) lanczos = lanczos && HB.herm[J.sys] && HB.herm[J.sys + 1];
   std::vector<double> xq, wq;
   gauss_legendre01(nq, xq, wq);
   int64_t builds = 0;
 
-  // Krylov basis of the states `x` (psi layout) under the tiles' Hamiltonian
+  // Krylov basis of the states `x` (psi layout) under the tiles' Hamiltonians
   auto build = [&](const double2* x, const TileInfo* tiles) {
     CK(cudaMemsetAsync(d_A, 0, sizeof(double2) * mm * nslots, st));
     PassArgs pa{};
@@ -378,7 +464,7 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
     for (int i = 0; i < m; ++i) {
       pe = h->prof.begin(st);
       k_spmm<<<nis, blk, 0, st>>>(tiles, d_items_s, d_map, i, d_Q, d_P);
-      h->prof.end(st, pe, PK_SPMM, 8.0 * (double)HB.nnz[0] * nslots, 20.0 * (double)HB.nnz[0] * ntiles + 32.0 * elems);
+      h->prof.end(st, pe, PK_SPMM, 8.0 * (double)nnz_tiles * SPC_LANES, 20.0 * (double)nnz_tiles + 32.0 * elems);
       h->count_launch();
       pa.col_i = i;
       int j0 = 0;
@@ -413,43 +499,65 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
         h->count_launch(2);
       }
     }
-    builds += M;
+    builds += Mtot;
     return SPC_OK;
   };
-  // y = exp(-i tau H) x from the current basis (tau < 0 runs backwards)
+  // y = exp(-i tau H) x from the current bases (tau < 0 runs backwards)
   auto apply = [&](double tau, const TileInfo* tiles, double2* y) {
     int pe = h->prof.begin(st);
     k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, tiles, d_map, d_A, d_E, tau, d_err);
-    h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * M, 32.0 * (double)mm * M);
+    h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * Mtot, 32.0 * (double)mm * Mtot);
     pe = h->prof.begin(st);
     k_first_col<<<(nslots + 127) / 128, 128, 0, st>>>(nslots, tiles, d_map, m, d_E, d_c, d_c2);
-    h->prof.end(st, pe, PK_SETUP, 2.0 * m * M, 32.0 * m * M);
+    h->prof.end(st, pe, PK_SETUP, 2.0 * m * Mtot, 32.0 * m * Mtot);
     pe = h->prof.begin(st);
     k_psi_update<<<nip, blk, 0, st>>>(tiles, d_items, m, d_map, d_scol, d_flag, d_Q, d_c2, y);
     h->prof.end(st, pe, PK_PSI, 8.0 * m * elems, 16.0 * (m + 1) * elems);
     h->count_launch(3);
   };
-  // acc += w * reduced matrices of (mu, nu); nsl_ = 1 takes the electron pair only
-  // algorithmic FLOPs and bytes of one contraction over the first nsl_ slots
-  auto con_cost = [&](int nsl_, double& f, double& by) {
-    f = by = 0.0;
-    for (int j = 0; j < nsl_; ++j) {
-      const double L = cs[j].owner < 0 ? (double)Z : 2.0 * Z / cs[j].g;
-      f += 8.0 * cs[j].G * cs[j].G * L * M;
-    }
-    by = 32.0 * elems;
-  };
-  double con_f1, con_b1, con_fn, con_bn;
-  con_cost(1, con_f1, con_b1);
-  con_cost(nsl, con_fn, con_bn);
-  auto contract = [&](const double2* mu, const double2* nu, double w, int nsl_, double2* acc) {
-    const int nb = ntiles * nsl_ * nch;
+  // algorithmic FLOPs of a contraction over the gradient slots / the pair slot
+  double con_fg = 0.0, con_ff = 0.0;
+  for (const ConPair& P : pairs) {
+    const GradSlot& Sl = cs[P.js];
+    const double Z = tile_n[P.t] / 4;
+    const double L = Sl.owner == -1 ? Z : (Sl.owner == -2 ? 4.0 * Z / Sl.g : 2.0 * Z / Sl.g);
+    const double f = 8.0 * Sl.G * Sl.G * L * SPC_LANES;
+    if (&P - pairs.data() < pf0)
+      con_fg += f;
+    else
+      con_ff += f;
+  }
+  // acc += w * reduced matrices of (mu, nu): forward = the electron pair only
+  auto contract = [&](const double2* mu, const double2* nu, double w, bool forward, double2* acc) {
     int pe = h->prof.begin(st);
-    k_contract<4><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, nsl_, nch, mu, nu, w, d_part, d_cnt, acc);
-    if (nsl_ > 1)
-      k_contract<6><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, nsl_, nch, mu, nu, w, d_part, d_cnt, acc);
-    h->prof.end(st, pe, PK_CONTRACT, nsl_ > 1 ? con_fn : con_f1, nsl_ > 1 ? con_bn : con_b1);
-    h->count_launch(nsl_ > 1 ? 2 : 1);
+    if (forward) {
+      k_contract<4><<<ntiles * chunks(ntiles), 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, pf0,
+                                                            chunks(ntiles), mu, nu, w, d_part, d_cnt, acc);
+      h->count_launch();
+    } else {
+      for (size_t gi = 0; gi < grp_G.size(); ++gi) {
+        const int nc = chunks(grp_cnt[gi]), nb = grp_cnt[gi] * nc, p0 = grp_p0[gi];
+        switch (grp_G[gi]) {
+          case 2:
+            k_contract<2><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
+            break;
+          case 3:
+            k_contract<3><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
+            break;
+          case 4:
+            k_contract<4><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
+            break;
+          case 5:
+            k_contract<5><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
+            break;
+          default:
+            k_contract<6><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
+            break;
+        }
+        h->count_launch();
+      }
+    }
+    h->prof.end(st, pe, PK_CONTRACT, forward ? con_ff : con_fg, 32.0 * elems);
   };
   // basis at psi_k under H: node states nu_q and psi_{k+1}
   auto step_forward = [&](const double2* x, double2* nodes, double2* y) {
@@ -461,12 +569,18 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
     return SPC_OK;
   };
   const dim3 lgrid(ntiles, std::max(1, h->sm_count * 4 / ntiles));
+  auto costate = [&](double c, const double2* psi, const double2* u) {
+    int pe = h->prof.begin(st);
+    k_costate<<<lgrid, blk, 0, st>>>(d_tf, d_map, d_scol, d_coefs, c, psi, u, lam);
+    h->prof.end(st, pe, PK_COSTATE, 6.0 * elems, 48.0 * elems);
+    h->count_launch();
+  };
 
   // forward sweep: checkpoints, the last segment's states and node states,
   // and F = sum_k c_k (electron-pair reduced matrix of psi_k)
   double2* cur = psi0;
   for (int k = 0; k < nsteps; ++k) {
-    if (cw[k] != 0.0) contract(cur, cur, cw[k], 1, d_facc);
+    if (cw[k] != 0.0) contract(cur, cur, cw[k], true, d_facc);
     double2* nxt;
     if (want_grad && k + 1 >= a_last)
       nxt = seg + S * (k + 1 - a_last);
@@ -478,14 +592,11 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
     if (rc) return rc;
     cur = nxt;
   }
-  if (cw[nsteps] != 0.0) contract(cur, cur, cw[nsteps], 1, d_facc);
+  if (cw[nsteps] != 0.0) contract(cur, cur, cw[nsteps], true, d_facc);
   // backward sweep
   if (want_grad) {
     CK(cudaMemsetAsync(lam, 0, sizeof(double2) * S, st));
-    int pe = h->prof.begin(st);
-    k_costate<<<lgrid, blk, 0, st>>>(d_tf, d_map, d_scol, cur, lam, cw[nsteps] * cI, cw[nsteps] * cP, lam);
-    h->prof.end(st, pe, PK_COSTATE, 6.0 * elems, 48.0 * elems);
-    h->count_launch();
+    costate(cw[nsteps], cur, lam);
   }
   for (int a = want_grad ? a_last : -1; a >= 0; a -= K) {
     const int b = std::min(nsteps, a + K);
@@ -507,29 +618,45 @@ int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int
       if (rc) return rc;
       for (int q = 0; q < nq; ++q) {
         apply(-dt * (1.0 - xq[q]), d_tb, gmu);
-        contract(gmu, nodes + S * q, wq[q] * dt, nsl, d_racc);
+        contract(gmu, nodes + S * q, wq[q] * dt, false, d_racc);
       }
       apply(-dt, d_tb, ulam);
-      int pe = h->prof.begin(st);
-      k_costate<<<lgrid, blk, 0, st>>>(d_tf, d_map, d_scol, seg + S * (k - a), ulam, cw[k] * cI,
-                                       cw[k] * cP, lam);
-      h->prof.end(st, pe, PK_COSTATE, 6.0 * elems, 48.0 * elems);
-      h->count_launch();
+      costate(cw[k], seg + S * (k - a), ulam);
     }
   }
   CK(cudaGetLastError());
-  racc_h.resize((size_t)nslots * nsl * con);
-  facc_h.resize((size_t)nslots * con);
+  std::vector<double2> racc_h((size_t)std::max<int64_t>(rtot, 1) * con), facc_h((size_t)nslots * con);
   CK(cudaMemcpyAsync(racc_h.data(), d_racc, sizeof(double2) * racc_h.size(), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(facc_h.data(), d_facc, sizeof(double2) * facc_h.size(), cudaMemcpyDeviceToHost, st));
   int err_h[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(err_h, h->err.p, 16, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   h->prof.collect();
+  // per-job sample sums in sample order
+  rsum.assign(nj, {});
+  fsum.assign(nj, {});
+  for (int k = 0; k < nj; ++k) {
+    const int ns = jobs[k].nslot;
+    rsum[k].assign((size_t)ns * con, double2{0.0, 0.0});
+    fsum[k].assign(con, double2{0.0, 0.0});
+    for (int s = 0; s < jobs[k].M; ++s) {
+      const int t = tile0[k] + s / SPC_LANES, l = s % SPC_LANES;
+      const double2* R = &racc_h[((size_t)roff[t] + (size_t)l * ns) * con];
+      for (size_t i = 0; i < (size_t)ns * con; ++i) {
+        rsum[k][i].x += R[i].x;
+        rsum[k][i].y += R[i].y;
+      }
+      const double2* F = &facc_h[((size_t)t * SPC_LANES + l) * con];
+      for (size_t i = 0; i < con; ++i) {
+        fsum[k][i].x += F[i].x;
+        fsum[k][i].y += F[i].y;
+      }
+    }
+  }
   h->stats.krylov_builds = builds;
   h->stats.lanczos_fallbacks = 0;
-  h->stats.sample_steps = (int64_t)(cw.size() - 1) * M;
   h->stats.rounds = cache ? 1 : 0;  // 1: node states kept per segment
+  h->stats.sample_steps = (int64_t)nsteps * Mtot;
   h->stats.kernel_launches = h->launches - launches0;
   h->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   if (err_h[0] == 2) return set_error(SPC_ERR_NUMERIC, "singular Pade denominator in expm");

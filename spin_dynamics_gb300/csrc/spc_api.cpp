@@ -447,72 +447,16 @@ int spc_yield_gradient_size(const spc_system* sys) {
   return 15 + 9 * (sys->n_nuc1 + sys->n_nuc2);
 }
 
-int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta, const double* zkets,
-                       int M, double dt, double t_end, int m, int n_quad, int checkpoint_every,
-                       double wS, double wT, double* yields, double* grad) {
-  if (!h || !sys || !theta || !zkets || !yields)
-    return spc::set_error(SPC_ERR_ARG, "spc_yield_gradient: null argument");
-  if (M < 1) return spc::set_error(SPC_ERR_ARG, "M must be positive");
-  if (!(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt must be positive");
-  if (m < 1 || m > 48) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d outside [1, 48]", m);
-  if (n_quad < 1 || n_quad > 16) return spc::set_error(SPC_ERR_ARG, "n_quad %d outside [1, 16]", n_quad);
-  if (checkpoint_every < 0) return spc::set_error(SPC_ERR_ARG, "checkpoint_every must be >= 0");
-  spc::HostSystem hs;
-  int rc = spc::make_host_system(sys, SPC_H_GENERAL, hs);
-  if (rc) return rc;
-  if (h->h.krylov_method == SPC_KRYLOV_LANCZOS && !hs.herm_shift)
-    return spc::set_error(SPC_ERR_ARG, "Lanczos needs H_eff = Hermitian - i*kappa (kS == kT)");
-  for (const spc::NucInfo& q : hs.nuc)
-    if (q.g > 3)
-      return spc::set_error(SPC_ERR_UNSUPPORTED, "the yield gradient takes nuclei of multiplicity <= 3");
-  CKR(cudaSetDevice(h->h.device));
-  spc::Handle& H = h->h;
+// Gradient of one job from its sample sums (pair slot first; then either
+// (electron, nucleus) slots or nucleus-only slots per nucleus with g >= 2).
+static void gradient_from_sums(const spc_system* sys, const spc::HostSystem& hs, int which, int M,
+                               double wS, double wT, const std::vector<double2>& rs,
+                               const std::vector<double2>& fs, double* yields, double* grad) {
   const int nn = (int)hs.nuc.size();
-  const int npar = 15 + 9 * nn;
-  if (grad) std::fill(grad, grad + npar, 0.0);
-  yields[0] = yields[1] = 0.0;
-  const int T = spc::num_time_points(dt, t_end);
-  const int nh = T / 2;
-  if (nh < 2) return SPC_OK;  // get_kinetics adds no Simpson panel
-  const int nsteps = 2 * nh - 2;
-  std::vector<double> cw(nsteps + 1);
-  for (int k = 0; k <= nsteps; ++k)
-    cw[k] = (dt / 3.0) * ((k == 0 || k == nsteps) ? 1.0 : (k % 2 ? 4.0 : 2.0));
-  const int K = std::min(checkpoint_every, nsteps);  // 0: chosen by device memory
-  // H and H^H = H_eff(-kS, -kT) as batch systems 0 and 1
-  spc_system pair[2] = {*sys, *sys};
-  pair[1].kS = -sys->kS;
-  pair[1].kT = -sys->kT;
-  rc = spc_build_h_batch(h, 2, pair, SPC_H_GENERAL);
-  if (rc) return rc;
-  const int64_t Z = hs.Z;
-  if (H.ensure(H.zk, sizeof(double) * 2 * Z * M)) return SPC_ERR_ALLOC;
-  CKR(cudaMemcpyAsync(H.zk.p, zkets, sizeof(double) * 2 * Z * M, cudaMemcpyHostToDevice, H.stream));
-  std::vector<spc::GradSlot> slots;
-  slots.push_back({4, -1, 1, 0, 1});
-  std::vector<int> slot_of(nn, -1);
-  for (int j = 0; j < nn; ++j)
-    if (hs.nuc[j].g >= 2) {
-      slot_of[j] = (int)slots.size();
-      slots.push_back({2 * hs.nuc[j].g, hs.nuc[j].owner, hs.nuc[j].g, 0, hs.nuc[j].stride});
-    }
-  const double cI = wT * sys->kT, cP = wS * sys->kS - wT * sys->kT;
-  std::vector<double2> racc, facc;
-  rc = spc::yield_gradient_run(&H, theta, (const double*)H.zk.p, M, slots, dt, nsteps, cw, cI, cP, m,
-                               n_quad, K, grad != nullptr, racc, facc);
-  if (rc) return rc;
-  // sample sums in sample order
-  const int nsl = (int)slots.size();
   const size_t con = 36;
-  std::vector<cplx> R(nsl * con, 0.0), F(con, 0.0);
-  for (int s = 0; s < M; ++s) {
-    for (int js = 0; js < nsl; ++js)
-      for (size_t i = 0; i < con; ++i) {
-        const double2 v = racc[((size_t)s * nsl + js) * con + i];
-        R[js * con + i] += cplx(v.x, v.y);
-      }
-    for (size_t i = 0; i < con; ++i) F[i] += cplx(facc[(size_t)s * con + i].x, facc[(size_t)s * con + i].y);
-  }
+  std::vector<cplx> R(rs.size()), F(con);
+  for (size_t i = 0; i < rs.size(); ++i) R[i] = cplx(rs[i].x, rs[i].y);
+  for (size_t i = 0; i < con; ++i) F[i] = cplx(fs[i].x, fs[i].y);
   Mat s2[3], I2 = eye(2), S1[3], S2[3];
   spin_ops(2, s2);
   for (int r = 0; r < 3; ++r) {
@@ -531,55 +475,155 @@ int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta
     PT[i] = 0.75 * d + S1S2[i];
   }
   const double inv_m = 1.0 / M;
-  // d/dp: (2/M) Im(sum_ab O_p R); the pair slot is slot 0
-  auto dpair = [&](const Mat& O) { return 2.0 * inv_m * contract_op(O, &R[0], 4).imag(); };
   const double ps_int = contract_op(PS, F.data(), 4).real() * inv_m;
   const double pt_int = contract_op(PT, F.data(), 4).real() * inv_m;
   yields[0] = sys->kS * ps_int;
   yields[1] = sys->kT * pt_int;
-  if (!grad) return SPC_OK;
+  if (!grad) return;
+  // d/dp = (2/M) Im(sum_ab O_p[a][b] R[a][b])
+  auto dslot = [&](const Mat& O, int slot, int G) { return 2.0 * inv_m * contract_op(O, &R[slot * con], G).imag(); };
+  // slot of nucleus j (its (electron, nucleus) or nucleus-only matrix)
+  std::vector<int> slot_of(nn, -1);
+  int next = 1;
+  for (int j = 0; j < nn; ++j)
+    if (hs.nuc[j].g >= 2) slot_of[j] = next++;
   for (int c = 0; c < 3; ++c) {
     Mat O(16);
     for (int i = 0; i < 16; ++i) O[i] = -(S1[c][i] + S2[c][i]);
-    double g = dpair(O);
+    double g = dslot(O, 0, 4);
     for (int j = 0; j < nn; ++j) {
       if (slot_of[j] < 0) continue;
       const int gj = hs.nuc[j].g;
       Mat I[3];
       spin_ops(gj, I);
-      const Mat Oj = kron(I2, 2, I[c], gj);
-      g += hs.nuc[j].gratio * 2.0 * inv_m * contract_op(Oj, &R[slot_of[j] * con], 2 * gj).imag();
+      if (which == SPC_GRAD_ALL)
+        g += hs.nuc[j].gratio * dslot(kron(I2, 2, I[c], gj), slot_of[j], 2 * gj);
+      else
+        g += hs.nuc[j].gratio * dslot(I[c], slot_of[j], gj);
     }
     grad[c] = g;
   }
   {
     Mat O(16);
     for (int i = 0; i < 16; ++i) O[i] = 2.0 * S1S2[i];
-    grad[3] = dpair(O);
+    grad[3] = dslot(O, 0, 4);
   }
   for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) grad[4 + r + 3 * c] = dpair(matmul(S1[r], S2[c], 4));
+    for (int c = 0; c < 3; ++c) grad[4 + r + 3 * c] = dslot(matmul(S1[r], S2[c], 4), 0, 4);
   {
     Mat OS(16), OT(16);
     for (int i = 0; i < 16; ++i) {
       OS[i] = cplx(0.0, -0.5) * PS[i];
       OT[i] = cplx(0.0, -0.5) * PT[i];
     }
-    grad[13] = dpair(OS) + wS * ps_int;
-    grad[14] = dpair(OT) + wT * pt_int;
+    grad[13] = dslot(OS, 0, 4) + wS * ps_int;
+    grad[14] = dslot(OT, 0, 4) + wT * pt_int;
   }
+  if (which != SPC_GRAD_ALL) return;  // hyperfine entries stay 0
   for (int j = 0; j < nn; ++j) {
     if (slot_of[j] < 0) continue;
     const int gj = hs.nuc[j].g;
     Mat I[3];
     spin_ops(gj, I);
     for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 3; ++c) {
-        const Mat O = kron(s2[r], 2, I[c], gj);
-        grad[15 + 9 * j + r + 3 * c] = 2.0 * inv_m * contract_op(O, &R[slot_of[j] * con], 2 * gj).imag();
-      }
+      for (int c = 0; c < 3; ++c) grad[15 + 9 * j + r + 3 * c] = dslot(kron(s2[r], 2, I[c], gj), slot_of[j], 2 * gj);
+  }
+}
+
+int spc_yield_gradient_batch(spc_handle* h, int n_jobs, const spc_system* systems, const int* M,
+                             const double* theta, const double* zkets, double dt, double t_end, int m,
+                             int n_quad, int checkpoint_every, double wS, double wT, int which,
+                             double* yields, double* grad) {
+  if (!h || n_jobs < 1 || !systems || !M || !theta || !zkets || !yields)
+    return spc::set_error(SPC_ERR_ARG, "spc_yield_gradient_batch: null argument");
+  if (!(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt must be positive");
+  if (m < 1 || m > 48) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d outside [1, 48]", m);
+  if (n_quad < 1 || n_quad > 16) return spc::set_error(SPC_ERR_ARG, "n_quad %d outside [1, 16]", n_quad);
+  if (checkpoint_every < 0) return spc::set_error(SPC_ERR_ARG, "checkpoint_every must be >= 0");
+  if (which != SPC_GRAD_ALL && which != SPC_GRAD_FIELD)
+    return spc::set_error(SPC_ERR_ARG, "unknown gradient set %d", which);
+  std::vector<spc::HostSystem> hs(n_jobs);
+  int64_t ztot = 0, gtot = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    if (M[k] < 1) return spc::set_error(SPC_ERR_ARG, "job %d has no samples", k);
+    int rc = spc::make_host_system(&systems[k], SPC_H_GENERAL, hs[k]);
+    if (rc) return rc;
+    if (h->h.krylov_method == SPC_KRYLOV_LANCZOS && !hs[k].herm_shift)
+      return spc::set_error(SPC_ERR_ARG, "Lanczos needs H_eff = Hermitian - i*kappa (kS == kT)");
+    for (const spc::NucInfo& q : hs[k].nuc) {
+      if (which == SPC_GRAD_ALL && q.g > 3)
+        return spc::set_error(SPC_ERR_UNSUPPORTED,
+                              "hyperfine gradients take nuclei of multiplicity <= 3 (use SPC_GRAD_FIELD)");
+      if (q.g > 6) return spc::set_error(SPC_ERR_UNSUPPORTED, "gradients take nuclei of multiplicity <= 6");
+    }
+    ztot += (int64_t)M[k] * hs[k].Z;
+    gtot += 15 + 9 * (int64_t)hs[k].nuc.size();
+  }
+  CKR(cudaSetDevice(h->h.device));
+  spc::Handle& H = h->h;
+  if (grad) std::fill(grad, grad + gtot, 0.0);
+  std::fill(yields, yields + 2 * n_jobs, 0.0);
+  const int T = spc::num_time_points(dt, t_end);
+  const int nh = T / 2;
+  if (nh < 2) return SPC_OK;  // get_kinetics adds no Simpson panel
+  const int nsteps = 2 * nh - 2;
+  std::vector<double> cw(nsteps + 1);
+  for (int k = 0; k <= nsteps; ++k)
+    cw[k] = (dt / 3.0) * ((k == 0 || k == nsteps) ? 1.0 : (k % 2 ? 4.0 : 2.0));
+  // H_k and H_k^H = H_eff(-kS, -kT) as batch systems 2k and 2k + 1
+  std::vector<spc_system> pairs(2 * (size_t)n_jobs);
+  for (int k = 0; k < n_jobs; ++k) {
+    pairs[2 * k] = pairs[2 * k + 1] = systems[k];
+    pairs[2 * k + 1].kS = -systems[k].kS;
+    pairs[2 * k + 1].kT = -systems[k].kT;
+  }
+  int rc = spc_build_h_batch(h, 2 * n_jobs, pairs.data(), SPC_H_GENERAL);
+  if (rc) return rc;
+  if (H.ensure(H.zk, sizeof(double) * 2 * ztot)) return SPC_ERR_ALLOC;
+  CKR(cudaMemcpyAsync(H.zk.p, zkets, sizeof(double) * 2 * ztot, cudaMemcpyHostToDevice, H.stream));
+  std::vector<spc::GradSlot> slots;
+  std::vector<spc::GradJob> jobs(n_jobs);
+  int64_t zoff = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    spc::GradJob& J = jobs[k];
+    J.sys = 2 * k;
+    J.M = M[k];
+    J.slot0 = (int)slots.size();
+    J.zk = (const double2*)H.zk.p + zoff;
+    J.cI = wT * systems[k].kT;
+    J.cP = wS * systems[k].kS - wT * systems[k].kT;
+    zoff += (int64_t)M[k] * hs[k].Z;
+    slots.push_back({4, -1, 1, 0, 1});
+    if (grad)
+      for (const spc::NucInfo& q : hs[k].nuc)
+        if (q.g >= 2) {
+          if (which == SPC_GRAD_ALL)
+            slots.push_back({2 * q.g, q.owner, q.g, 0, q.stride});
+          else
+            slots.push_back({q.g, -2, q.g, 0, q.stride});
+        }
+    J.nslot = (int)slots.size() - J.slot0;
+  }
+  const int K = std::min(checkpoint_every, nsteps);  // 0: chosen by device memory
+  std::vector<std::vector<double2>> rsum, fsum;
+  rc = spc::yield_gradient_run(&H, theta, jobs, slots, dt, nsteps, cw, m, n_quad, K, grad != nullptr, rsum,
+                               fsum);
+  if (rc) return rc;
+  int64_t goff = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    gradient_from_sums(&systems[k], hs[k], which, M[k], wS, wT, rsum[k], fsum[k], yields + 2 * k,
+                       grad ? grad + goff : nullptr);
+    goff += 15 + 9 * (int64_t)hs[k].nuc.size();
   }
   return SPC_OK;
+}
+
+int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta, const double* zkets,
+                       int M, double dt, double t_end, int m, int n_quad, int checkpoint_every,
+                       double wS, double wT, double* yields, double* grad) {
+  if (!sys) return spc::set_error(SPC_ERR_ARG, "spc_yield_gradient: null argument");
+  return spc_yield_gradient_batch(h, 1, sys, &M, theta, zkets, dt, t_end, m, n_quad, checkpoint_every, wS, wT,
+                                  SPC_GRAD_ALL, yields, grad);
 }
 
 }  // extern "C"

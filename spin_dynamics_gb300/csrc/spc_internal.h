@@ -151,14 +151,25 @@ struct JobSpec {
 };
 
 // One reduced-matrix slot of the yield gradient: the electron pair (G = 4,
-// owner = -1) or (spin of electron `owner`, nucleus of multiplicity g) with
-// G = 2g classes; stride is the nucleus' stride in the nuclear index.
+// owner = -1), one nucleus alone (G = g, owner = -2), or (spin of electron
+// `owner`, nucleus of multiplicity g) with G = 2g classes; stride is the
+// nucleus' stride in the nuclear index.
 struct GradSlot {
   int G;
   int owner;
   int g;
   int pad;
   int64_t stride;
+};
+// One job of the yield gradient: system `sys` of the batch store (its H^H at
+// sys + 1), M samples (device, M x Z), slots [slot0, slot0 + nslot) of the
+// slot table (slot0 is the electron pair).
+struct GradJob {
+  int sys;
+  int M;
+  int slot0, nslot;
+  const double2* zk;
+  double cI, cP;  // source of the costate: cI psi + cP Pi_S psi (times c_k)
 };
 
 int set_error(int code, const char* fmt, ...);
@@ -168,14 +179,15 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
 int propagate_batch(Handle* h, const double* theta, const double* init_pop,
                     const std::vector<JobSpec>& jobs, double dt, double t_end, int m, double tol,
                     int T);
-// Adjoint sweep of spc_yield_gradient on the batch store's systems 0 (H) and
-// 1 (H^H): per-sample reduced matrices racc (slots x cs.size() x 36 complex)
-// of the gradient integrals and facc (slots x 36) of sum_k cw[k] psi_k psi_k^H
-// on the electron pair. want_grad = false runs the forward sweep only.
-int yield_gradient_run(Handle* h, const double* theta, const double* zk_dev, int M,
+// Adjoint sweeps of spc_yield_gradient(_batch) over the batch store's
+// Hamiltonians: per job, the sample sums of the reduced matrices of the
+// gradient integrals (rsum[job]: nslot x 36 complex) and of
+// sum_k cw[k] psi_k psi_k^H on the electron pair (fsum[job]: 36 complex).
+// want_grad = false runs the forward sweep only.
+int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob>& jobs,
                        const std::vector<GradSlot>& cs, double dt, int nsteps,
-                       const std::vector<double>& cw, double cI, double cP, int m, int nq, int K,
-                       bool want_grad, std::vector<double2>& racc_h, std::vector<double2>& facc_h);
+                       const std::vector<double>& cw, int m, int nq, int K, bool want_grad,
+                       std::vector<std::vector<double2>>& rsum, std::vector<std::vector<double2>>& fsum);
 // Nonzero count spc_build_h produces for a system (closed form per mode).
 int64_t predict_nnz(const HostSystem& hs, int mode);
 int num_time_points(double dt, double t_end);

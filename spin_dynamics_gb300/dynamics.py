@@ -303,6 +303,42 @@ class TraceSampler:
             _dptr(g)))
         return YieldGradient.unpack(y, g, len(sys.e1.g_I), len(sys.e2.g_I))
 
+    def yield_gradient_batch(self, systems, fields, zkets_list, dt: float, t_end: float, m: int,
+                             n_quad: int = 6, checkpoint_every: int = 0, wS: float = 1.0,
+                             wT: float = 0.0, hyperfine: bool = True, init_state: str = "singlet",
+                             gradient: bool = True) -> list:
+        """spc_yield_gradient_batch: job k = (systems[k], fields[k],
+        zkets_list[k]); all jobs share every launch. hyperfine=False computes
+        the B, J, D, kS, kT entries only (nuclei up to multiplicity 6).
+        gradient=False returns the yields only. Returns one YieldGradient per
+        job."""
+        structs, keep = [], []
+        for s, B in zip(systems, fields):
+            st, k = make_system(s, B)
+            structs.append(st)
+            keep.append(k)
+        arr = (nat.spc_system * len(structs))(*structs)
+        sizes = [nat.lib().spc_yield_gradient_size(C.byref(st)) for st in structs]
+        M = np.array([z.shape[0] for z in zkets_list], np.int32)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(z, np.complex128).reshape(-1)
+                                                    for z in zkets_list]))
+        th, _ = init_el_state(init_state)
+        th = np.ascontiguousarray(th).view(np.float64)
+        y = np.zeros(2 * len(structs))
+        g = np.zeros(int(sum(sizes)))
+        which = nat.SPC_GRAD_ALL if hyperfine else nat.SPC_GRAD_FIELD
+        nat.check(nat.lib().spc_yield_gradient_batch(
+            self._h, len(structs), C.cast(arr, C.c_void_p), _dptr(M), _dptr(th),
+            _dptr(flat.view(np.float64)), float(dt), float(t_end), int(m), int(n_quad),
+            int(checkpoint_every), float(wS), float(wT), which, _dptr(y),
+            _dptr(g) if gradient else None))
+        out, off = [], 0
+        for k, s in enumerate(systems):
+            out.append(YieldGradient.unpack(y[2 * k:2 * k + 2], g[off:off + sizes[k]], len(s.e1.g_I),
+                                            len(s.e2.g_I)))
+            off += sizes[k]
+        return out
+
     def stepwise_yields(self, sys: SysParam, B, zkets, dt: float, t_end: float, m: int,
                         init_state: str = "singlet") -> tuple:
         """(Phi_S, Phi_T) of the stepwise propagation spc_yield_gradient

@@ -178,3 +178,67 @@ def test_torch_autograd_matches_adjoint(sampler):
         lambda q: yield_objective(q, sampler, s, zk, DT, t_end, 32, n_quad=8),
         (p.detach().clone().requires_grad_(True),), eps=1e-6, atol=1e-8, rtol=1e-5)
     assert ok
+
+
+def test_batch_equals_single_calls(sampler):
+    """Jobs of dims 48, 288 and 72 with 5, 33 and 7 samples in one sweep
+    against one call per job."""
+    a = aniso_pair([2], [2, 3], seed=5, kS=0.03, kT=0.01)
+    b = W.small_pair()
+    rng = np.random.default_rng(4)
+    for e in (b.e1, b.e2):
+        e.A = [(lambda R: R @ np.diag(rng.uniform(-1, 1, 3)) @ R.T)(W._haar_rotation(rng)) for _ in e.A]
+    b.kS, b.kT = 0.02, 0.05
+    c = aniso_pair([3, 2], [3], seed=6, kS=0.01, kT=0.01)
+    systems = [a, b, c]
+    fields = [np.array([0.1, 0.0, 0.2]), np.array([0.0, 0.03, 0.05]), np.array([0.05, 0.05, 0.0])]
+    zks = [W.random_phase_samples(s.Z, M, seed=20 + i) for i, (s, M) in enumerate(zip(systems, (5, 33, 7)))]
+    t_end = 9 * DT
+    got = sampler.yield_gradient_batch(systems, fields, zks, DT, t_end, 24, n_quad=6, checkpoint_every=3)
+    for s, B, zk, g in zip(systems, fields, zks, got):
+        one = sampler.yield_gradient(s, B, zk, DT, t_end, 24, n_quad=6, checkpoint_every=3)
+        scale = np.max(np.abs(one.raw))
+        assert np.max(np.abs(g.raw - one.raw)) <= 1e-12 * scale
+        assert abs(g.Phi_S - one.Phi_S) <= 1e-14
+        assert abs(g.Phi_T - one.Phi_T) <= 1e-14
+
+
+def test_field_set_matches_full_set(sampler):
+    s = aniso_pair([2, 2], [3], seed=3, kS=0.02, kT=0.01)
+    B = np.array([0.02, -0.04, 0.1])
+    zk = W.random_phase_samples(s.Z, 9, seed=5)
+    t_end = 7 * DT
+    full = sampler.yield_gradient(s, B, zk, DT, t_end, 24)
+    fld = sampler.yield_gradient_batch([s], [B], [zk], DT, t_end, 24, hyperfine=False)[0]
+    scale = np.max(np.abs(full.raw))
+    assert np.max(np.abs(fld.raw[:15] - full.raw[:15])) <= 1e-12 * scale
+    assert not np.any(fld.raw[15:])
+
+
+def test_field_gradient_of_a_spin2_group(sampler):
+    """A symmetry-block-like system: one effective nucleus of multiplicity 5
+    (four equivalent 1H at total spin 2, gyromagnetic ratio of 1H) and one 1H;
+    dPhi/d(B, J, D, kS, kT) against central differences of the dense model."""
+    from spin_dynamics_gb300.spinsys import GAMMA_1H
+    s = SysParam(e1=Electron(g_I=[5], A=[np.eye(3) * 0.4], gamma_I=[GAMMA_1H]),
+                 e2=Electron(g_I=[2], A=[np.diag([0.3, 0.5, -0.2])], gamma_I=[GAMMA_1H]),
+                 J=0.02, D=W.axial_dipolar(-0.3), kS=0.03, kT=0.01)
+    B = np.array([0.3, 0.1, 0.4])
+    zk = W.random_phase_samples(s.Z, 4, seed=8)
+    t_end = 10 * DT
+    got = sampler.yield_gradient_batch([s], [B], [zk], DT, t_end, 40, n_quad=8, hyperfine=False)[0]
+
+    def phi(v):
+        H = dense.hamiltonian(s.e1.g_I, s.e1.A, s.e2.g_I, s.e2.A, v[0:3], v[3], v[4:13].reshape(3, 3).T,
+                              v[13], v[14], gam1=s.e1.gamma_I, gam2=s.e2.gamma_I)
+        return dense.stepwise_yields(H, zk, DT, num_time_points(DT, t_end), v[13], v[14])[0]
+
+    v0 = np.concatenate([B, [s.J], np.asarray(s.D).T.reshape(9), [s.kS, s.kT]])
+    ref = np.zeros(15)
+    for i in range(15):
+        e = np.zeros(15)
+        e[i] = 1e-5
+        ref[i] = (phi(v0 + e) - phi(v0 - e)) / 2e-5
+    assert abs(got.Phi_S - phi(v0)) <= 1e-12
+    err = np.abs(got.raw[:15] - ref)
+    assert np.max(err) <= 2e-7 * np.max(np.abs(ref)), (np.argmax(err), got.raw[:15], ref)
