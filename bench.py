@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--batch-window-ns", type=float, default=20.0)
     p.add_argument("--batch-krylov", type=int, default=20)
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient leg")
+    p.add_argument("--no-batch-adjoint", action="store_true", help="skip the batched-adjoint leg")
+    p.add_argument("--batch-adjoint-window-ns", type=float, default=10.0)
     p.add_argument("--adjoint-samples", type=int, default=256)
     p.add_argument("--adjoint-window-ns", type=float, default=20.0)
     p.add_argument("--adjoint-checkpoint", type=int, default=10)
@@ -267,9 +269,11 @@ def run_ours(args, rank, world, local_rank):
                "ms_per_step": el * 1e3}
     batched = None if args.no_batch else batched_leg(args, sampler, local_rank)
     adjoint = None if args.no_adjoint else adjoint_leg(args, sampler, value / world)
+    batch_adjoint = None if args.no_batch_adjoint else batched_adjoint_leg(args, sampler, local_rank)
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
-    return dict(ms=ms, value=value, e2e=e2e, batched=batched, adjoint=adjoint, prof=prof, clocks=clk.summary(), launches=launches,
+    return dict(ms=ms, value=value, e2e=e2e, batched=batched, adjoint=adjoint, batch_adjoint=batch_adjoint,
+                prof=prof, clocks=clk.summary(), launches=launches,
                 builds=builds, fallbacks=fallbacks, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
                 sysp=sysp, B=B, sim=sim)
 
@@ -283,15 +287,8 @@ def batched_leg(args, sampler, local_rank):
 
     from spin_dynamics_gb300.dynamics import num_time_points
 
-    pairs = W.uneven_pairs(args.batch_pairs)
-    dirs = W.fibonacci_sphere(args.batch_orient)
-    systems, fields, zks, Ms = [], [], [], []
-    for p, (s, M) in enumerate(pairs):
-        for d in dirs:
-            systems.append(s)
-            fields.append(d)
-            zks.append(W.random_phase_samples(s.Z, M, seed=100 + p))
-            Ms.append(M)
+    pairs, dirs, systems, fields, zks = uneven_jobs(args)
+    Ms = [z.shape[0] for z in zks]
     dt = 1.0 * 176.08596 / 1000
     t_end = args.batch_window_ns * 176.08596 / 1000
     m = args.batch_krylov
@@ -332,6 +329,72 @@ def batched_leg(args, sampler, local_rank):
             "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m,
             "workload": "uneven pairs (2-10 nuclei from 1H/14N, anisotropic) x Fibonacci-sphere "
                         "orientations at 0.05 mT, own Hamiltonian per job"}
+
+
+def uneven_jobs(args):
+    pairs = W.uneven_pairs(args.batch_pairs)
+    dirs = W.fibonacci_sphere(args.batch_orient)
+    systems, fields, zks = [], [], []
+    for p, (s, M) in enumerate(pairs):
+        for d in dirs:
+            systems.append(s)
+            fields.append(d)
+            zks.append(W.random_phase_samples(s.Z, M, seed=100 + p))
+    return pairs, dirs, systems, fields, zks
+
+
+def batched_adjoint_leg(args, sampler, local_rank):
+    """Yields and full gradients of every job of the uneven set (pairs x
+    orientations) in one spc_yield_gradient_batch call, against one
+    spc_yield_gradient call per job and against the plain per-instance
+    forward (spc_build_h + spc_trace_sampling, Krylov reuse) of the same
+    jobs over the same window. Host vectors in, results out, in every arm."""
+    import torch
+
+    pairs, dirs, systems, fields, zks = uneven_jobs(args)
+    dt = 1.0 * 176.08596 / 1000
+    t_end = args.batch_adjoint_window_ns * 176.08596 / 1000
+    m = args.batch_krylov
+
+    def batched():
+        return sampler.yield_gradient_batch(systems, fields, zks, dt, t_end, m, n_quad=args.adjoint_quad)
+
+    def per_instance():
+        return [sampler.yield_gradient(s, f, z, dt, t_end, m, n_quad=args.adjoint_quad)
+                for s, f, z in zip(systems, fields, zks)]
+
+    def plain():
+        out = []
+        for s, f, z in zip(systems, fields, zks):
+            sampler.build_h(s, f, "general")
+            out.append(sampler.trace_sampling(z, dt, t_end, m, 1e-5))
+        return out
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    gb, t_b = timed(batched)
+    st = sampler.stats()
+    gi, t_i = timed(per_instance)
+    _, t_p = timed(plain)
+    steps = st["sample_steps"] // sum(z.shape[0] for z in zks)
+    work = sum(z.shape[0] for z in zks) * steps
+    dev = max(float(np.max(np.abs(a.raw - b.raw)) / max(np.max(np.abs(b.raw)), 1e-300)) for a, b in zip(gb, gi))
+    dims = [4 * s.Z for s in systems]
+    return {"value": work / t_b, "unit": "sample-steps/s", "seconds": t_b,
+            "per_instance_adjoint_value": work / t_i, "ratio_vs_per_instance_adjoint": t_i / t_b,
+            "plain_per_instance_value": work / t_p, "cost_vs_plain_per_instance": t_b / t_p,
+            "max_rel_diff_vs_per_instance": dev, "jobs": len(zks), "pairs": len(pairs),
+            "orientations": len(dirs), "dims": [min(dims), max(dims)],
+            "samples": int(sum(z.shape[0] for z in zks)), "dt_steps": int(steps), "krylov": m,
+            "params_per_job": [int(min(g.raw.size for g in gb)), int(max(g.raw.size for g in gb))],
+            "workload": "uneven pairs x orientations: Phi_S and dPhi_S/d(B, J, D, kS, kT, every "
+                        "hyperfine element) per job"}
 
 
 def adjoint_leg(args, sampler, plain_value):
@@ -465,7 +528,8 @@ def main():
                           "fp64": {"achieved_tflops": ach_tf, "peak_tflops": r["fp64_peak"] / 1e12,
                                    "frac": (ach_tf * 1e12 / r["fp64_peak"]) if ach_tf else None,
                                    "peak_source": "measured DFMA probe (spc_fp64_peak)"}},
-                kernel_share=share, batched=r["batched"], adjoint=r["adjoint"], cpu_baseline=cpu)
+                kernel_share=share, batched=r["batched"], adjoint=r["adjoint"],
+                batched_adjoint=r["batch_adjoint"], cpu_baseline=cpu)
     print(json.dumps(line))
 
 

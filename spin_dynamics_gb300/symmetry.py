@@ -234,32 +234,134 @@ def rng_stream(seed, n: int) -> np.ndarray:
     return out[:n]
 
 
+def _selected(sys_: SysParam, sim: SimParam):
+    """Blocks that run (weight >= sim.block_tol, from sim.restart on), with
+    their 1-based indices and per-block seeds drawn from sim.seed."""
+    bl = blocks(sys_, sim.M1, sim.M2)
+    seeds = rng_stream(sim.seed, 2 * len(bl)).reshape(-1, 2) if bl else np.zeros((0, 2), np.uint64)
+    start = sim.restart if sim.isRestart else 1
+    out = []
+    for i, (w_k, sysb, Zb) in enumerate(bl, start=1):
+        if i < start or w_k < sim.block_tol:
+            continue
+        out.append((i, w_k, sysb, Zb, (int(seeds[i - 1, 0]), int(seeds[i - 1, 1]))))
+    return out
+
+
+def _block_vectors(sel, sim: SimParam, exact_blocks: bool):
+    from . import dynamics
+    if exact_blocks:
+        return [np.eye(Zb, dtype=np.complex128) for _, _, _, Zb, _ in sel]
+    return [dynamics.seeded_samples(seed, Zb, sim.N_samples) for _, _, _, Zb, seed in sel]
+
+
+def _chunks(rows_x_samples, budget_entries):
+    """Split jobs (list of rows * samples) into consecutive groups whose sum
+    stays under budget_entries (at least one job per group)."""
+    groups, cur, tot = [], [], 0
+    for i, x in enumerate(rows_x_samples):
+        if cur and tot + x > budget_entries:
+            groups.append(cur)
+            cur, tot = [], 0
+        cur.append(i)
+        tot += x
+    if cur:
+        groups.append(cur)
+    return groups
+
+
+def _budget_entries(states_per_entry: float) -> float:
+    """Vector entries (rows x samples) a batch may hold: a third of the free
+    device memory over `states_per_entry` complex states per entry."""
+    try:
+        import torch
+        free, _ = torch.cuda.mem_get_info()
+    except Exception:
+        free = 16 << 30
+    return max(1.0, free / 3.0 / (16.0 * states_per_entry))
+
+
 def symmetrised_dynamics(sys_: SysParam, sim: SimParam, out: Optional[str] = None, sampler=None,
                          exact_blocks: bool = False) -> Observables:
     """symmetrised_dynamics (src/symmetry.f90:16-139): trace sampling over
     every block whose weight reaches sim.block_tol (sim.N_samples vectors per
     block, seeds drawn per block from sim.seed), each scaled by its weight,
-    summed, then yields (get_kinetics) and the output files. With
-    exact_blocks=True every block is traced exactly over its basis states."""
+    summed in block order, then yields (get_kinetics) and the output files.
+    The blocks propagate together through the batch API (groups bounded by
+    device memory). With exact_blocks=True every block is traced exactly over
+    its basis states."""
     from . import dynamics
     sp = sampler or dynamics.default_sampler()
-    bl = blocks(sys_, sim.M1, sim.M2)
-    seeds = rng_stream(sim.seed, 2 * len(bl)).reshape(-1, 2) if bl else np.zeros((0, 2), np.uint64)
+    sel = _selected(sys_, sim)
+    zks = _block_vectors(sel, sim, exact_blocks)
     T = dynamics.num_time_points(sim.dt, sim.t_end)
     res = Observables.zeros(T)
-    start = sim.restart if sim.isRestart else 1
-    for i, (w_k, sysb, Zb) in enumerate(bl, start=1):
-        if i < start or w_k < sim.block_tol:
-            continue
-        sp.build_h(sysb, -sysb.e1.w, "reference")
-        if exact_blocks:
-            zk = np.eye(Zb, dtype=np.complex128)
-        else:
-            zk = dynamics.seeded_samples((int(seeds[i - 1, 0]), int(seeds[i - 1, 1])), Zb, sim.N_samples)
-        r = sp.trace_sampling(zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol, sim.init_state)
-        r.scale(w_k)
-        res.update(r)
+    sizes = [4 * Zb * z.shape[0] for (_, _, _, Zb, _), z in zip(sel, zks)]
+    for grp in _chunks(sizes, _budget_entries(sim.N_krylov + 4)):
+        systems = [sel[j][2] for j in grp]
+        sp.build_h_batch(systems, [-s.e1.w for s in systems], "reference")
+        rs = sp.trace_sampling_batch([zks[j] for j in grp], sim.dt, sim.t_end, sim.N_krylov, sim.tol,
+                                     sim.init_state)
+        for j, r in zip(grp, rs):
+            r.scale(sel[j][1])
+            res.update(r)
     res.get_kinetics(sim.dt, sys_.kS, sys_.kT)
     if out is not None:
         res.output(out)
     return res
+
+
+def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, directions=None,
+                               n_quad: int = 6, checkpoint_every: int = 0, wS: float = 1.0,
+                               wT: float = 0.0, exact_blocks: bool = False) -> list:
+    """Yields of the block decomposition and their gradient with respect to
+    the field vector, J, D, kS and kT (the field set of
+    spc_yield_gradient_batch), for the field B (mT, 3-vector) or for each of
+    `directions` (n x 3 unit vectors, field |B| along each). Every (block,
+    direction) job shares one adjoint sweep (groups bounded by device
+    memory). Block results enter with their weights. Returns one dict per
+    direction: Phi_S, Phi_T, B (3), J, D (3 x 3), kS, kT, and for directions
+    the derivatives with respect to the polar and azimuthal angles theta, phi
+    of the field."""
+    from . import dynamics
+    sp = sampler or dynamics.default_sampler()
+    B = np.asarray(B, float).reshape(3)
+    if directions is None:
+        fields = [B]
+    else:
+        fields = [np.linalg.norm(B) * np.asarray(d, float) / np.linalg.norm(d) for d in directions]
+    sel = _selected(sys_, sim)
+    zks = _block_vectors(sel, sim, exact_blocks)
+    jobs = [(f, j) for f in range(len(fields)) for j in range(len(sel))]
+    acc = [dict(Phi_S=0.0, Phi_T=0.0, B=np.zeros(3), J=0.0, D=np.zeros((3, 3)), kS=0.0, kT=0.0)
+           for _ in fields]
+    sizes = [4 * sel[j][3] * zks[j].shape[0] for _, j in jobs]
+    # states per vector entry held by the sweep: basis, checkpoints, segment, node states
+    for grp in _chunks(sizes, _budget_entries(sim.N_krylov + 6 + 8 * (n_quad + 1))):
+        systems = [sel[jobs[q][1]][2] for q in grp]
+        got = sp.yield_gradient_batch(systems, [fields[jobs[q][0]] for q in grp], [zks[jobs[q][1]] for q in grp],
+                                      sim.dt, sim.t_end, sim.N_krylov, n_quad=n_quad,
+                                      checkpoint_every=checkpoint_every, wS=wS, wT=wT, hyperfine=False,
+                                      init_state=sim.init_state)
+        for q, g in zip(grp, got):
+            f, j = jobs[q]
+            w = sel[j][1]
+            a = acc[f]
+            a["Phi_S"] += w * g.Phi_S
+            a["Phi_T"] += w * g.Phi_T
+            a["B"] += w * g.B
+            a["J"] += w * g.J
+            a["D"] += w * g.D
+            a["kS"] += w * g.kS
+            a["kT"] += w * g.kT
+    if directions is not None:
+        for f, a in zip(fields, acc):
+            r = np.linalg.norm(f)
+            th = np.arccos(np.clip(f[2] / r, -1.0, 1.0))
+            ph = np.arctan2(f[1], f[0])
+            dth = r * np.array([np.cos(th) * np.cos(ph), np.cos(th) * np.sin(ph), -np.sin(th)])
+            dph = r * np.array([-np.sin(th) * np.sin(ph), np.sin(th) * np.cos(ph), 0.0])
+            a["theta"], a["phi"] = float(th), float(ph)
+            a["dtheta"] = float(a["B"] @ dth)
+            a["dphi"] = float(a["B"] @ dph)
+    return acc

@@ -62,3 +62,40 @@ def test_block_tolerance_skips_light_blocks(sampler):
     assert 0 < len(kept) < len(bl)
     res = S.symmetrised_dynamics(s, sm, sampler=sampler, exact_blocks=True)
     assert abs(res.P_S[0] - sum(kept)) < 1e-14  # P_S(0) = 1 per block, weighted
+
+
+def test_block_gradient_equals_full_space_gradient(sampler):
+    """Exact traces: the weighted block yields and their field/coupling
+    gradient equal the full-space ones (basis-state samples, Z of them)."""
+    s = small_equivalent_system()
+    sm = sim()
+    sm.t_end = 12 * sm.dt
+    B = np.array([0.03, 0.02, 0.1])
+    blk = S.symmetrised_yield_gradient(s, sm, B, sampler=sampler, exact_blocks=True, n_quad=8)[0]
+    full = sampler.yield_gradient_batch([s], [B], [np.eye(s.Z, dtype=complex)], sm.dt, sm.t_end,
+                                        sm.N_krylov, n_quad=8, hyperfine=False)[0]
+    assert abs(blk["Phi_S"] - full.Phi_S) <= 1e-9 * abs(full.Phi_S)
+    scale = max(np.max(np.abs(full.B)), abs(full.J), abs(full.kS))
+    for k in ("B", "J", "D", "kS", "kT"):
+        assert np.max(np.abs(np.asarray(blk[k]) - np.asarray(getattr(full, k)))) <= 1e-8 * scale, k
+
+
+def test_compass_map_angle_derivatives(sampler):
+    """dPhi_S/dtheta, dPhi_S/dphi of the block decomposition against central
+    differences of its own yields."""
+    s = small_equivalent_system()
+    sm = sim(M=4)
+    sm.t_end = 10 * sm.dt
+    dirs = np.array([[0.3, 0.4, 0.866], [-0.5, 0.2, 0.3]])
+    Bmag = 0.2
+    got = S.symmetrised_yield_gradient(s, sm, [0, 0, Bmag], sampler=sampler, directions=dirs, n_quad=8)
+    for d, g in zip(dirs, got):
+        th, ph = g["theta"], g["phi"]
+        for key, (dth, dph) in (("dtheta", (1e-5, 0.0)), ("dphi", (0.0, 1e-5))):
+            vals = []
+            for sgn in (1, -1):
+                t2, p2 = th + sgn * dth, ph + sgn * dph
+                f = Bmag * np.array([np.sin(t2) * np.cos(p2), np.sin(t2) * np.sin(p2), np.cos(t2)])
+                vals.append(S.symmetrised_yield_gradient(s, sm, f, sampler=sampler, n_quad=8)[0]["Phi_S"])
+            fd = (vals[0] - vals[1]) / 2e-5
+            assert abs(g[key] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(g["Phi_S"])), (key, g[key], fd)

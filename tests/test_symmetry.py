@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from spin_dynamics_gb300 import symmetry as S
-from spin_dynamics_gb300.spinsys import GAMMA_14N, GAMMA_1H, GAMMA_E, Electron, SysParam
+from spin_dynamics_gb300.spinsys import GAMMA_14N, GAMMA_1H, GAMMA_E, Electron, SimParam, SysParam
 
 
 def test_cartesian_product_order_and_weights():
@@ -81,3 +81,20 @@ def test_block_sum_equals_full_trace(oracle):
     n = int(np.ceil(t_end / dt)) + 1
     for k in tot:
         assert np.max(np.abs(tot[k][:n] - full[k][:n])) < 1e-11, k
+
+
+def test_selected_blocks_and_their_seeded_vectors():
+    from spin_dynamics_gb300.dynamics import seeded_samples
+    s = small_equivalent_system()
+    sm = SimParam.from_input_units(type="symmetry_dynamics", B=[0.1], init_state="singlet",
+                                   seed=(42, 99), N_samples=3, t_end_ns=10.0, dt_ns=1.0,
+                                   N_krylov=8, tol=1e-5, M1=1, M2=1, block_tol=0.2)
+    sel = S._selected(s, sm)
+    bl = S.blocks(s, 1, 1)
+    assert [i for i, *_ in sel] == [i + 1 for i, (w, _, _) in enumerate(bl) if w >= 0.2]
+    seeds = S.rng_stream(sm.seed, 2 * len(bl)).reshape(-1, 2)
+    zks = S._block_vectors(sel, sm, exact_blocks=False)
+    for (i, w, b, Zb, seed), z in zip(sel, zks):
+        assert seed == (int(seeds[i - 1, 0]), int(seeds[i - 1, 1]))
+        assert np.array_equal(z, seeded_samples(seed, Zb, 3))
+    assert S._chunks([5, 5, 5, 20, 1], 10) == [[0, 1], [2], [3], [4]]
