@@ -67,6 +67,10 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient leg")
     p.add_argument("--no-batch-adjoint", action="store_true", help="skip the batched-adjoint leg")
     p.add_argument("--batch-adjoint-window-ns", type=float, default=10.0)
+    p.add_argument("--no-symmetry", action="store_true", help="skip the symmetry-block leg")
+    p.add_argument("--sym-samples", type=int, default=32)
+    p.add_argument("--sym-window-ns", type=float, default=4.0)
+    p.add_argument("--sym-directions", type=int, default=2)
     p.add_argument("--adjoint-samples", type=int, default=256)
     p.add_argument("--adjoint-window-ns", type=float, default=20.0)
     p.add_argument("--adjoint-checkpoint", type=int, default=10)
@@ -270,9 +274,11 @@ def run_ours(args, rank, world, local_rank):
     batched = None if args.no_batch else batched_leg(args, sampler, local_rank)
     adjoint = None if args.no_adjoint else adjoint_leg(args, sampler, value / world)
     batch_adjoint = None if args.no_batch_adjoint else batched_adjoint_leg(args, sampler, local_rank)
+    symmetry = None if args.no_symmetry else symmetry_leg(args, sampler)
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
     return dict(ms=ms, value=value, e2e=e2e, batched=batched, adjoint=adjoint, batch_adjoint=batch_adjoint,
+                symmetry=symmetry,
                 prof=prof, clocks=clk.summary(), launches=launches,
                 builds=builds, fallbacks=fallbacks, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
                 sysp=sysp, B=B, sim=sim)
@@ -321,14 +327,35 @@ def batched_leg(args, sampler, local_rank):
     steps = int(round(t_end / dt))
     work = sum(Ms) * steps
     t_single = timed(per_instance)
+    breakdown = profiled(sampler, batched)
     t_batch = timed(batched)
     dims = [4 * s.Z for s in systems]
     return {"value": work / t_batch, "per_instance_value": work / t_single,
             "ratio": t_single / t_batch, "unit": "sample-steps/s", "jobs": len(zks),
             "pairs": len(pairs), "orientations": len(dirs), "dims": [min(dims), max(dims)],
-            "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m,
+            "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m, "kernel_breakdown": breakdown,
             "workload": "uneven pairs (2-10 nuclei from 1H/14N, anisotropic) x Fibonacci-sphere "
                         "orientations at 0.05 mT, own Hamiltonian per job"}
+
+
+def profiled(sampler, fn):
+    """Run fn once with per-kernel-class CUDA-event timing on; returns
+    {class: {ms, launches, tflops}} (an untimed warm-up run)."""
+    import ctypes as C
+
+    from spin_dynamics_gb300 import _native as nat
+    nat.check(nat.lib().spc_set_profiling(sampler.handle, 1))
+    fn()
+    out = {}
+    for k in range(nat.SPC_KERNEL_KINDS):
+        a, n, f, b = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
+        nat.lib().spc_get_profile(sampler.handle, k, C.byref(a), C.byref(n), C.byref(f), C.byref(b))
+        if n.value:
+            out[nat.lib().spc_kernel_kind_name(k).decode()] = {
+                "ms": round(a.value, 3), "launches": n.value,
+                "tflops": round(f.value / (a.value / 1e3) / 1e12, 4) if a.value else None}
+    nat.check(nat.lib().spc_set_profiling(sampler.handle, 0))
+    return out
 
 
 def uneven_jobs(args):
@@ -397,6 +424,50 @@ def batched_adjoint_leg(args, sampler, local_rank):
                         "hyperfine element) per job"}
 
 
+def symmetry_leg(args, sampler):
+    """The symmetry-reduced large system (full dim 37,748,736 -> 243 total-spin
+    blocks of dims 36..112,500): Phi_S and dPhi_S/d(field direction) for
+    --sym-directions Fibonacci-sphere directions at 0.05 mT, every (block,
+    direction) job in one batched adjoint sweep (split only by device memory),
+    against the plain batched forward of the same blocks (Krylov reuse) for
+    the first direction. Bounded window and samples per block."""
+    import torch
+
+    from spin_dynamics_gb300 import symmetry as S
+    from spin_dynamics_gb300.dynamics import num_time_points
+    from spin_dynamics_gb300.spinsys import SimParam
+
+    sysp = W.symmetric_large_pair()
+    sim = SimParam.from_input_units(type="symmetry_dynamics", B=[0.05], init_state="singlet", seed=(42, 99),
+                                    N_samples=args.sym_samples, t_end_ns=args.sym_window_ns, dt_ns=1.0,
+                                    N_krylov=args.batch_krylov, tol=1e-5, M1=3, M2=2, block_tol=0.0)
+    dirs = W.fibonacci_sphere(args.sym_directions, 1.0)
+    bl = S.blocks(sysp, 3, 2)
+    dims = [4 * Zb for _, _, Zb in bl]
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    g, t_g = timed(lambda: S.symmetrised_yield_gradient(sysp, sim, [0, 0, 0.05], sampler=sampler,
+                                                        directions=dirs, n_quad=args.adjoint_quad))
+    _, t_p = timed(lambda: S.symmetrised_dynamics(sysp, sim, sampler=sampler, field=0.05 * dirs[0]))
+    work_g = len(bl) * args.sym_samples * len(dirs)
+    T_steps = 2 * (num_time_points(sim.dt, sim.t_end) // 2) - 2  # steps of the Simpson grid
+    return {"value": work_g * T_steps / t_g, "unit": "sample-steps/s", "seconds": t_g,
+            "plain_batched_forward_value": len(bl) * args.sym_samples * int(round(sim.t_end / sim.dt)) / t_p,
+            "blocks": len(bl), "block_dims": [min(dims), max(dims)], "sum_block_dims": int(sum(dims)),
+            "full_dim": int(4 * sysp.Z), "samples_per_block": args.sym_samples, "directions": len(dirs),
+            "dt_steps": T_steps, "krylov": args.batch_krylov,
+            "Phi_S": [d["Phi_S"] for d in g], "dPhi_S_dtheta": [d["dtheta"] for d in g],
+            "dPhi_S_dphi": [d["dphi"] for d in g],
+            "workload": "symmetry-reduced large pair (14N + 3x4 equivalent 1H | 14N + 2x4 equivalent 1H), "
+                        "compass directions at 0.05 mT, batched + adjoint"}
+
+
 def adjoint_leg(args, sampler, plain_value):
     """Yields and their gradient with respect to all 15 + 9*12 parameters of
     the large pair (spc_yield_gradient, host sample vectors in, gradient out)
@@ -427,19 +498,7 @@ def adjoint_leg(args, sampler, plain_value):
             return r, time.perf_counter() - t0
 
         # untimed first call (allocation, page-in) with per-kernel-class timing
-        import ctypes as C
-        from spin_dynamics_gb300 import _native as nat
-        nat.check(nat.lib().spc_set_profiling(sampler.handle, 1))
-        grad()
-        breakdown = {}
-        for k in range(nat.SPC_KERNEL_KINDS):
-            a, n, f, b = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
-            nat.lib().spc_get_profile(sampler.handle, k, C.byref(a), C.byref(n), C.byref(f), C.byref(b))
-            if n.value:
-                breakdown[nat.lib().spc_kernel_kind_name(k).decode()] = {
-                    "ms": round(a.value, 3), "launches": n.value,
-                    "tflops": round(f.value / (a.value / 1e3) / 1e12, 4) if a.value else None}
-        nat.check(nat.lib().spc_set_profiling(sampler.handle, 0))
+        breakdown = profiled(sampler, grad)
         g, t_grad = timed(grad)
         st = sampler.stats()
         y, t_fwd = timed(fwd)
@@ -529,7 +588,7 @@ def main():
                                    "frac": (ach_tf * 1e12 / r["fp64_peak"]) if ach_tf else None,
                                    "peak_source": "measured DFMA probe (spc_fp64_peak)"}},
                 kernel_share=share, batched=r["batched"], adjoint=r["adjoint"],
-                batched_adjoint=r["batch_adjoint"], cpu_baseline=cpu)
+                batched_adjoint=r["batch_adjoint"], symmetry=r["symmetry"], cpu_baseline=cpu)
     print(json.dumps(line))
 
 

@@ -40,19 +40,23 @@ struct ConPair {
   int64_t roff;
 };
 
-// R[a][b] += w * sum_o conj(mu_row(a,o)) nu_row(b,o) for the (tile, slot)
-// pairs [p0, p0 + gridDim.x / nch), all of slot size G; one warp per CTA,
-// lanes = samples, the `o` range split into nch chunks; the last CTA of each
-// pair adds the chunk partials in chunk order.
-template <int G>
-__global__ void __launch_bounds__(32)
+// Partial reduced matrices P[a][b] = sum_{o in chunk} conj(mu_row(a,o))
+// nu_row(b,o) for the (tile, slot) pairs [p0, p0 + cnt), all of slot size G:
+// CTA b = ((pair * nch) + chunk) * (G / RB) + row block; one warp per CTA,
+// lanes = samples; rows a of the block [rb*RB, rb*RB + RB) against all G
+// columns (RB x G accumulators keep the register footprint small enough for
+// many resident warps). k_contract_close adds the chunks in order.
+template <int G, int RB>
+__global__ void __launch_bounds__(32, (RB * G > 20 ? 8 : 16))
     k_contract(const TileInfo* __restrict__ tiles, const int* __restrict__ map,
                const int* __restrict__ scol, const GradSlot* __restrict__ slots,
                const ConPair* __restrict__ pairs, int p0, int nch, const double2* __restrict__ mu,
-               const double2* __restrict__ nu, double w, double2* __restrict__ partial,
-               unsigned* __restrict__ counters, double2* __restrict__ racc) {
+               const double2* __restrict__ nu, double2* __restrict__ partial) {
+  constexpr int NRB = G / RB;
   const int b = blockIdx.x;
-  const int pl = b / nch, ch = b % nch;
+  const int rb = b % NRB;
+  const int pc = b / NRB;
+  const int pl = pc / nch, ch = pc % nch;
   const ConPair PR = pairs[p0 + pl];
   const GradSlot S = slots[PR.js];
   const TileInfo& T = tiles[PR.t];
@@ -63,72 +67,73 @@ __global__ void __launch_bounds__(32)
   const int64_t L = S.owner == -1 ? Z : (S.owner == -2 ? 4 * Z / S.g : 2 * Z / S.g);
   const int64_t per = (L + nch - 1) / nch;
   const int64_t o0 = (int64_t)ch * per, o1 = min(L, o0 + per);
-  double2 acc[G * G];
+  double2 acc[RB * G];
 #pragma unroll
-  for (int i = 0; i < G * G; ++i) acc[i] = cz();
+  for (int i = 0; i < RB * G; ++i) acc[i] = cz();
   if (act) {
     const int64_t ld = T.ldp;
     const double2* Mu = mu + T.psi_off + scol[wslot];
     const double2* Nu = nu + T.psi_off + scol[wslot];
     const int64_t zg = S.owner == -1 ? Z : Z / S.g;
     for (int64_t o = o0; o < o1; ++o) {
-      double2 a[G], v[G];
-      if (S.owner == -1) {
-        // electron pair: o = nuclear index
-#pragma unroll
-        for (int c = 0; c < G; ++c) {
-          const int64_t row = (int64_t)c * Z + o;
-          a[c] = Mu[row * ld];
-          v[c] = Nu[row * ld];
-        }
-      } else {
-        // o = (electron state or spin of the other electron, nuclear index
-        // without nucleus j)
-        const int so = (int)(o / zg);
+      // o = nuclear index (electron pair), else (electron state or spin of
+      // the other electron, nuclear index without nucleus j)
+      int so = 0;
+      int64_t nbase = o;
+      if (S.owner != -1) {
+        so = (int)(o / zg);
         const int64_t rem = o - (int64_t)so * zg;
         const int64_t hi = rem / S.stride, lo = rem - hi * S.stride;
-        const int64_t nbase = hi * S.g * S.stride + lo;
-#pragma unroll
-        for (int c = 0; c < G; ++c) {
-          int e, mm;
-          if (S.owner == -2) {
-            e = so;
-            mm = c;
-          } else {
-            const int sk = c / (G / 2);
-            mm = c % (G / 2);
-            e = S.owner == 0 ? (sk * 2 + so) : (so * 2 + sk);
-          }
-          const int64_t row = (int64_t)e * Z + nbase + (int64_t)mm * S.stride;
-          a[c] = Mu[row * ld];
-          v[c] = Nu[row * ld];
-        }
+        nbase = hi * S.g * S.stride + lo;
       }
+      auto row_of = [&](int c) -> int64_t {
+        if (S.owner == -1) return (int64_t)c * Z + o;
+        int e, mm;
+        if (S.owner == -2) {
+          e = so;
+          mm = c;
+        } else {
+          const int sk = c / (G / 2);
+          mm = c % (G / 2);
+          e = S.owner == 0 ? (sk * 2 + so) : (so * 2 + sk);
+        }
+        return (int64_t)e * Z + nbase + (int64_t)mm * S.stride;
+      };
+      double2 a[RB], v[G];
 #pragma unroll
-      for (int i = 0; i < G; ++i)
+      for (int i = 0; i < RB; ++i) a[i] = Mu[row_of(rb * RB + i) * ld];
+#pragma unroll
+      for (int c = 0; c < G; ++c) v[c] = Nu[row_of(c) * ld];
+#pragma unroll
+      for (int i = 0; i < RB; ++i)
 #pragma unroll
         for (int j = 0; j < G; ++j) acc[i * G + j] = cjfma(a[i], v[j], acc[i * G + j]);
     }
   }
-  double2* P = partial + (size_t)b * G * G * SPC_LANES + lane;
+  // partial[(pair * nch + chunk)][entry][lane]
+  double2* P = partial + ((size_t)pc * G * G + (size_t)rb * RB * G) * SPC_LANES + lane;
 #pragma unroll
-  for (int i = 0; i < G * G; ++i) P[(size_t)i * SPC_LANES] = acc[i];
-  __threadfence();
-  __shared__ bool am_last;
-  if (lane == 0) am_last = atomicAdd(&counters[p0 + pl], 1u) == (unsigned)nch - 1;
-  __syncwarp();
-  if (!am_last) return;
-  __threadfence();
-  if (act) {
-    double2* R = racc + ((size_t)PR.roff + (size_t)lane * PR.nsl + PR.jl) * CON_MAXG * CON_MAXG;
-    const double2* base = partial + (size_t)pl * nch * G * G * SPC_LANES + lane;
-    for (int i = 0; i < G * G; ++i) {
-      double2 s = cz();
-      for (int c = 0; c < nch; ++c) s = cadd(s, __ldcg(base + ((size_t)c * G * G + i) * SPC_LANES));
-      R[i] = make_double2(fma(w, s.x, R[i].x), fma(w, s.y, R[i].y));
-    }
-  }
-  if (lane == 0) counters[p0 + pl] = 0u;
+  for (int i = 0; i < RB * G; ++i) P[(size_t)i * SPC_LANES] = acc[i];
+}
+
+// R += w * sum over chunks (in chunk order) of the partials, one thread per
+// (pair, entry, lane).
+template <int G>
+__global__ void __launch_bounds__(256)
+    k_contract_close(const int* __restrict__ map, const ConPair* __restrict__ pairs, int p0, int cnt,
+                     int nch, const double2* __restrict__ partial, double w, double2* __restrict__ racc) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)cnt * G * G * SPC_LANES) return;
+  const int lane = (int)(idx % SPC_LANES);
+  const int e = (int)((idx / SPC_LANES) % (G * G));
+  const int pl = (int)(idx / ((int64_t)SPC_LANES * G * G));
+  const ConPair PR = pairs[p0 + pl];
+  if (map[PR.t * SPC_LANES + lane] < 0) return;
+  double2 s = cz();
+  const double2* src = partial + ((size_t)pl * nch * G * G + e) * SPC_LANES + lane;
+  for (int c = 0; c < nch; ++c) s = cadd(s, src[(size_t)c * G * G * SPC_LANES]);
+  double2* R = racc + ((size_t)PR.roff + (size_t)lane * PR.nsl + PR.jl) * CON_MAXG * CON_MAXG + e;
+  *R = make_double2(fma(w, s.x, R->x), fma(w, s.y, R->y));
 }
 
 // Krylov coordinates of y = exp(-i tau A) (beta e1): beta * E[:, 0] per slot,
@@ -298,8 +303,29 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
   for (int t = 0; t < ntiles; ++t)
     pairs.push_back(ConPair{t, jobs[tile_job[t]].slot0, 0, 1, (int64_t)t * SPC_LANES});
   const int npairs = (int)pairs.size();
-  auto chunks = [&](int cnt) { return std::max(1, h->sm_count * 32 / std::max(1, cnt)); };
-  const size_t part_cap = (size_t)std::max(npairs, h->sm_count * 64) * con * SPC_LANES;
+  // chunks per pair: about two waves of one-warp CTAs over the group (row
+  // blocks included), at least 32 rows of `o` each
+  auto pair_len = [&](const ConPair& P) {
+    const GradSlot& Sl = cs[P.js];
+    const int64_t Z = tile_n[P.t] / 4;
+    return Sl.owner == -1 ? Z : (Sl.owner == -2 ? 4 * Z / Sl.g : 2 * Z / Sl.g);
+  };
+  auto nrb_of = [](int G) { return G == 6 ? 2 : 1; };
+  auto chunks_for = [&](int p0, int cnt, int G) {
+    int64_t L = 1;
+    for (int q = p0; q < p0 + cnt; ++q) L = std::max(L, pair_len(pairs[q]));
+    const int64_t by_wave = (int64_t)h->sm_count * 64 / std::max(1, cnt * nrb_of(G));
+    const int64_t by_len = (L + 31) / 32;
+    return (int)std::max<int64_t>(1, std::min(by_wave, by_len));
+  };
+  const int nch_f = chunks_for(pf0, ntiles, 4);
+  std::vector<int> grp_nch(grp_G.size());
+  size_t part_need = (size_t)ntiles * nch_f * 16 * SPC_LANES;
+  for (size_t gi = 0; gi < grp_G.size(); ++gi) {
+    grp_nch[gi] = chunks_for(grp_p0[gi], grp_cnt[gi], grp_G[gi]);
+    part_need = std::max(part_need, (size_t)grp_cnt[gi] * grp_nch[gi] * grp_G[gi] * grp_G[gi] * SPC_LANES);
+  }
+  const size_t part_cap = part_need;
 
   // checkpoint spacing K and whether a segment's node states are kept (one
   // Krylov build per step saved). K = 0 picks the largest spacing whose
@@ -528,34 +554,44 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
       con_ff += f;
   }
   // acc += w * reduced matrices of (mu, nu): forward = the electron pair only
+  auto launch_group = [&](int G, int p0, int cnt, int nc, const double2* mu, const double2* nu, double w,
+                          double2* acc) {
+    const int nb = cnt * nc * nrb_of(G);
+    switch (G) {
+      case 2:
+        k_contract<2, 2><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, d_part);
+        break;
+      case 3:
+        k_contract<3, 3><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, d_part);
+        break;
+      case 4:
+        k_contract<4, 4><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, d_part);
+        break;
+      case 5:
+        k_contract<5, 5><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, d_part);
+        break;
+      default:
+        k_contract<6, 3><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, d_part);
+        break;
+    }
+    const int64_t nt = (int64_t)cnt * G * G * SPC_LANES;
+    const int gb = (int)((nt + 255) / 256);
+    switch (G) {
+      case 2: k_contract_close<2><<<gb, 256, 0, st>>>(d_map, d_pairs, p0, cnt, nc, d_part, w, acc); break;
+      case 3: k_contract_close<3><<<gb, 256, 0, st>>>(d_map, d_pairs, p0, cnt, nc, d_part, w, acc); break;
+      case 4: k_contract_close<4><<<gb, 256, 0, st>>>(d_map, d_pairs, p0, cnt, nc, d_part, w, acc); break;
+      case 5: k_contract_close<5><<<gb, 256, 0, st>>>(d_map, d_pairs, p0, cnt, nc, d_part, w, acc); break;
+      default: k_contract_close<6><<<gb, 256, 0, st>>>(d_map, d_pairs, p0, cnt, nc, d_part, w, acc); break;
+    }
+    h->count_launch(2);
+  };
   auto contract = [&](const double2* mu, const double2* nu, double w, bool forward, double2* acc) {
     int pe = h->prof.begin(st);
     if (forward) {
-      k_contract<4><<<ntiles * chunks(ntiles), 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, pf0,
-                                                            chunks(ntiles), mu, nu, w, d_part, d_cnt, acc);
-      h->count_launch();
+      launch_group(4, pf0, ntiles, nch_f, mu, nu, w, acc);
     } else {
-      for (size_t gi = 0; gi < grp_G.size(); ++gi) {
-        const int nc = chunks(grp_cnt[gi]), nb = grp_cnt[gi] * nc, p0 = grp_p0[gi];
-        switch (grp_G[gi]) {
-          case 2:
-            k_contract<2><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
-            break;
-          case 3:
-            k_contract<3><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
-            break;
-          case 4:
-            k_contract<4><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
-            break;
-          case 5:
-            k_contract<5><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
-            break;
-          default:
-            k_contract<6><<<nb, 32, 0, st>>>(d_tf, d_map, d_scol, d_slots, d_pairs, p0, nc, mu, nu, w, d_part, d_cnt, acc);
-            break;
-        }
-        h->count_launch();
-      }
+      for (size_t gi = 0; gi < grp_G.size(); ++gi)
+        launch_group(grp_G[gi], grp_p0[gi], grp_cnt[gi], grp_nch[gi], mu, nu, w, acc);
     }
     h->prof.end(st, pe, PK_CONTRACT, forward ? con_ff : con_fg, 32.0 * elems);
   };

@@ -499,12 +499,18 @@ __global__ void __launch_bounds__(128)
 //   S  = 1/2 (Q_b2 - Q_b3)^H (Q_b2 - Q_b3),  T0 = 1/2 (Q_b2 + Q_b3)^H (Q_b2 + Q_b3)
 // with b1..b4 the Z-row blocks |aa>, |ab>, |ba>, |bb>. S and T0 are the
 // Hermitian parts of the reference's P_S, P_T0; Re(c^H P c) is unchanged.
-// Grid (slots, Z splits); 256 threads each own up to MAXC (type, i<=j).
+// Grid (slots, splits); 256 threads each own up to MAXC (type, i<=j). A
+// sample with Z nuclear rows uses min(nsplit, ceil(Z/rps)) splits of about
+// rps rows (proj_splits), so CTAs of an uneven batch carry similar work.
 #define PROJ_NC 32
+__host__ __device__ __forceinline__ int proj_splits(int nsplit, int64_t rps, int64_t Z) {
+  const int64_t c = (Z + rps - 1) / rps;
+  return (int)(c < 1 ? 1 : (c > nsplit ? nsplit : c));
+}
 template <int MAXC>
 __global__ void __launch_bounds__(256)
     k_proj(const TileInfo* __restrict__ tiles, const int* __restrict__ map, int m, int ncombo,
-           const unsigned* __restrict__ combos, const double2* __restrict__ Q, int nsplit,
+           const unsigned* __restrict__ combos, const double2* __restrict__ Q, int nsplit, int64_t rps,
            double2* __restrict__ part) {
   extern __shared__ double2 V[];  // [4][m][PROJ_NC]
   const int w = blockIdx.x;
@@ -515,7 +521,9 @@ __global__ void __launch_bounds__(256)
   const int split = blockIdx.y;
   const int tid = threadIdx.x;
   const int64_t Z = Ti.n / 4;
-  const int64_t per = (Z + nsplit - 1) / nsplit;
+  const int nsp = proj_splits(nsplit, rps, Z);
+  if (split >= nsp) return;
+  const int64_t per = (Z + nsp - 1) / nsp;
   const int64_t n0 = (int64_t)split * per;
   const int64_t n1 = min(Z, n0 + per);
   double2 acc[MAXC];
@@ -555,7 +563,7 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
 #pragma unroll 4
-    for (int nn = 0; nn < PROJ_NC; ++nn) {
+    for (int nn = 0; nn < len; ++nn) {
 #pragma unroll
       for (int q = 0; q < MAXC; ++q)
         if (tid + q * 256 < ncombo) acc[q] = cjfma(V[oi[q] + nn], V[oj[q] + nn], acc[q]);
@@ -570,15 +578,16 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void k_proj_reduce(int nslots, const int* __restrict__ map, int m, int ncombo,
-                              int nsplit, const unsigned* __restrict__ combos,
+__global__ void k_proj_reduce(const TileInfo* __restrict__ tiles, int nslots, const int* __restrict__ map,
+                              int m, int ncombo, int nsplit, int64_t rps, const unsigned* __restrict__ combos,
                               const double2* __restrict__ part, double2* __restrict__ proj) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (int64_t)nslots * ncombo) return;
   const int w = (int)(idx / ncombo), cid = (int)(idx % ncombo);
   if (map[w] < 0) return;
+  const int nsp = proj_splits(nsplit, rps, tiles[w / SPC_LANES].n / 4);
   double2 s = cz();
-  for (int sp = 0; sp < nsplit; ++sp) s = cadd(s, part[((size_t)sp * nslots + w) * ncombo + cid]);
+  for (int sp = 0; sp < nsp; ++sp) s = cadd(s, part[((size_t)sp * nslots + w) * ncombo + cid]);
   const unsigned cb = combos[cid];
   const int t = cb >> 16, i = (cb >> 8) & 255, j = cb & 255;
   if (t == 1 || t == 2) s = make_double2(0.5 * s.x, 0.5 * s.y);
@@ -1113,34 +1122,50 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, d_tiles, d_map, d_A, d_E, dt, d_err);
     h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * list.size(),
                 32.0 * (double)mm * list.size());
-    // projector split: the count in [1, nsplit_max] whose grid wastes the
-    // least of its last wave
+    // projector splits: rows per split `rps` minimising the estimated time
+    // (all rows plus a per-CTA overhead of 32 rows, over the resident CTAs,
+    // plus the longest CTA); each sample takes ceil(Z/rps) splits, at most
+    // nsplit_max
     int ns = 1;
+    int64_t rps = 1;
     {
-      double best = 1e30;
+      int64_t zmax = 1;
+      std::vector<int64_t> zact;  // Z of every active slot
+      for (int t = 0; t < ntiles; ++t)
+        for (int l = 0; l < SPC_LANES; ++l)
+          if (map[t * SPC_LANES + l] >= 0) zact.push_back(tiles[t].n / 4);
+      for (int64_t z : zact) zmax = std::max(zmax, z);
+      double best = 1e300;
       for (int c = 1; c <= nsplit_max; ++c) {
-        const double waves = (double)list.size() * c / res_proj;
-        const double loss = std::ceil(waves) / waves - 1.0 + 0.002 * c;
-        if (loss < best) {
-          best = loss;
-          ns = c;
+        const int64_t r = (zmax + c - 1) / c;
+        double rows = 0.0, ctas = 0.0;
+        for (int64_t z : zact) {
+          const int k = proj_splits(nsplit_max, r, z);
+          ctas += k;
+          rows += (double)z;
+        }
+        const double est = (rows + 32.0 * ctas) / res_proj + (double)r;
+        if (est < best) {
+          best = est;
+          rps = r;
         }
       }
+      for (int64_t z : zact) ns = std::max(ns, proj_splits(nsplit_max, rps, z));
     }
     const dim3 pgrid(nslots, ns);
     pe = h->prof.begin(st);
     if (maxc <= 8)
-      k_proj<8><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, d_ppart);
+      k_proj<8><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, rps, d_ppart);
     else if (maxc <= 16)
-      k_proj<16><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, d_ppart);
+      k_proj<16><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, rps, d_ppart);
     else
-      k_proj<24><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, d_ppart);
+      k_proj<24><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, rps, d_ppart);
     h->prof.end(st, pe, PK_PROJ, 8.0 * (double)ncombo * zsum + 4.0 * (double)m * zsum,
                 64.0 * (double)m * zsum);
     {
       const int64_t tot = (int64_t)nslots * ncombo;
       pe = h->prof.begin(st);
-      k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(nslots, d_map, m, ncombo, ns, d_combos,
+      k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(d_tiles, nslots, d_map, m, ncombo, ns, rps, d_combos,
                                                              d_ppart, d_proj);
       h->prof.end(st, pe, PK_PROJ_REDUCE, 2.0 * tot * ns, 16.0 * tot * (ns + 1));
       h->count_launch(3);

@@ -270,6 +270,11 @@ def _chunks(rows_x_samples, budget_entries):
     return groups
 
 
+def _padded(M: int) -> int:
+    """Sample columns a job occupies on the device (tiles of 32)."""
+    return (M + 31) // 32 * 32
+
+
 def _budget_entries(states_per_entry: float) -> float:
     """Vector entries (rows x samples) a batch may hold: a third of the free
     device memory over `states_per_entry` complex states per entry."""
@@ -282,24 +287,29 @@ def _budget_entries(states_per_entry: float) -> float:
 
 
 def symmetrised_dynamics(sys_: SysParam, sim: SimParam, out: Optional[str] = None, sampler=None,
-                         exact_blocks: bool = False) -> Observables:
+                         exact_blocks: bool = False, field=None) -> Observables:
     """symmetrised_dynamics (src/symmetry.f90:16-139): trace sampling over
     every block whose weight reaches sim.block_tol (sim.N_samples vectors per
     block, seeds drawn per block from sim.seed), each scaled by its weight,
     summed in block order, then yields (get_kinetics) and the output files.
     The blocks propagate together through the batch API (groups bounded by
     device memory). With exact_blocks=True every block is traced exactly over
-    its basis states."""
+    its basis states. field (a 3-vector, mT) switches to the general
+    Hamiltonian (anisotropic explicit nuclei, tilted field); by default the
+    reference's builder with the field -w along z."""
     from . import dynamics
     sp = sampler or dynamics.default_sampler()
     sel = _selected(sys_, sim)
     zks = _block_vectors(sel, sim, exact_blocks)
     T = dynamics.num_time_points(sim.dt, sim.t_end)
     res = Observables.zeros(T)
-    sizes = [4 * Zb * z.shape[0] for (_, _, _, Zb, _), z in zip(sel, zks)]
+    sizes = [4 * Zb * _padded(z.shape[0]) for (_, _, _, Zb, _), z in zip(sel, zks)]
     for grp in _chunks(sizes, _budget_entries(sim.N_krylov + 4)):
         systems = [sel[j][2] for j in grp]
-        sp.build_h_batch(systems, [-s.e1.w for s in systems], "reference")
+        if field is None:
+            sp.build_h_batch(systems, [-s.e1.w for s in systems], "reference")
+        else:
+            sp.build_h_batch(systems, [np.asarray(field, float)] * len(systems), "general")
         rs = sp.trace_sampling_batch([zks[j] for j in grp], sim.dt, sim.t_end, sim.N_krylov, sim.tol,
                                      sim.init_state)
         for j, r in zip(grp, rs):
@@ -335,7 +345,7 @@ def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, d
     jobs = [(f, j) for f in range(len(fields)) for j in range(len(sel))]
     acc = [dict(Phi_S=0.0, Phi_T=0.0, B=np.zeros(3), J=0.0, D=np.zeros((3, 3)), kS=0.0, kT=0.0)
            for _ in fields]
-    sizes = [4 * sel[j][3] * zks[j].shape[0] for _, j in jobs]
+    sizes = [4 * sel[j][3] * _padded(zks[j].shape[0]) for _, j in jobs]
     # states per vector entry held by the sweep: basis, checkpoints, segment, node states
     for grp in _chunks(sizes, _budget_entries(sim.N_krylov + 6 + 8 * (n_quad + 1))):
         systems = [sel[jobs[q][1]][2] for q in grp]

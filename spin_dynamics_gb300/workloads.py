@@ -114,6 +114,25 @@ def uneven_pairs(n_pairs: int = 256, seed: int = 3) -> list:
     return out
 
 
+def symmetric_large_pair(seed: int = 5) -> SysParam:
+    """The symmetry-reduced large system: radical A = one 14N + 12 equivalent
+    1H in 3 groups of 4 (one isotropic coupling per group, uniform in
+    [0.2, 0.8] mT), radical B = one 14N + 8 1H in 2 groups of 4; full Hilbert
+    dimension 4*3^2*2^20 = 37,748,736. The 14N tensors are anisotropic
+    (principal values uniform in [-2, 2] mT, Haar rotation) so the yield
+    depends on the field direction; J = 0.01 mT, D = -0.4 mT axial,
+    kS = kT = 1/us. The decomposition into total-spin blocks of the groups is
+    exact (symmetry.blocks with M1 = 3, M2 = 2): 243 blocks."""
+    rng = np.random.default_rng(seed)
+    a1 = rng.uniform(0.2, 0.8, 3)
+    a2 = rng.uniform(0.2, 0.8, 2)
+    N1 = _tensors(rng, 1, -2.0, 2.0, True)
+    N2 = _tensors(rng, 1, -2.0, 2.0, True)
+    e1 = Electron(g_I=[2] * 12 + [3], A=[np.eye(3) * a for a in np.repeat(a1, 4)] + N1)
+    e2 = Electron(g_I=[2] * 8 + [3], A=[np.eye(3) * a for a in np.repeat(a2, 4)] + N2)
+    return SysParam.from_input_units(e1, e2, J=0.01, D=axial_dipolar(-0.4), kS_per_us=1.0, kT_per_us=1.0)
+
+
 def random_phase_samples(Z: int, M: int, seed: int = 7) -> np.ndarray:
     """M normalised random-phase vectors e^{i phi}/sqrt(Z), phi ~ U[0, 2 pi)."""
     rng = np.random.default_rng(seed)
@@ -133,5 +152,5 @@ def large_sim(M: int = 512, t_end_ns: float = 2000.0) -> SimParam:
                                      N_krylov=30, tol=1e-5)
 
 
-__all__ = ["small_pair", "large_pair", "notebook_pair", "random_phase_samples", "small_sim",
+__all__ = ["small_pair", "large_pair", "notebook_pair", "symmetric_large_pair", "uneven_pairs", "random_phase_samples", "small_sim",
            "large_sim", "axial_dipolar", "GAMMA_1H", "GAMMA_14N"]
