@@ -499,7 +499,10 @@ __global__ void __launch_bounds__(128)
 //   S  = 1/2 (Q_b2 - Q_b3)^H (Q_b2 - Q_b3),  T0 = 1/2 (Q_b2 + Q_b3)^H (Q_b2 + Q_b3)
 // with b1..b4 the Z-row blocks |aa>, |ab>, |ba>, |bb>. S and T0 are the
 // Hermitian parts of the reference's P_S, P_T0; Re(c^H P c) is unchanged.
-// Grid (slots, splits); 256 threads each own up to MAXC (type, i<=j). A
+// Grid (slots, splits); each of the CTA's threads owns MAXC (type, i<=j)
+// combinations, MAXC = ceil(ncombo / 256) exactly and the block trimmed to
+// ceil(ncombo / MAXC) threads: combination slots that no thread needs would
+// still issue their (predicated-off) DFMAs and hold the FP64 pipe. A
 // sample with Z nuclear rows uses min(nsplit, ceil(Z/rps)) splits of about
 // rps rows (proj_splits), so CTAs of an uneven batch carry similar work.
 #define PROJ_NC 32
@@ -519,7 +522,7 @@ __global__ void __launch_bounds__(256)
   const int me = Ti.m;
   const int lane = w % SPC_LANES;
   const int split = blockIdx.y;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, nth = blockDim.x;
   const int64_t Z = Ti.n / 4;
   const int nsp = proj_splits(nsplit, rps, Z);
   if (split >= nsp) return;
@@ -531,7 +534,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int q = 0; q < MAXC; ++q) {
     acc[q] = cz();
-    const int cid = tid + q * 256;
+    const int cid = tid + q * nth;
     if (cid < ncombo) {
       const unsigned cb = combos[cid];
       const int t = cb >> 16, i = (cb >> 8) & 255, j = cb & 255;
@@ -545,7 +548,7 @@ __global__ void __launch_bounds__(256)
   const double2* Qt = Q + Ti.q_off + lane;
   for (int64_t c0 = n0; c0 < n1; c0 += PROJ_NC) {
     const int len = (int)min((int64_t)PROJ_NC, n1 - c0);
-    for (int idx = tid; idx < m * PROJ_NC; idx += 256) {
+    for (int idx = tid; idx < m * PROJ_NC; idx += nth) {
       const int j = idx / PROJ_NC, nn = idx % PROJ_NC;
       double2 q1 = cz(), q2 = cz(), q3 = cz(), q4 = cz();
       if (nn < len && j < me) {
@@ -566,14 +569,14 @@ __global__ void __launch_bounds__(256)
     for (int nn = 0; nn < len; ++nn) {
 #pragma unroll
       for (int q = 0; q < MAXC; ++q)
-        if (tid + q * 256 < ncombo) acc[q] = cjfma(V[oi[q] + nn], V[oj[q] + nn], acc[q]);
+        if (tid + q * nth < ncombo) acc[q] = cjfma(V[oi[q] + nn], V[oj[q] + nn], acc[q]);
     }
     __syncthreads();
   }
   double2* out = part + ((size_t)split * gridDim.x + w) * ncombo;
 #pragma unroll
   for (int q = 0; q < MAXC; ++q) {
-    const int cid = tid + q * 256;
+    const int cid = tid + q * nth;
     if (cid < ncombo) out[cid] = acc[q];
   }
 }
@@ -941,9 +944,32 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   const size_t expm_smem = sizeof(double2) * 5 * mm;
   const size_t proj_smem = sizeof(double2) * 4 * m * PROJ_NC;
   CK(cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expm_smem));
-  const int maxc = (ncombo + 255) / 256;
-  const void* proj_fn = maxc <= 8 ? (const void*)k_proj<8> : maxc <= 16 ? (const void*)k_proj<16>
-                                                                         : (const void*)k_proj<24>;
+  // combinations per thread (instantiated counts) and threads per CTA
+  const int maxc_need = (ncombo + 255) / 256;
+  static const int kProjMaxc[] = {1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 16, 20, 24};
+  int maxc = 24;
+  for (int c : kProjMaxc)
+    if (c >= maxc_need) {
+      maxc = c;
+      break;
+    }
+  const int proj_threads = std::min(256, ((ncombo + maxc - 1) / maxc + 31) / 32 * 32);
+  const void* proj_fn = nullptr;
+  switch (maxc) {
+    case 1: proj_fn = (const void*)k_proj<1>; break;
+    case 2: proj_fn = (const void*)k_proj<2>; break;
+    case 3: proj_fn = (const void*)k_proj<3>; break;
+    case 4: proj_fn = (const void*)k_proj<4>; break;
+    case 5: proj_fn = (const void*)k_proj<5>; break;
+    case 6: proj_fn = (const void*)k_proj<6>; break;
+    case 7: proj_fn = (const void*)k_proj<7>; break;
+    case 8: proj_fn = (const void*)k_proj<8>; break;
+    case 10: proj_fn = (const void*)k_proj<10>; break;
+    case 12: proj_fn = (const void*)k_proj<12>; break;
+    case 16: proj_fn = (const void*)k_proj<16>; break;
+    case 20: proj_fn = (const void*)k_proj<20>; break;
+    default: proj_fn = (const void*)k_proj<24>; break;
+  }
   CK(cudaFuncSetAttribute(proj_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)proj_smem));
   // resident CTAs per kernel: item lists are sized to whole waves
   auto resident = [&](const void* fn, int threads, size_t smem) {
@@ -954,7 +980,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   const int res_spmm = resident((const void*)k_spmm, 256, 0);
   const int res_pass = std::min(resident((const void*)k_rowpass<PASS_AXPY_DOT>, 256, 0),
                                 resident((const void*)k_rowpass<PASS_AXPY_NORM>, 256, 0));
-  const int res_proj = resident(proj_fn, 256, proj_smem);
+  const int res_proj = resident(proj_fn, proj_threads, proj_smem);
 
   std::vector<int> active;
   if (0.0 < t_end)
@@ -1154,12 +1180,11 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     }
     const dim3 pgrid(nslots, ns);
     pe = h->prof.begin(st);
-    if (maxc <= 8)
-      k_proj<8><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, rps, d_ppart);
-    else if (maxc <= 16)
-      k_proj<16><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, rps, d_ppart);
-    else
-      k_proj<24><<<pgrid, 256, proj_smem, st>>>(d_tiles, d_map, m, ncombo, d_combos, d_Q, ns, rps, d_ppart);
+    {
+      void* args[] = {(void*)&d_tiles, (void*)&d_map, (void*)&m, (void*)&ncombo, (void*)&d_combos,
+                      (void*)&d_Q, (void*)&ns, (void*)&rps, (void*)&d_ppart};
+      CK(cudaLaunchKernel(proj_fn, pgrid, dim3(proj_threads), args, proj_smem, st));
+    }
     h->prof.end(st, pe, PK_PROJ, 8.0 * (double)ncombo * zsum + 4.0 * (double)m * zsum,
                 64.0 * (double)m * zsum);
     {
