@@ -188,7 +188,9 @@ int spc_trace_sampling_device(spc_handle* h, const double* theta, const double* 
  * handle as a batch; system k is addressed by index k below. Replaces the
  * per-block / per-field calls of getHiso_sp in symmetrised_dynamics
  * (src/symmetry.f90:102-110) and the field loop of app/main.f90:48-79 with
- * one device-resident set. The handle's single Hamiltonian is overwritten. */
+ * one device-resident set. All systems are built with two synchronisations
+ * in total. The handle's single Hamiltonian is unset (spc_build_h or
+ * spc_set_h sets it again). */
 int spc_build_h_batch(spc_handle* h, int n_sys, const spc_system* systems, int mode);
 
 /* Trace-sample n_jobs jobs together: job k propagates M[k] caller-supplied
@@ -244,7 +246,7 @@ int spc_yield_gradient_size(const spc_system* sys);
  * 16 * n * ceil(M/32)*32 bytes, or (m + 6 + n_steps/K + K + n_quad) when that
  * does not fit (node states rebuilt per step); SPC_ERR_ALLOC when neither
  * fits. Nuclei of multiplicity above 3 return SPC_ERR_UNSUPPORTED. The
- * handle's Hamiltonian and batch are replaced by H and H^H. Cost: three
+ * handle's batch is replaced by H and H^H (its single Hamiltonian unset). Cost: three
  * Krylov builds per sample and step (four when node states are rebuilt);
  * spc_get_stats reports rounds = 1 when node states were kept. */
 int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta,
@@ -262,7 +264,7 @@ int spc_yield_gradient(spc_handle* h, const spc_system* sys, const double* theta
  * to back. yields: n_jobs x (Phi_S, Phi_T); grad (NULL: yields only): the
  * jobs' spc_yield_gradient_size(systems[k]) blocks back to back. Every build,
  * contraction and costate step of all jobs shares one set of launches. The
- * handle's Hamiltonian and batch are replaced by H_k and H_k^H. */
+ * handle's batch is replaced by H_k and H_k^H (its single Hamiltonian unset). */
 int spc_yield_gradient_batch(spc_handle* h, int n_jobs, const spc_system* systems, const int* M,
                              const double* theta, const double* zkets, double dt, double t_end, int m,
                              int n_quad, int checkpoint_every, double wS, double wT, int which,

@@ -255,45 +255,12 @@ int spc_trace_sampling(spc_handle* h, const double* theta, const double* init_po
 int spc_build_h_batch(spc_handle* h, int n_sys, const spc_system* systems, int mode) {
   if (!h || n_sys < 1 || !systems) return spc::set_error(SPC_ERR_ARG, "spc_build_h_batch: bad argument");
   CKR(cudaSetDevice(h->h.device));
-  spc::Handle& H = h->h;
   std::vector<spc::HostSystem> hs(n_sys);
-  auto& B = H.hb;
-  B.n.assign(n_sys, 0);
-  B.nnz.assign(n_sys, 0);
-  B.rp_off.assign(n_sys, 0);
-  B.nz_off.assign(n_sys, 0);
-  B.herm.assign(n_sys, 0);
-  int64_t rp_tot = 0, nz_tot = 0;
   for (int k = 0; k < n_sys; ++k) {
     int rc = spc::make_host_system(&systems[k], mode, hs[k]);
     if (rc != SPC_OK) return rc;
-    B.n[k] = (int)hs[k].N;
-    B.nnz[k] = spc::predict_nnz(hs[k], mode);
-    B.rp_off[k] = rp_tot;
-    B.nz_off[k] = nz_tot;
-    B.herm[k] = hs[k].herm_shift;
-    rp_tot += hs[k].N + 1;
-    nz_tot += B.nnz[k];
   }
-  if (H.ensure(B.rowptr, sizeof(int) * rp_tot) || H.ensure(B.split, sizeof(int) * rp_tot) ||
-      H.ensure(B.col, sizeof(int) * nz_tot) || H.ensure(B.val, sizeof(double2) * nz_tot))
-    return SPC_ERR_ALLOC;
-  for (int k = 0; k < n_sys; ++k) {
-    int rc = spc::build_h_device(&H, hs[k], mode);
-    if (rc != SPC_OK) return rc;
-    if (H.nnz != B.nnz[k]) return spc::set_error(SPC_ERR_STATE, "internal: nonzero count mismatch");
-    cudaStream_t st = H.stream;
-    CKR(cudaMemcpyAsync((int*)B.rowptr.p + B.rp_off[k], H.d_rowptr, sizeof(int) * (B.n[k] + 1),
-                        cudaMemcpyDeviceToDevice, st));
-    CKR(cudaMemcpyAsync((int*)B.split.p + B.rp_off[k], H.xsplit.p, sizeof(int) * B.n[k],
-                        cudaMemcpyDeviceToDevice, st));
-    CKR(cudaMemcpyAsync((int*)B.col.p + B.nz_off[k], H.xcol.p, sizeof(int) * B.nnz[k],
-                        cudaMemcpyDeviceToDevice, st));
-    CKR(cudaMemcpyAsync((double2*)B.val.p + B.nz_off[k], H.xval.p, sizeof(double2) * B.nnz[k],
-                        cudaMemcpyDeviceToDevice, st));
-  }
-  CKR(cudaStreamSynchronize(H.stream));
-  return SPC_OK;
+  return spc::build_h_batch_device(&h->h, hs, mode);
 }
 
 static int batch_jobs(spc_handle* h, int n_jobs, const int* job_sys, const int* M,

@@ -262,59 +262,154 @@ __global__ void k_scan_rows(const int* __restrict__ cnt, int* __restrict__ rowpt
 }
 
 // ---------------------------------------------------------------------------
-int build_h_device(Handle* h, const HostSystem& hs, int mode) {
-  const int64_t N = hs.N, Z = hs.Z;
-  int nn = (int)hs.nuc.size();
-  NucInfo* d_nuc = nullptr;
-  int* d_cnt = nullptr;
-  long long* d_total = nullptr;
+// Builds of one or many systems into caller-placed CSR slices, in two phases
+// with one synchronisation each: count + scan for every system, a check of
+// every nonzero count against its closed form (so the fill never writes past
+// the space reserved for it), then fill + row split for every system.
+struct BuildSlice {
+  const HostSystem* hs;
+  const NucInfo* nuc;   // device nucleus table
+  int* cnt;             // N per-row counts (scratch)
+  int* rowptr;          // N + 1
+  int* col;             // fill target (nnz)
+  double2* val;
+  int* xcol;            // execution-order copy for k_spmm (nnz)
+  double2* xval;
+  int* split;           // N
+  long long* total;     // 1
+};
+
+static int build_slices(Handle* h, std::vector<BuildSlice>& sl, const std::vector<int64_t>& predicted,
+                        int mode) {
   cudaStream_t st = h->stream;
-  int rc = SPC_OK;
-  if (cudaMalloc(&d_nuc, sizeof(NucInfo) * (nn > 0 ? nn : 1)) != cudaSuccess ||
-      cudaMalloc(&d_cnt, sizeof(int) * N) != cudaSuccess ||
-      cudaMalloc(&d_total, sizeof(long long)) != cudaSuccess) {
-    cudaFree(d_nuc);
-    cudaFree(d_cnt);
-    cudaFree(d_total);
-    return set_error(SPC_ERR_ALLOC, "device allocation for the Hamiltonian build failed");
-  }
-  if (nn > 0) cudaMemcpyAsync(d_nuc, hs.nuc.data(), sizeof(NucInfo) * nn, cudaMemcpyHostToDevice, st);
-  int threads = 256;
-  int blocks = (int)((N + threads - 1) / threads);
-  if (mode == SPC_H_REFERENCE)
-    k_ref_count<<<blocks, threads, 0, st>>>(N, Z, nn, d_nuc, d_cnt);
-  else
-    k_gen_count<<<blocks, threads, 0, st>>>(N, Z, nn, d_nuc, d_cnt);
-  h->ensure_rowptr(N + 1);
-  k_scan_rows<<<1, 1024, 0, st>>>(d_cnt, h->d_rowptr, N, d_total);
-  long long nnz = 0;
-  cudaMemcpyAsync(&nnz, d_total, sizeof(long long), cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) {
-    rc = set_error(SPC_ERR_CUDA, "Hamiltonian count/scan failed: %s",
-                   cudaGetErrorString(cudaGetLastError()));
-  } else if (nnz > INT32_MAX) {
-    rc = set_error(SPC_ERR_ARG, "Hamiltonian has %lld nonzeros, above the int32 CSR limit", nnz);
-  } else if (h->ensure_h_entries(nnz) != SPC_OK) {
-    rc = SPC_ERR_ALLOC;
-  } else {
+  const int threads = 256;
+  for (const BuildSlice& b : sl) {
+    const int64_t N = b.hs->N, Z = b.hs->Z;
+    const int nn = (int)b.hs->nuc.size();
+    const int blocks = (int)((N + threads - 1) / threads);
     if (mode == SPC_H_REFERENCE)
-      k_ref_fill<<<blocks, threads, 0, st>>>(N, Z, nn, d_nuc, hs.ref, h->d_rowptr, h->d_col,
-                                              h->d_val);
+      k_ref_count<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.cnt);
     else
-      k_gen_fill<<<blocks, threads, 0, st>>>(N, Z, nn, d_nuc, hs.gen, h->d_rowptr, h->d_col,
-                                              h->d_val);
-    h->count_launch(4);
-    if (cudaStreamSynchronize(st) != cudaSuccess)
-      rc = set_error(SPC_ERR_CUDA, "Hamiltonian fill failed: %s",
-                     cudaGetErrorString(cudaGetLastError()));
-    h->n = (int)N;
-    h->nnz = nnz;
-    h->herm_shift = hs.herm_shift;
-    if (rc == SPC_OK) rc = prepare_spmm_rows(h);
+      k_gen_count<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.cnt);
+    k_scan_rows<<<1, 1024, 0, st>>>(b.cnt, b.rowptr, N, b.total);
+    h->count_launch(2);
   }
-  cudaFree(d_nuc);
-  cudaFree(d_cnt);
-  cudaFree(d_total);
+  std::vector<long long> tot(sl.size());
+  if (!sl.empty()) {
+    // totals sit back to back (one slot per system)
+    if (cudaMemcpyAsync(tot.data(), sl[0].total, sizeof(long long) * sl.size(), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return set_error(SPC_ERR_CUDA, "Hamiltonian count/scan failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  for (size_t k = 0; k < sl.size(); ++k)
+    if (tot[k] != predicted[k])
+      return set_error(SPC_ERR_STATE, "internal: system %zu has %lld nonzeros, %lld predicted", k, tot[k],
+                       (long long)predicted[k]);
+  for (const BuildSlice& b : sl) {
+    const int64_t N = b.hs->N, Z = b.hs->Z;
+    const int nn = (int)b.hs->nuc.size();
+    const int blocks = (int)((N + threads - 1) / threads);
+    if (mode == SPC_H_REFERENCE)
+      k_ref_fill<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->ref, b.rowptr, b.col, b.val);
+    else
+      k_gen_fill<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->gen, b.rowptr, b.col, b.val);
+    enqueue_split_rows(N, b.rowptr, b.col, b.val, b.xcol, b.xval, b.split, st);
+    h->count_launch(2);
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess)
+    return set_error(SPC_ERR_CUDA, "Hamiltonian fill failed: %s", cudaGetErrorString(cudaGetLastError()));
+  return SPC_OK;
+}
+
+// Nucleus tables of the systems back to back on the device (scratch in h).
+static int upload_nuclei(Handle* h, const std::vector<const HostSystem*>& hs, std::vector<size_t>& off) {
+  std::vector<NucInfo> all;
+  off.resize(hs.size());
+  for (size_t k = 0; k < hs.size(); ++k) {
+    off[k] = all.size();
+    all.insert(all.end(), hs[k]->nuc.begin(), hs[k]->nuc.end());
+  }
+  if (h->ensure(h->bnuc, sizeof(NucInfo) * std::max<size_t>(1, all.size()))) return SPC_ERR_ALLOC;
+  if (!all.empty() &&
+      cudaMemcpyAsync(h->bnuc.p, all.data(), sizeof(NucInfo) * all.size(), cudaMemcpyHostToDevice, h->stream) !=
+          cudaSuccess)
+    return set_error(SPC_ERR_CUDA, "nucleus table upload failed");
+  return SPC_OK;
+}
+
+int build_h_device(Handle* h, const HostSystem& hs, int mode) {
+  const int64_t N = hs.N;
+  const int64_t nnz = predict_nnz(hs, mode);
+  if (nnz > INT32_MAX)
+    return set_error(SPC_ERR_ARG, "Hamiltonian has %lld nonzeros, above the int32 CSR limit", (long long)nnz);
+  std::vector<size_t> noff;
+  int rc = upload_nuclei(h, {&hs}, noff);
+  if (rc) return rc;
+  if (h->ensure_rowptr(N + 1) || h->ensure_h_entries(nnz) || h->ensure(h->bcnt, sizeof(int) * N) ||
+      h->ensure(h->btot, sizeof(long long)) || h->ensure(h->xcol, sizeof(int) * std::max<int64_t>(nnz, 1)) ||
+      h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nnz, 1)) || h->ensure(h->xsplit, sizeof(int) * N))
+    return SPC_ERR_ALLOC;
+  std::vector<BuildSlice> sl(1);
+  sl[0] = BuildSlice{&hs, (const NucInfo*)h->bnuc.p, (int*)h->bcnt.p, h->d_rowptr, h->d_col, h->d_val,
+                     (int*)h->xcol.p, (double2*)h->xval.p, (int*)h->xsplit.p, (long long*)h->btot.p};
+  rc = build_slices(h, sl, {nnz}, mode);
+  if (rc) return rc;
+  h->n = (int)N;
+  h->nnz = nnz;
+  h->herm_shift = hs.herm_shift;
+  return SPC_OK;
+}
+
+int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode) {
+  auto& B = h->hb;
+  const size_t ns = hs.size();
+  B.n.assign(ns, 0);
+  B.nnz.assign(ns, 0);
+  B.rp_off.assign(ns, 0);
+  B.nz_off.assign(ns, 0);
+  B.herm.assign(ns, 0);
+  int64_t rp_tot = 0, nz_tot = 0, n_tot = 0;
+  std::vector<const HostSystem*> ptrs(ns);
+  for (size_t k = 0; k < ns; ++k) {
+    ptrs[k] = &hs[k];
+    B.n[k] = (int)hs[k].N;
+    B.nnz[k] = predict_nnz(hs[k], mode);
+    if (B.nnz[k] > INT32_MAX)
+      return set_error(SPC_ERR_ARG, "system %zu has %lld nonzeros, above the int32 CSR limit", k,
+                       (long long)B.nnz[k]);
+    B.rp_off[k] = rp_tot;
+    B.nz_off[k] = nz_tot;
+    B.herm[k] = hs[k].herm_shift;
+    rp_tot += hs[k].N + 1;
+    nz_tot += B.nnz[k];
+    n_tot += hs[k].N;
+  }
+  std::vector<size_t> noff;
+  int rc = upload_nuclei(h, ptrs, noff);
+  if (rc) return rc;
+  // fill into the unsplit scratch (xcol/xval), split into the store
+  if (h->ensure(B.rowptr, sizeof(int) * rp_tot) || h->ensure(B.split, sizeof(int) * rp_tot) ||
+      h->ensure(B.col, sizeof(int) * std::max<int64_t>(nz_tot, 1)) ||
+      h->ensure(B.val, sizeof(double2) * std::max<int64_t>(nz_tot, 1)) ||
+      h->ensure(h->xcol, sizeof(int) * std::max<int64_t>(nz_tot, 1)) ||
+      h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nz_tot, 1)) ||
+      h->ensure(h->bcnt, sizeof(int) * std::max<int64_t>(n_tot, 1)) || h->ensure(h->btot, sizeof(long long) * ns))
+    return SPC_ERR_ALLOC;
+  std::vector<BuildSlice> sl(ns);
+  int64_t coff = 0;
+  for (size_t k = 0; k < ns; ++k) {
+    sl[k] = BuildSlice{&hs[k], (const NucInfo*)h->bnuc.p + noff[k], (int*)h->bcnt.p + coff,
+                       (int*)B.rowptr.p + B.rp_off[k], (int*)h->xcol.p + B.nz_off[k],
+                       (double2*)h->xval.p + B.nz_off[k], (int*)B.col.p + B.nz_off[k],
+                       (double2*)B.val.p + B.nz_off[k], (int*)B.split.p + B.rp_off[k],
+                       (long long*)h->btot.p + k};
+    coff += hs[k].N;
+  }
+  rc = build_slices(h, sl, B.nnz, mode);
+  // the single-Hamiltonian execution copy (xcol/xval) served as scratch
+  h->n = 0;
+  h->nnz = 0;
   return rc;
 }
 

@@ -68,7 +68,7 @@ Handle::~Handle() {
   Buf* all[] = {&psi, &Q,  &P,    &partial, &counters, &coef, &rbeta, &Ahess, &Aexp, &proj, &projpart,
                 &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag, &xcol, &xval, &xsplit, &plan, &jobtab,
                 &hb.rowptr, &hb.split, &hb.col, &hb.val, &gck, &gseg, &gnu, &gmu, &glam, &cvec2,
-                &gslots, &gracc, &gfacc};
+                &gslots, &gracc, &gfacc, &bcnt, &bnuc, &btot};
   for (Buf* b : all)
     if (b->p) cudaFree(b->p);
   if (d_rowptr) cudaFree(d_rowptr);

@@ -105,6 +105,8 @@ struct Handle {
   };
   Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
       map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit, plan, jobtab;
+  // Hamiltonian build scratch: row counts, nucleus tables, nonzero totals
+  Buf bcnt, bnuc, btot;
   // yield-gradient workspace: checkpoints, segment states, node states,
   // costate pair, second coordinate vector, slot table, accumulators
   Buf gck, gseg, gnu, gmu, glam, cvec2, gslots, gracc, gfacc;
@@ -174,6 +176,12 @@ struct GradJob {
 
 int set_error(int code, const char* fmt, ...);
 int build_h_device(Handle* h, const HostSystem& hs, int mode);
+// Every system into the batch store (h->hb) with two synchronisations in all;
+// the handle's single Hamiltonian is left unset.
+int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode);
+// Row split of a CSR for k_spmm (complex entries first), enqueued on st.
+void enqueue_split_rows(int64_t N, const int* rowptr, const int* col, const double2* val, int* xcol,
+                        double2* xval, int* split, cudaStream_t st);
 int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev,
               int M, double dt, double t_end, int m, double tol, double* out_dev, int T);
 int propagate_batch(Handle* h, const double* theta, const double* init_pop,

@@ -309,6 +309,11 @@ __global__ void k_split_rows(int64_t N, const int* __restrict__ rowptr, const in
     }
 }
 
+void enqueue_split_rows(int64_t N, const int* rowptr, const int* col, const double2* val, int* xcol,
+                        double2* xval, int* split, cudaStream_t st) {
+  if (N > 0) k_split_rows<<<(int)((N + 255) / 256), 256, 0, st>>>(N, rowptr, col, val, xcol, xval, split);
+}
+
 int prepare_spmm_rows(Handle* h) {
   const int64_t N = h->n, nnz = h->nnz;
   if (h->ensure(h->xcol, sizeof(int) * (nnz > 0 ? nnz : 1)) ||
