@@ -297,8 +297,10 @@ def batched_leg(args, sampler, local_rank):
     Ms = [z.shape[0] for z in zks]
     dt = 1.0 * 176.08596 / 1000
     t_end = args.batch_window_ns * 176.08596 / 1000
-    m = args.batch_krylov
     T = num_time_points(dt, t_end)
+    # Krylov dimension by the autotuner (one tile per job, 10 ns), shared by both arms
+    sampler.build_h_batch(systems, fields, "general")
+    m, tune_rates = sampler.autotune_krylov(zks, dt, 10 * dt, 1e-5, candidates=(12, 16, 20, 24, 30, 40))
     offs = np.cumsum([0] + [z.size for z in zks])
     zk_dev = torch.from_numpy(np.concatenate([z.reshape(-1) for z in zks])).to(f"cuda:{local_rank}")
     out_dev = torch.empty(len(zks) * 4 * T, dtype=torch.float64, device=f"cuda:{local_rank}")
@@ -330,11 +332,14 @@ def batched_leg(args, sampler, local_rank):
     t_single = timed(per_instance)
     breakdown = profiled(sampler, batched)
     t_batch = timed(batched)
+    t_build = timed(lambda: sampler.build_h_batch(systems, fields, "general"))
     dims = [4 * s.Z for s in systems]
     return {"value": work / t_batch, "per_instance_value": work / t_single,
             "ratio": t_single / t_batch, "unit": "sample-steps/s", "jobs": len(zks),
             "pairs": len(pairs), "orientations": len(dirs), "dims": [min(dims), max(dims)],
             "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m, "kernel_breakdown": breakdown,
+            "seconds": t_batch, "build_seconds": t_build, "per_instance_seconds": t_single,
+            "krylov_autotune_rates": tune_rates,
             "workload": "uneven pairs (2-10 nuclei from 1H/14N, anisotropic) x Fibonacci-sphere "
                         "orientations at 0.05 mT, own Hamiltonian per job"}
 

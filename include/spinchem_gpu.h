@@ -270,6 +270,17 @@ int spc_yield_gradient_batch(spc_handle* h, int n_jobs, const spc_system* system
                              int n_quad, int checkpoint_every, double wS, double wT, int which,
                              double* yields, double* grad);
 
+/* Krylov-dimension autotuner (no counterpart in the reference): propagates
+ * the first min(M[k], 32) vectors of every job of the batch store (as in
+ * spc_trace_sampling_batch) over [0, t_window] once per candidate dimension,
+ * times each run with CUDA events after a warm-up run, and returns the
+ * candidate with the most sample-steps per second in *best_m (rates, if not
+ * NULL, gets the rate of every candidate). The reference fixes N_krylov in
+ * input.ini; results at any m are the reference's algorithm at that m. */
+int spc_autotune_krylov(spc_handle* h, int n_jobs, const int* job_sys, const int* M, const double* theta,
+                        const double* init_pop, const double* zkets, double dt, double t_window, double tol,
+                        const int* candidates, int n_candidates, int* best_m, double* rates);
+
 /* Select the Krylov orthogonalisation (SPC_KRYLOV_*). In exact arithmetic
  * Lanczos and MGS give the same basis when H_eff = Hermitian - i*kappa; the
  * Lanczos path skips the O(m^2 n) re-orthogonalisation and verifies the

@@ -333,6 +333,82 @@ int spc_trace_sampling_batch(spc_handle* h, int n_jobs, const int* job_sys, cons
   return SPC_OK;
 }
 
+int spc_autotune_krylov(spc_handle* h, int n_jobs, const int* job_sys, const int* M, const double* theta,
+                        const double* init_pop, const double* zkets, double dt, double t_window, double tol,
+                        const int* candidates, int n_candidates, int* best_m, double* rates) {
+  if (!h || n_jobs < 1 || !M || !theta || !init_pop || !zkets || !candidates || n_candidates < 1 || !best_m)
+    return spc::set_error(SPC_ERR_ARG, "spc_autotune_krylov: null argument");
+  if (!(dt > 0.0) || !(t_window > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt and t_window must be positive");
+  for (int c = 0; c < n_candidates; ++c)
+    if (candidates[c] < 1 || candidates[c] > 48)
+      return spc::set_error(SPC_ERR_ARG, "candidate Krylov dimension %d outside [1, 48]", candidates[c]);
+  CKR(cudaSetDevice(h->h.device));
+  spc::Handle& H = h->h;
+  const auto& B = H.hb;
+  if (B.n.empty()) return spc::set_error(SPC_ERR_STATE, "no batch Hamiltonians: call spc_build_h_batch first");
+  // one tile (up to 32 samples) of every job, over a short window
+  std::vector<int> Ms(n_jobs), sys(n_jobs);
+  int64_t zsub = 0, ztot_src = 0;
+  std::vector<int64_t> src_off(n_jobs);
+  for (int k = 0; k < n_jobs; ++k) {
+    sys[k] = job_sys ? job_sys[k] : k;
+    if (sys[k] < 0 || sys[k] >= (int)B.n.size())
+      return spc::set_error(SPC_ERR_ARG, "job %d refers to system %d", k, sys[k]);
+    if (M[k] < 1) return spc::set_error(SPC_ERR_ARG, "job %d has no samples", k);
+    Ms[k] = std::min(M[k], 32);
+    src_off[k] = ztot_src;
+    ztot_src += (int64_t)M[k] * (B.n[sys[k]] / 4);
+    zsub += (int64_t)Ms[k] * (B.n[sys[k]] / 4);
+  }
+  const int T = spc::num_time_points(dt, t_window);
+  if (H.ensure(H.tune_zk, sizeof(double2) * zsub) || H.ensure(H.tune_out, sizeof(double) * 4 * T * n_jobs))
+    return SPC_ERR_ALLOC;
+  {
+    // the jobs' first Ms[k] sample vectors, back to back
+    std::vector<double2> sub(zsub);
+    int64_t o = 0;
+    for (int k = 0; k < n_jobs; ++k) {
+      const int64_t Z = B.n[sys[k]] / 4;
+      std::memcpy(&sub[o], (const double2*)zkets + src_off[k], sizeof(double2) * Ms[k] * Z);
+      o += Ms[k] * Z;
+    }
+    CKR(cudaMemcpyAsync(H.tune_zk.p, sub.data(), sizeof(double2) * zsub, cudaMemcpyHostToDevice, H.stream));
+  }
+  std::vector<spc::JobSpec> jobs;
+  int rc = batch_jobs(h, n_jobs, sys.data(), Ms.data(), (const double2*)H.tune_zk.p, (double*)H.tune_out.p, T,
+                      jobs);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  CKR(cudaEventCreate(&e0));
+  CKR(cudaEventCreate(&e1));
+  double best = -1.0;
+  *best_m = candidates[0];
+  for (int c = 0; c < n_candidates && rc == SPC_OK; ++c) {
+    const int m = candidates[c];
+    double secs = 0.0;
+    for (int rep = 0; rep < 2 && rc == SPC_OK; ++rep) {  // the first run grows the buffers
+      cudaEventRecord(e0, H.stream);
+      rc = spc::propagate_batch(&H, theta, init_pop, jobs, dt, t_window, m, tol, T);
+      cudaEventRecord(e1, H.stream);
+      if (rc == SPC_OK && cudaEventSynchronize(e1) == cudaSuccess) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        secs = ms / 1e3;
+      }
+    }
+    if (rc) break;
+    const double rate = secs > 0.0 ? (double)H.stats.sample_steps / secs : 0.0;
+    if (rates) rates[c] = rate;
+    if (rate > best) {
+      best = rate;
+      *best_m = m;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
 int spc_set_profiling(spc_handle* h, int enable) {
   if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
   h->h.prof.on = enable != 0;

@@ -173,8 +173,14 @@ __global__ void k_gen_count(int64_t N, int64_t Z, int nn, const NucInfo* __restr
   cnt[row] = gen_row_count(row, Z, nn, nuc);
 }
 
-// One thread per row; entries accumulated in generation order into the
-// row's CSR slots, then insertion-sorted by column.
+// One thread per row, every entry written straight to its place in the
+// ascending-column row. Row (e, n) has, for each electron state ep, the block
+// of columns ep*Z + n + delta: delta = -stride_j for the nuclei j (ascending)
+// that S_k.A.I_j lowers, then delta = 0 (the electronic entry, plus every
+// term that keeps the nuclear state, added in nucleus order), then
+// delta = +stride_j for the nuclei (descending) that it raises. Strides of
+// nuclei with multiplicity >= 2 are distinct and |delta| < Z, so this is the
+// sorted order and no column repeats.
 __global__ void k_gen_fill(int64_t N, int64_t Z, int nn, const NucInfo* __restrict__ nuc,
                            GenElectron el, const int* __restrict__ rowptr, int* __restrict__ col,
                            double2* __restrict__ val) {
@@ -183,18 +189,24 @@ __global__ void k_gen_fill(int64_t N, int64_t Z, int nn, const NucInfo* __restri
   int e = (int)(row / Z);
   int64_t nidx = row - (int64_t)e * Z;
   int base = rowptr[row];
-  int ne = 0;
-  auto put = [&](int64_t c, double2 v) {
-    for (int t = 0; t < ne; ++t)
-      if (col[base + t] == (int)c) {
-        val[base + t] = xadd(val[base + t], v);
-        return;
+  auto couples = [&](int k, int ep) { return k == 0 ? ((e & 1) == (ep & 1)) : ((e >> 1) == (ep >> 1)); };
+  // entries below and above the diagonal per electron block
+  int nminus[4] = {0, 0, 0, 0}, nplus[4] = {0, 0, 0, 0};
+  for (int j = 0; j < nn; ++j) {
+    const NucInfo& q = nuc[j];
+    const int mj = nuc_state(q, nidx);
+    for (int ep = 0; ep < 4; ++ep)
+      if (couples(q.owner, ep)) {
+        nminus[ep] += mj > 0;
+        nplus[ep] += mj < q.g - 1;
       }
-    col[base + ne] = (int)c;
-    val[base + ne] = v;
-    ne++;
-  };
-  for (int ep = 0; ep < 4; ++ep) put((int64_t)ep * Z + nidx, el.H[e][ep]);
+  }
+  int off[4];
+  off[0] = base;
+  for (int ep = 1; ep < 4; ++ep) off[ep] = off[ep - 1] + nminus[ep - 1] + 1 + nplus[ep - 1];
+  double2 d[4];
+  for (int ep = 0; ep < 4; ++ep) d[ep] = el.H[e][ep];
+  int seen_minus[4] = {0, 0, 0, 0}, seen_plus[4] = {0, 0, 0, 0};
   for (int j = 0; j < nn; ++j) {
     const NucInfo& q = nuc[j];
     int g = q.g, k = q.owner;
@@ -202,35 +214,93 @@ __global__ void k_gen_fill(int64_t N, int64_t Z, int nn, const NucInfo* __restri
     for (int mp = mj - 1; mp <= mj + 1; ++mp) {
       if (mp < 0 || mp >= g) continue;
       int64_t nc = nidx + (int64_t)(mp - mj) * q.stride;
+      double2 ie[3];
+      for (int c = 0; c < 3; ++c) ie[c] = nuc_el(g, c, mj, mp);
       for (int ep = 0; ep < 4; ++ep) {
-        int other_same = k == 0 ? ((e & 1) == (ep & 1)) : ((e >> 1) == (ep >> 1));
-        if (!other_same) continue;
+        if (!couples(k, ep)) continue;
         double2 v = cz();
         for (int r = 0; r < 3; ++r) {
           double2 se = pair_el(k, r, e, ep);
-          for (int c = 0; c < 3; ++c) {
-            double2 ie = nuc_el(g, c, mj, mp);
-            v = xadd(v, xrscale(q.A[r * 3 + c], xmul(se, ie)));
-          }
+          for (int c = 0; c < 3; ++c) v = xadd(v, xrscale(q.A[r * 3 + c], xmul(se, ie[c])));
         }
         if (ep == e)
-          for (int c = 0; c < 3; ++c) v = xadd(v, xrscale(q.zeta[c], nuc_el(g, c, mj, mp)));
-        put((int64_t)ep * Z + nc, v);
+          for (int c = 0; c < 3; ++c) v = xadd(v, xrscale(q.zeta[c], ie[c]));
+        int pos;
+        if (mp == mj) {
+          d[ep] = xadd(d[ep], v);
+          continue;
+        } else if (mp < mj) {
+          pos = off[ep] + seen_minus[ep]++;
+        } else {
+          pos = off[ep] + nminus[ep] + 1 + (nplus[ep] - 1 - seen_plus[ep]++);
+        }
+        col[pos] = (int)((int64_t)ep * Z + nc);
+        val[pos] = v;
       }
     }
   }
-  // insertion sort by column
-  for (int i = 1; i < ne; ++i) {
-    int c = col[base + i];
-    double2 v = val[base + i];
-    int t = i - 1;
-    while (t >= 0 && col[base + t] > c) {
-      col[base + t + 1] = col[base + t];
-      val[base + t + 1] = val[base + t];
-      t--;
+  for (int ep = 0; ep < 4; ++ep) {
+    col[off[ep] + nminus[ep]] = (int)((int64_t)ep * Z + nidx);
+    val[off[ep] + nminus[ep]] = d[ep];
+  }
+}
+
+// k_gen_fill with the entry values read from the host-built tables
+// (HostSystem::gen_tab): the same values, without the per-row FP64 work that
+// dominates a build on a part with a narrow FP64 pipe.
+__global__ void k_gen_fill_tab(int64_t N, int64_t Z, int nn, const NucInfo* __restrict__ nuc,
+                               GenElectron el, const double2* __restrict__ tab,
+                               const int* __restrict__ rowptr, int* __restrict__ col,
+                               double2* __restrict__ val) {
+  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= N) return;
+  int e = (int)(row / Z);
+  int64_t nidx = row - (int64_t)e * Z;
+  int base = rowptr[row];
+  auto couples = [&](int k, int ep) { return k == 0 ? ((e & 1) == (ep & 1)) : ((e >> 1) == (ep >> 1)); };
+  int nminus[4] = {0, 0, 0, 0}, nplus[4] = {0, 0, 0, 0};
+  for (int j = 0; j < nn; ++j) {
+    const NucInfo& q = nuc[j];
+    const int mj = nuc_state(q, nidx);
+    for (int ep = 0; ep < 4; ++ep)
+      if (couples(q.owner, ep)) {
+        nminus[ep] += mj > 0;
+        nplus[ep] += mj < q.g - 1;
+      }
+  }
+  int off[4];
+  off[0] = base;
+  for (int ep = 1; ep < 4; ++ep) off[ep] = off[ep - 1] + nminus[ep - 1] + 1 + nplus[ep - 1];
+  double2 d[4];
+  for (int ep = 0; ep < 4; ++ep) d[ep] = el.H[e][ep];
+  int seen_minus[4] = {0, 0, 0, 0}, seen_plus[4] = {0, 0, 0, 0};
+  for (int j = 0; j < nn; ++j) {
+    const NucInfo& q = nuc[j];
+    const int g = q.g, k = q.owner;
+    const int mj = nuc_state(q, nidx);
+    for (int mp = mj - 1; mp <= mj + 1; ++mp) {
+      if (mp < 0 || mp >= g) continue;
+      const int64_t nc = nidx + (int64_t)(mp - mj) * q.stride;
+      for (int ep = 0; ep < 4; ++ep) {
+        if (!couples(k, ep)) continue;
+        const double2 v = tab[q.tab_off + ((int64_t)(e * 4 + ep) * g + mj) * 3 + (mp - mj + 1)];
+        int pos;
+        if (mp == mj) {
+          d[ep] = xadd(d[ep], v);
+          continue;
+        } else if (mp < mj) {
+          pos = off[ep] + seen_minus[ep]++;
+        } else {
+          pos = off[ep] + nminus[ep] + 1 + (nplus[ep] - 1 - seen_plus[ep]++);
+        }
+        col[pos] = (int)((int64_t)ep * Z + nc);
+        val[pos] = v;
+      }
     }
-    col[base + t + 1] = c;
-    val[base + t + 1] = v;
+  }
+  for (int ep = 0; ep < 4; ++ep) {
+    col[off[ep] + nminus[ep]] = (int)((int64_t)ep * Z + nidx);
+    val[off[ep] + nminus[ep]] = d[ep];
   }
 }
 
@@ -269,6 +339,7 @@ __global__ void k_scan_rows(const int* __restrict__ cnt, int* __restrict__ rowpt
 struct BuildSlice {
   const HostSystem* hs;
   const NucInfo* nuc;   // device nucleus table
+  const double2* tab;   // device entry tables (general builder)
   int* cnt;             // N per-row counts (scratch)
   int* rowptr;          // N + 1
   int* col;             // fill target (nnz)
@@ -313,7 +384,7 @@ static int build_slices(Handle* h, std::vector<BuildSlice>& sl, const std::vecto
     if (mode == SPC_H_REFERENCE)
       k_ref_fill<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->ref, b.rowptr, b.col, b.val);
     else
-      k_gen_fill<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->gen, b.rowptr, b.col, b.val);
+      k_gen_fill_tab<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->gen, b.tab, b.rowptr, b.col, b.val);
     enqueue_split_rows(N, b.rowptr, b.col, b.val, b.xcol, b.xval, b.split, st);
     h->count_launch(2);
   }
@@ -322,19 +393,34 @@ static int build_slices(Handle* h, std::vector<BuildSlice>& sl, const std::vecto
   return SPC_OK;
 }
 
-// Nucleus tables of the systems back to back on the device (scratch in h).
+// Nucleus descriptions and entry tables of the systems back to back on the
+// device (scratch in h): system k's nuclei from element off[k] of bnuc, their
+// tab_off rebased onto the concatenated table in btab.
 static int upload_nuclei(Handle* h, const std::vector<const HostSystem*>& hs, std::vector<size_t>& off) {
   std::vector<NucInfo> all;
+  std::vector<double2> tab;
   off.resize(hs.size());
   for (size_t k = 0; k < hs.size(); ++k) {
     off[k] = all.size();
-    all.insert(all.end(), hs[k]->nuc.begin(), hs[k]->nuc.end());
+    const int64_t tb = (int64_t)tab.size();
+    for (NucInfo q : hs[k]->nuc) {
+      q.tab_off += tb;
+      all.push_back(q);
+    }
+    tab.insert(tab.end(), hs[k]->gen_tab.begin(), hs[k]->gen_tab.end());
   }
-  if (h->ensure(h->bnuc, sizeof(NucInfo) * std::max<size_t>(1, all.size()))) return SPC_ERR_ALLOC;
+  if (h->ensure(h->bnuc, sizeof(NucInfo) * std::max<size_t>(1, all.size())) ||
+      h->ensure(h->btab, sizeof(double2) * std::max<size_t>(1, tab.size())))
+    return SPC_ERR_ALLOC;
   if (!all.empty() &&
       cudaMemcpyAsync(h->bnuc.p, all.data(), sizeof(NucInfo) * all.size(), cudaMemcpyHostToDevice, h->stream) !=
           cudaSuccess)
     return set_error(SPC_ERR_CUDA, "nucleus table upload failed");
+  if (!tab.empty() &&
+      cudaMemcpyAsync(h->btab.p, tab.data(), sizeof(double2) * tab.size(), cudaMemcpyHostToDevice, h->stream) !=
+          cudaSuccess)
+    return set_error(SPC_ERR_CUDA, "entry table upload failed");
+  // the host vectors are pageable: the copies have completed on return
   return SPC_OK;
 }
 
@@ -351,7 +437,8 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode) {
       h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nnz, 1)) || h->ensure(h->xsplit, sizeof(int) * N))
     return SPC_ERR_ALLOC;
   std::vector<BuildSlice> sl(1);
-  sl[0] = BuildSlice{&hs, (const NucInfo*)h->bnuc.p, (int*)h->bcnt.p, h->d_rowptr, h->d_col, h->d_val,
+  sl[0] = BuildSlice{&hs, (const NucInfo*)h->bnuc.p, (const double2*)h->btab.p, (int*)h->bcnt.p, h->d_rowptr,
+                     h->d_col, h->d_val,
                      (int*)h->xcol.p, (double2*)h->xval.p, (int*)h->xsplit.p, (long long*)h->btot.p};
   rc = build_slices(h, sl, {nnz}, mode);
   if (rc) return rc;
@@ -399,7 +486,7 @@ int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode)
   std::vector<BuildSlice> sl(ns);
   int64_t coff = 0;
   for (size_t k = 0; k < ns; ++k) {
-    sl[k] = BuildSlice{&hs[k], (const NucInfo*)h->bnuc.p + noff[k], (int*)h->bcnt.p + coff,
+    sl[k] = BuildSlice{&hs[k], (const NucInfo*)h->bnuc.p + noff[k], (const double2*)h->btab.p, (int*)h->bcnt.p + coff,
                        (int*)B.rowptr.p + B.rp_off[k], (int*)h->xcol.p + B.nz_off[k],
                        (double2*)h->xval.p + B.nz_off[k], (int*)B.col.p + B.nz_off[k],
                        (double2*)B.val.p + B.nz_off[k], (int*)B.split.p + B.rp_off[k],

@@ -68,7 +68,7 @@ Handle::~Handle() {
   Buf* all[] = {&psi, &Q,  &P,    &partial, &counters, &coef, &rbeta, &Ahess, &Aexp, &proj, &projpart,
                 &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag, &xcol, &xval, &xsplit, &plan, &jobtab,
                 &hb.rowptr, &hb.split, &hb.col, &hb.val, &gck, &gseg, &gnu, &gmu, &glam, &cvec2,
-                &gslots, &gracc, &gfacc, &bcnt, &bnuc, &btot};
+                &gslots, &gracc, &gfacc, &bcnt, &bnuc, &btot, &btab, &tune_out, &tune_zk};
   for (Buf* b : all)
     if (b->p) cudaFree(b->p);
   if (d_rowptr) cudaFree(d_rowptr);
@@ -102,6 +102,49 @@ static cd pair_el(int k, int r, int e, int ep) {
   int s1 = e >> 1, s2 = e & 1, t1 = ep >> 1, t2 = ep & 1;
   if (k == 0) return s2 == t2 ? spin_half_el(r, s1, t1) : cd{0.0, 0.0};
   return s1 == t1 ? spin_half_el(r, s2, t2) : cd{0.0, 0.0};
+}
+
+// <a|I_c|b> for multiplicity g, states m = I, I-1, ...; the device builder's
+// formula with the same rounding points
+static cd nuc_el(int g, int c, int a, int b) {
+  const double I = (g - 1) / 2.0;
+  const double ma = I - a, mb = I - b;
+  if (c == 2) return a == b ? cd{ma, 0.0} : cd{0.0, 0.0};
+  if (!(a == b - 1 || a == b + 1)) return cd{0.0, 0.0};
+  const double l = std::sqrt(I * (I + 1.0) - ma * mb);
+  if (c == 0) return cd{0.5 * l, 0.0};
+  return a == b - 1 ? cd{0.0, -0.5 * l} : cd{0.0, 0.5 * l};
+}
+
+// Entry tables of the general builder (see HostSystem::gen_tab): the values
+// k_gen_fill would compute per row, in the same operation order.
+static void general_tables(HostSystem& hs) {
+  hs.gen_tab.clear();
+  for (NucInfo& q : hs.nuc) {
+    q.tab_off = (int64_t)hs.gen_tab.size();
+    const int g = q.g, k = q.owner;
+    hs.gen_tab.resize(hs.gen_tab.size() + (size_t)48 * g, make_double2(0.0, 0.0));
+    for (int e = 0; e < 4; ++e)
+      for (int ep = 0; ep < 4; ++ep) {
+        const bool couples = k == 0 ? ((e & 1) == (ep & 1)) : ((e >> 1) == (ep >> 1));
+        if (!couples) continue;
+        for (int mj = 0; mj < g; ++mj)
+          for (int d = 0; d < 3; ++d) {
+            const int mp = mj + d - 1;
+            if (mp < 0 || mp >= g) continue;
+            cd ie[3];
+            for (int c = 0; c < 3; ++c) ie[c] = nuc_el(g, c, mj, mp);
+            cd v{0.0, 0.0};
+            for (int r = 0; r < 3; ++r) {
+              const cd se = pair_el(k, r, e, ep);
+              for (int c = 0; c < 3; ++c) v = cadd(v, rsc(q.A[r * 3 + c], cmulx(se, ie[c])));
+            }
+            if (ep == e)
+              for (int c = 0; c < 3; ++c) v = cadd(v, rsc(q.zeta[c], ie[c]));
+            hs.gen_tab[q.tab_off + ((size_t)(e * 4 + ep) * g + mj) * 3 + d] = make_double2(v.re, v.im);
+          }
+      }
+  }
 }
 
 int make_host_system(const spc_system* sys, int mode, HostSystem& hs) {
@@ -215,6 +258,7 @@ int make_host_system(const spc_system* sys, int mode, HostSystem& hs) {
         if (e == ep) hv = csub(hv, cd{0.0, 0.5 * k_bar});
         hs.gen.H[e][ep] = make_double2(hv.re, hv.im);
       }
+    general_tables(hs);
   }
   return SPC_OK;
 }

@@ -21,6 +21,7 @@ struct NucInfo {
   double A[9];      // full tensor, A[r*3+c] (general builder)
   double zeta[3];   // (gamma/gamma_e) * B_c (general builder)
   double gratio;    // gamma/gamma_e
+  int64_t tab_off;  // general builder: offset of this nucleus' entry table (48 g complex)
 };
 
 // Electronic 4x4 pieces of getHiso_sp, rounded as the reference rounds them.
@@ -40,6 +41,11 @@ struct HostSystem {
   RefElectron ref;
   GenElectron gen;
   bool herm_shift = false;  // kS == kT: H_eff is Hermitian minus i*kbar/2
+  // general builder: per nucleus j, the matrix element of the Hamiltonian
+  // terms of nucleus j between (e, m_j) and (ep, m_j + d - 1), d = 0..2, at
+  // [tab_off + ((e * 4 + ep) * g + m_j) * 3 + d] (zero where S_k.A.I_j does
+  // not couple e and ep)
+  std::vector<double2> gen_tab;
 };
 
 // Builds the host-side description; returns SPC_OK or an error code with
@@ -106,7 +112,9 @@ struct Handle {
   Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
       map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit, plan, jobtab;
   // Hamiltonian build scratch: row counts, nucleus tables, nonzero totals
-  Buf bcnt, bnuc, btot;
+  Buf bcnt, bnuc, btot, btab;
+  // autotuner outputs and sample subsets
+  Buf tune_out, tune_zk;
   // yield-gradient workspace: checkpoints, segment states, node states,
   // costate pair, second coordinate vector, slot table, accumulators
   Buf gck, gseg, gnu, gmu, glam, cvec2, gslots, gracc, gfacc;

@@ -717,6 +717,92 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// The same dt loop with 32/LPS samples per warp, LPS lanes each, for Krylov
+// dimensions m <= LPS (one row of c per lane). A warp instruction costs the
+// same FP64 issue time however many lanes are active, so packing small bases
+// raises throughput; the group sums add the same nonzero terms in the same
+// tree order as the 32-lane sum (whose extra lanes add exact zeros), so the
+// results are identical to k_dtloop's. Samples of one warp may stop after
+// different steps: every sync and shuffle is masked to the sample's lanes.
+template <int LPS>
+__global__ void __launch_bounds__(128)
+    k_dtloop_packed(int m, int nslots, int T, const TileInfo* __restrict__ tiles,
+                    const int* __restrict__ map, const int* __restrict__ skip,
+                    const double2* __restrict__ Aexp, const double2* __restrict__ proj,
+                    double2* __restrict__ cvec, double* __restrict__ tt, int* __restrict__ kk,
+                    int* __restrict__ done, double* __restrict__ obs, double dt, double t_end, double tol,
+                    long long* __restrict__ nsteps, int* __restrict__ err) {
+  constexpr int SPW = 32 / LPS;  // samples per warp
+  __shared__ double2 cs[4 * SPW][LPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int grp = lane / LPS, gl = lane % LPS;
+  const unsigned gmask = ((1u << LPS) - 1u) << (grp * LPS);
+  const int w = (blockIdx.x * 4 + warp) * SPW + grp;
+  if (w >= nslots || map[w] < 0 || skip[w]) return;  // the sample's whole lane group leaves
+  const int s = map[w];
+  const size_t mm = (size_t)m * m;
+  const double2* E = Aexp + (size_t)w * mm;
+  const double2* PX = proj + (size_t)w * 4 * mm;
+  double2* c = cs[warp * SPW + grp];
+  const int me = tiles[w / SPC_LANES].m;
+  const bool l0 = gl < me;
+  if (l0) c[gl] = cvec[(size_t)w * m + gl];
+  __syncwarp(gmask);
+  auto gsum = [&](double v) {
+#pragma unroll
+    for (int o = LPS / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
+    return v;
+  };
+  double t = tt[s];
+  int k = kk[s];
+  double c2 = 1.0, cm2 = 0.0;
+  double* o = obs + (size_t)s * 4 * T;
+  const int slot[4] = {2, 0, 1, 3};  // proj type -> obs slot
+  long long steps = 0;
+  while (cm2 <= tol * c2 && t < t_end) {
+    double2 n0 = cz();
+    for (int j = 0; j < me; ++j) {
+      const double2 cj = c[j];
+      if (l0) n0 = cfma(E[gl + j * m], cj, n0);
+    }
+    __syncwarp(gmask);
+    if (l0) c[gl] = n0;
+    __syncwarp(gmask);
+    if (k >= T) {
+      if (gl == 0) atomicExch(err, 1);
+      break;
+    }
+    for (int ty = 0; ty < 4; ++ty) {
+      const double2* P = PX + ty * mm;
+      double2 v0 = cz();
+      for (int j = 0; j < me; ++j) {
+        const double2 cj = c[j];
+        if (l0) v0 = cfma(P[gl + j * m], cj, v0);
+      }
+      double term = 0.0;
+      if (l0) term = fma(n0.x, v0.x, n0.y * v0.y);
+      term = gsum(term);
+      if (gl == 0) o[slot[ty] * T + k] = term;
+    }
+    double nn = 0.0;
+    if (l0) nn = fma(n0.x, n0.x, n0.y * n0.y);
+    c2 = gsum(nn);
+    const double2 cmv = c[me - 1];
+    cm2 = cmv.x * cmv.x + cmv.y * cmv.y;
+    t = t + dt;
+    k = k + 1;
+    steps++;
+  }
+  __syncwarp(gmask);
+  if (l0) cvec[(size_t)w * m + gl] = c[gl];
+  if (gl == 0) {
+    tt[s] = t;
+    kk[s] = k;
+    done[s] = (t < t_end) ? 0 : 1;
+    atomicAdd((unsigned long long*)nsteps, (unsigned long long)steps);
+  }
+}
+
 // psi[:, scol] = Q c for the tile of a pass item (src/qm_dynamics.f90:365)
 __global__ void __launch_bounds__(256)
     k_psi_update(const TileInfo* __restrict__ tiles, const int2* __restrict__ items, int m,
@@ -1211,8 +1297,17 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
         if (map[w] >= 0 && flag_h[w]) failed.push_back(map[w]);
     }
     pe = h->prof.begin(st);
-    k_dtloop<<<(nslots + 3) / 4, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj, d_c, d_t,
-                                               d_k, d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
+    if (m <= 8)
+      k_dtloop_packed<8><<<(nslots + 15) / 16, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj,
+                                                              d_c, d_t, d_k, d_done, d_obs, dt, t_end, tol,
+                                                              d_nsteps, d_err);
+    else if (m <= 16)
+      k_dtloop_packed<16><<<(nslots + 7) / 8, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj,
+                                                             d_c, d_t, d_k, d_done, d_obs, dt, t_end, tol,
+                                                             d_nsteps, d_err);
+    else
+      k_dtloop<<<(nslots + 3) / 4, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj, d_c, d_t,
+                                                 d_k, d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
     h->prof.end(st, pe, PK_DTLOOP, 0.0, 0.0);
     pe = h->prof.begin(st);
     k_psi_update<<<nip, blk, 0, st>>>(d_tiles, d_items_p, m, d_map, d_scol, d_flag, d_Q, d_c, d_psi);

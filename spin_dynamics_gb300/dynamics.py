@@ -29,10 +29,9 @@ def _dptr(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
 
 
-def make_system(sys: SysParam, B) -> tuple:
-    """Fill an spc_system from a SysParam and a field (scalar along z, or a
-    3-vector). Returns (struct, keepalive arrays)."""
-    Bv = np.array([0.0, 0.0, float(B)]) if np.isscalar(B) else np.asarray(B, np.float64).reshape(3)
+def _system_template(sys: SysParam) -> tuple:
+    """The field-independent part of an spc_system: (struct, keepalive
+    arrays) with nuclei, couplings and rates filled and B = 0."""
     keep = []
 
     def arr(x, dt):
@@ -60,8 +59,6 @@ def make_system(sys: SysParam, B) -> tuple:
     if sys.e2.gamma_I is not None:
         g2 = arr(sys.e2.gamma_I, np.float64)
         s.gamma2 = g2.ctypes.data_as(C.POINTER(C.c_double))
-    for i in range(3):
-        s.B[i] = float(Bv[i])
     s.J = float(sys.J)
     Dc = np.asarray(sys.D, np.float64).reshape(3, 3).T.reshape(9)
     for i in range(9):
@@ -69,6 +66,38 @@ def make_system(sys: SysParam, B) -> tuple:
     s.kS = float(sys.kS)
     s.kT = float(sys.kT)
     return s, keep
+
+
+def _with_field(template: tuple, B) -> tuple:
+    s0, keep = template
+    s = nat.spc_system.from_buffer_copy(s0)
+    if np.isscalar(B):
+        s.B[0], s.B[1], s.B[2] = 0.0, 0.0, float(B)
+    else:
+        Bv = np.asarray(B, np.float64).reshape(3)
+        s.B[0], s.B[1], s.B[2] = float(Bv[0]), float(Bv[1]), float(Bv[2])
+    return s, keep
+
+
+def make_system(sys: SysParam, B) -> tuple:
+    """Fill an spc_system from a SysParam and a field (scalar along z, or a
+    3-vector). Returns (struct, keepalive arrays)."""
+    return _with_field(_system_template(sys), B)
+
+
+def make_systems(systems, fields) -> tuple:
+    """spc_system array for (system, field) pairs; a system object that
+    appears with several fields is converted once. Returns (ctypes array,
+    keepalive)."""
+    cache, structs, keep = {}, [], []
+    for sy, B in zip(systems, fields):
+        t = cache.get(id(sy))
+        if t is None:
+            t = cache[id(sy)] = _system_template(sy)
+            keep.append(t)
+        structs.append(_with_field(t, B)[0])
+    arr = (nat.spc_system * len(structs))(*structs)
+    return arr, (keep, systems)
 
 
 def num_time_points(dt: float, t_end: float) -> int:
@@ -241,13 +270,8 @@ class TraceSampler:
         """Build one Hamiltonian per (system, field) pair and keep them as
         the handle's batch. Returns the dimensions."""
         m = {"reference": nat.SPC_H_REFERENCE, "general": nat.SPC_H_GENERAL}[mode]
-        structs, keep = [], []
-        for s, B in zip(systems, fields):
-            st, k = make_system(s, B)
-            structs.append(st)
-            keep.append(k)
-        arr = (nat.spc_system * len(structs))(*structs)
-        nat.check(nat.lib().spc_build_h_batch(self._h, len(structs), C.cast(arr, C.c_void_p), m))
+        arr, keep = make_systems(systems, fields)
+        nat.check(nat.lib().spc_build_h_batch(self._h, len(arr), C.cast(arr, C.c_void_p), m))
         return [4 * s.Z for s in systems]
 
     def trace_sampling_batch(self, zkets_list, dt: float, t_end: float, m: int, tol: float,
@@ -312,13 +336,9 @@ class TraceSampler:
         the B, J, D, kS, kT entries only (nuclei up to multiplicity 6).
         gradient=False returns the yields only. Returns one YieldGradient per
         job."""
-        structs, keep = [], []
-        for s, B in zip(systems, fields):
-            st, k = make_system(s, B)
-            structs.append(st)
-            keep.append(k)
-        arr = (nat.spc_system * len(structs))(*structs)
-        sizes = [nat.lib().spc_yield_gradient_size(C.byref(st)) for st in structs]
+        arr, keep = make_systems(systems, fields)
+        structs = list(arr)
+        sizes = [15 + 9 * (len(s.e1.g_I) + len(s.e2.g_I)) for s in systems]
         M = np.array([z.shape[0] for z in zkets_list], np.int32)
         flat = np.ascontiguousarray(np.concatenate([np.asarray(z, np.complex128).reshape(-1)
                                                     for z in zkets_list]))
@@ -352,6 +372,27 @@ class TraceSampler:
             self._h, C.byref(st), _dptr(th), _dptr(zk.view(np.float64)), zk.shape[0], float(dt),
             float(t_end), int(m), 1, 0, 1.0, 0.0, _dptr(y), None))
         return float(y[0]), float(y[1])
+
+    def autotune_krylov(self, zkets_list, dt: float, t_window: float, tol: float,
+                        candidates=(12, 16, 20, 24, 30, 40), init_state: str = "singlet",
+                        job_sys=None) -> tuple:
+        """spc_autotune_krylov over the batch store: the Krylov dimension with
+        the most sample-steps/s on one tile of every job. Returns (best_m,
+        {m: rate})."""
+        M = np.array([z.shape[0] for z in zkets_list], np.int32)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(z, np.complex128).reshape(-1)
+                                                    for z in zkets_list]))
+        th, pop = init_el_state(init_state)
+        th = np.ascontiguousarray(th).view(np.float64)
+        cand = np.ascontiguousarray(candidates, np.int32)
+        rates = np.zeros(cand.size)
+        best = C.c_int(0)
+        js = None if job_sys is None else np.ascontiguousarray(job_sys, np.int32)
+        nat.check(nat.lib().spc_autotune_krylov(
+            self._h, len(zkets_list), _dptr(js) if js is not None else None, _dptr(M), _dptr(th), _dptr(pop),
+            _dptr(flat.view(np.float64)), float(dt), float(t_window), float(tol), _dptr(cand), int(cand.size),
+            C.byref(best), _dptr(rates)))
+        return int(best.value), {int(m): float(r) for m, r in zip(cand, rates)}
 
     def stats(self) -> dict:
         s = nat.spc_stats()

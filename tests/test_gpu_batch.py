@@ -111,3 +111,21 @@ def test_krylov_dimension_capped_at_job_dimension(sampler, oracle):
     assert np.max(np.abs(got[0].P_S[:n] - PS)) < 1e-12
     rp, col, val = iso_csr(oracle, big, 0.1)
     _check(got[1], oracle.trace_sampling(rp, col, val, zb, DT, t_end, 20, 1e-6))
+
+
+def test_autotuned_krylov_dimension(sampler, oracle):
+    """The autotuner returns one of the candidates with a positive rate for
+    each, and a batch run at the chosen dimension keeps parity."""
+    systems = [W.notebook_pair(), W.small_pair()]
+    for s in systems:
+        s.kS = s.kT = 1.0 / GAMMA_E
+    fields = [0.1, 0.05]
+    zks = [W.random_phase_samples(s.Z, M, seed=30 + i) for i, (s, M) in enumerate(zip(systems, (40, 20)))]
+    sampler.build_h_batch(systems, fields, "reference")
+    best, rates = sampler.autotune_krylov(zks, DT, 8 * DT, 1e-6, candidates=(8, 12, 16))
+    assert best in (8, 12, 16)
+    assert all(r > 0 for r in rates.values()) and rates[best] == max(rates.values())
+    got = sampler.trace_sampling_batch(zks, DT, 15 * DT, best, 1e-6)
+    for s, f, zk, g in zip(systems, fields, zks, got):
+        rp, col, val = iso_csr(oracle, s, f)
+        _check(g, oracle.trace_sampling(rp, col, val, zk, DT, 15 * DT, best, 1e-6))
