@@ -450,8 +450,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
       h->count_launch();
     }
   }
-  const size_t expm_smem = sizeof(double2) * 5 * mm;
-  CK(cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expm_smem));
+  CK(set_expm_smem(m));
   const dim3 blk(SPC_LANES, SPC_WARPS);
   // the three-term recurrence only on explicit request: no projector Gram
   // verifies these bases (the trace-sampling path checks its own)
@@ -531,7 +530,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
   // y = exp(-i tau H) x from the current bases (tau < 0 runs backwards)
   auto apply = [&](double tau, const TileInfo* tiles, double2* y) {
     int pe = h->prof.begin(st);
-    k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, tiles, d_map, d_A, d_E, tau, d_err);
+    launch_expm(m, nslots, tiles, d_map, d_A, d_E, tau, d_err, st);
     h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * Mtot, 32.0 * (double)mm * Mtot);
     pe = h->prof.begin(st);
     k_first_col<<<(nslots + 127) / 128, 128, 0, st>>>(nslots, tiles, d_map, m, d_E, d_c, d_c2);

@@ -329,11 +329,22 @@ int prepare_spmm_rows(Handle* h) {
 }
 
 // ---------------------------------------------------------------------------
-// expm (src/matrix_exponential.f90:14-87) of -i dt A, one CTA per sample.
-// Column-major m x m matrices in shared memory.
-__device__ void smem_matmul(int m, const double2* A, const double2* B, double2* C) {
+// expm (src/matrix_exponential.f90:14-87) of -i dt A per sample, column-major
+// m x m matrices in shared memory. expm_one is run by nt threads (index tid)
+// that synchronise as a whole CTA (one sample per CTA) or as one warp (k_expm
+// packs four samples per 128-thread CTA for m <= 16); every element is
+// computed by the same serial loop either way, so both give the same bits.
+template <bool WARP>
+__device__ __forceinline__ void expm_sync() {
+  if (WARP)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
+__device__ void smem_matmul(int m, const double2* A, const double2* B, double2* C, int tid, int nt) {
   const int mm = m * m;
-  for (int idx = threadIdx.x; idx < mm; idx += blockDim.x) {
+  for (int idx = tid; idx < mm; idx += nt) {
     const int i = idx % m, j = idx / m;
     double2 acc = cz();
     for (int k = 0; k < m; ++k) acc = cfma(A[i + k * m], B[k + j * m], acc);
@@ -341,39 +352,29 @@ __device__ void smem_matmul(int m, const double2* A, const double2* B, double2* 
   }
 }
 
-__global__ void __launch_bounds__(128)
-    k_expm(int mld, int nslots, const TileInfo* __restrict__ tiles, const int* __restrict__ map,
-           const double2* __restrict__ Ahess, double2* __restrict__ Aexp, double dt,
-           int* __restrict__ err) {
-  extern __shared__ double2 sm[];
-  __shared__ double rowsum[SPC_MAX_M];
-  __shared__ int piv[SPC_MAX_M];
-  __shared__ int s_sh, p_sh;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int w = blockIdx.x;
-  if (w >= nslots || map[w] < 0) return;
-  // working dimension m <= mld (the storage leading dimension)
-  const int m = tiles[w / SPC_LANES].m;
+template <bool WARP>
+__device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double2* __restrict__ out, double dt,
+                         double2* sm, double* rowsum, int* piv, int* s_sh, int* p_sh, int tid, int nt,
+                         int* __restrict__ err) {
   const int mm = m * m;
   double2* A2 = sm;
   double2* X = A2 + mm;
   double2* E = X + mm;
   double2* D = E + mm;
   double2* T = D + mm;
-  const double2* Ain = Ahess + (size_t)w * mld * mld;
   // (0,-1)*dt*A
   for (int i = tid; i < mm; i += nt) {
     double2 a = Ain[(i % m) + (size_t)(i / m) * mld];
     A2[i] = make_double2(dt * a.y, -dt * a.x);
   }
-  __syncthreads();
+  expm_sync<WARP>();
   // L-infinity norm (mat_norm_linf :89-104)
   for (int i = tid; i < m; i += nt) {
     double s = 0.0;
     for (int j = 0; j < m; ++j) s += hypot(A2[i + j * m].x, A2[i + j * m].y);
     rowsum[i] = s;
   }
-  __syncthreads();
+  expm_sync<WARP>();
   if (tid == 0) {
     double an = 0.0;
     for (int i = 0; i < m; ++i) an = fmax(an, rowsum[i]);
@@ -383,10 +384,10 @@ __global__ void __launch_bounds__(128)
       const int ee = (int)l2 + 1;            // int() truncates toward zero
       s = max(0, ee + 1);
     }
-    s_sh = s;
+    *s_sh = s;
   }
-  __syncthreads();
-  const int s = s_sh;
+  expm_sync<WARP>();
+  const int s = *s_sh;
   const double sc = ldexp(1.0, -s);  // A/2**s, exact
   for (int i = tid; i < mm; i += nt) {
     double2 a = make_double2(A2[i].x * sc, A2[i].y * sc);
@@ -396,15 +397,15 @@ __global__ void __launch_bounds__(128)
     E[i] = make_double2(id + 0.5 * a.x, 0.5 * a.y);
     D[i] = make_double2(id - 0.5 * a.x, -0.5 * a.y);
   }
-  __syncthreads();
+  expm_sync<WARP>();
   // Pade(6,6) by the c_k recurrence (:54-77)
   const int q = 6;
   double c = 0.5;
   bool p = true;
   for (int k = 2; k <= q; ++k) {
     c = c * (double)(q - k + 1) / (double)(k * (2 * q - k + 1));
-    smem_matmul(m, A2, X, T);
-    __syncthreads();
+    smem_matmul(m, A2, X, T, tid, nt);
+    expm_sync<WARP>();
     for (int i = tid; i < mm; i += nt) {
       const double2 x = T[i];
       X[i] = x;
@@ -413,7 +414,7 @@ __global__ void __launch_bounds__(128)
                : make_double2(D[i].x - c * x.x, D[i].y - c * x.y);
     }
     p = !p;
-    __syncthreads();
+    expm_sync<WARP>();
   }
   // inv(D) by LU with partial pivoting (|re|+|im| pivot, as izamax), in place
   for (int k = 0; k < m; ++k) {
@@ -437,29 +438,29 @@ __global__ void __launch_bounds__(128)
         }
       }
       if (tid == 0) {
-        p_sh = bi;
+        *p_sh = bi;
         piv[k] = bi;
         if (best == 0.0) atomicExch(err, 2);
       }
     }
-    __syncthreads();
-    const int pr = p_sh;
+    expm_sync<WARP>();
+    const int pr = *p_sh;
     if (pr != k)
       for (int j = tid; j < m; j += nt) {
         const double2 t0 = D[k + j * m];
         D[k + j * m] = D[pr + j * m];
         D[pr + j * m] = t0;
       }
-    __syncthreads();
+    expm_sync<WARP>();
     const double2 dkk = D[k + k * m];
     for (int i = k + 1 + tid; i < m; i += nt) D[i + k * m] = cdiv(D[i + k * m], dkk);
-    __syncthreads();
+    expm_sync<WARP>();
     const int rem = m - k - 1;
     for (int idx = tid; idx < rem * rem; idx += nt) {
       const int i = k + 1 + idx % rem, j = k + 1 + idx / rem;
       D[i + j * m] = cfms(D[i + k * m], D[k + j * m], D[i + j * m]);
     }
-    __syncthreads();
+    expm_sync<WARP>();
   }
   // T = inv(D): column j solves LU x = P e_j
   for (int j = tid; j < m; j += nt) {
@@ -482,20 +483,76 @@ __global__ void __launch_bounds__(128)
       x[i] = cdiv(acc, D[i + i * m]);
     }
   }
-  __syncthreads();
+  expm_sync<WARP>();
   // E = inv(D) E, then s squarings
-  smem_matmul(m, T, E, X);
-  __syncthreads();
+  smem_matmul(m, T, E, X, tid, nt);
+  expm_sync<WARP>();
   for (int i = tid; i < mm; i += nt) E[i] = X[i];
-  __syncthreads();
+  expm_sync<WARP>();
   for (int k = 0; k < s; ++k) {
-    smem_matmul(m, E, E, X);
-    __syncthreads();
+    smem_matmul(m, E, E, X, tid, nt);
+    expm_sync<WARP>();
     for (int i = tid; i < mm; i += nt) E[i] = X[i];
-    __syncthreads();
+    expm_sync<WARP>();
   }
-  double2* out = Aexp + (size_t)w * mld * mld;
   for (int i = tid; i < mm; i += nt) out[(i % m) + (size_t)(i / m) * mld] = E[i];
+}
+
+__global__ void __launch_bounds__(128)
+    k_expm(int mld, int nslots, const TileInfo* __restrict__ tiles, const int* __restrict__ map,
+           const double2* __restrict__ Ahess, double2* __restrict__ Aexp, double dt,
+           int* __restrict__ err) {
+  extern __shared__ double2 sm[];
+  __shared__ double rowsum[SPC_MAX_M];
+  __shared__ int piv[SPC_MAX_M];
+  __shared__ int s_sh, p_sh;
+  const int w = blockIdx.x;
+  if (w >= nslots || map[w] < 0) return;
+  // working dimension m <= mld (the storage leading dimension)
+  const int m = tiles[w / SPC_LANES].m;
+  expm_one<false>(m, mld, Ahess + (size_t)w * mld * mld, Aexp + (size_t)w * mld * mld, dt, sm, rowsum, piv,
+                  &s_sh, &p_sh, threadIdx.x, blockDim.x, err);
+}
+
+// Four samples per 128-thread CTA, one warp each (m <= 16); dynamic shared
+// memory 4 x 5 mld^2 complex.
+__global__ void __launch_bounds__(128)
+    k_expm_warp(int mld, int nslots, const TileInfo* __restrict__ tiles, const int* __restrict__ map,
+                const double2* __restrict__ Ahess, double2* __restrict__ Aexp, double dt,
+                int* __restrict__ err) {
+  extern __shared__ double2 sm[];
+  __shared__ double rowsum[4][SPC_MAX_M];
+  __shared__ int piv[4][SPC_MAX_M];
+  __shared__ int s_sh[4], p_sh[4];
+  const int g = threadIdx.x >> 5;
+  const int w = blockIdx.x * 4 + g;
+  if (w >= nslots || map[w] < 0) return;
+  const int m = tiles[w / SPC_LANES].m;
+  expm_one<true>(m, mld, Ahess + (size_t)w * mld * mld, Aexp + (size_t)w * mld * mld, dt,
+                 sm + (size_t)g * 5 * mld * mld, rowsum[g], piv[g], &s_sh[g], &p_sh[g], threadIdx.x & 31, 32,
+                 err);
+}
+
+// Launch of the expm of every slot: packed warps for m <= 16.
+static void launch_expm(int m, int nslots, const TileInfo* tiles, const int* map, const double2* Ahess,
+                        double2* Aexp, double dt, int* err, cudaStream_t st) {
+  const size_t mm = (size_t)m * m;
+  if (m <= 16)
+    k_expm_warp<<<(nslots + 3) / 4, 128, sizeof(double2) * 20 * mm, st>>>(m, nslots, tiles, map, Ahess, Aexp,
+                                                                          dt, err);
+  else
+    k_expm<<<nslots, 128, sizeof(double2) * 5 * mm, st>>>(m, nslots, tiles, map, Ahess, Aexp, dt, err);
+}
+
+// Shared-memory limits of both expm kernels for Krylov dimension m.
+static cudaError_t set_expm_smem(int m) {
+  const size_t mm = (size_t)m * m;
+  cudaError_t e = cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(double2) * 5 * mm));
+  if (e == cudaSuccess && m <= 16)
+    e = cudaFuncSetAttribute(k_expm_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(double2) * 20 * mm));
+  return e;
 }
 
 // ---------------------------------------------------------------------------
@@ -1032,9 +1089,8 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   h->count_launch();
   CK(cudaGetLastError());
 
-  const size_t expm_smem = sizeof(double2) * 5 * mm;
   const size_t proj_smem = sizeof(double2) * 4 * m * PROJ_NC;
-  CK(cudaFuncSetAttribute(k_expm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expm_smem));
+  CK(set_expm_smem(m));
   // combinations per thread (instantiated counts) and threads per CTA
   const int maxc_need = (ncombo + 255) / 256;
   static const int kProjMaxc[] = {1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 16, 20, 24};
@@ -1236,7 +1292,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     for (size_t c = 0; c < map.size(); ++c)
       if (map[c] >= 0) zsum += tiles[c / SPC_LANES].n / 4;
     pe = h->prof.begin(st);
-    k_expm<<<nslots, 128, expm_smem, st>>>(m, nslots, d_tiles, d_map, d_A, d_E, dt, d_err);
+    launch_expm(m, nslots, d_tiles, d_map, d_A, d_E, dt, d_err, st);
     h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * list.size(),
                 32.0 * (double)mm * list.size());
     // projector splits: rows per split `rps` minimising the estimated time
