@@ -35,7 +35,10 @@ sys.path.insert(0, ROOT)
 
 from spin_dynamics_gb300 import workloads as W  # noqa: E402
 
-METRIC = "sample-steps/s at dim 55296 (trace sampling, complex128, M=512, m=30)"
+# The headline metric as named for this path; `value` is the plain (per-instance) trace
+# sampling at dim 55296, `adjoint` / `batched_adjoint` the gradient legs, `accuracy` the
+# |Delta Phi_S| check against the oracle on the CPU leg's vectors.
+METRIC = "sample-steps/s at dim 55296: batched+adjoint vs plain on GB300 at |\u0394\u03a6S|\u22641e-10"
 
 # DRAM traffic per k_spmm launch (dram__bytes_read.sum + dram__bytes_write.sum)
 # from one ncu capture at 64 sample columns (profiles/k_spmm_dim55296_M64_full.md:
@@ -78,6 +81,11 @@ def parse():
     return p.parse_args()
 
 
+def workload_name(args, M, m, tol) -> str:
+    return (f"large pair dim 55296 (A: 2x14N+5x1H, B: 14N+4x1H), anisotropic hyperfine, tilted B 0.05 mT, "
+            f"J 0.01 mT, D -0.4 mT; M={M}, m={m}, tol={tol:g}, dt 1 ns, window {args.window_ns:g} ns")
+
+
 def workload(args):
     sysp, B = W.large_pair()
     sim = W.large_sim(M=args.samples, t_end_ns=args.window_ns)
@@ -118,10 +126,29 @@ def cpu_leg(args, sysp, B, sim, threads):
                                 fast=True, threads=threads)
     el = time.perf_counter() - t0
     steps = int(round(sim.t_end / sim.dt))
+    cpu_leg.last = (zk, r)  # the vectors and oracle populations, for the accuracy check
     return {"value": ns * steps / el, "unit": "sample-steps/s", "cores": threads, "kind": "port",
             "sample": f"{ns} samples x {steps} dt steps of the same system (Krylov builds "
                       f"{int(r['n_builds'].sum())}), oracle -O3 native OpenMP, {el:.2f} s, "
                       f"CPU {cpu_model()}"}
+
+
+def accuracy_check(sysp, B, sim, zk, ref):
+    """|Delta Phi_S| and max |Delta P_S| between the GPU path and the oracle on
+    the CPU leg's vectors (same system, window, m, tol)."""
+    from spin_dynamics_gb300.dynamics import TraceSampler
+    from spin_dynamics_gb300.observables import Observables
+
+    with TraceSampler(0) as s:
+        s.build_h(sysp, B, "general")
+        got = s.trace_sampling(zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol)
+    cpu = Observables(ref["P_S"].copy(), ref["P_T0"].copy(), ref["P_Tp"].copy(), ref["P_Tm"].copy())
+    got.get_kinetics(sim.dt, sysp.kS, sysp.kT)
+    cpu.get_kinetics(sim.dt, sysp.kS, sysp.kT)
+    return {"max_abs_dPhi_S": float(np.max(np.abs(got.Phi_S - cpu.Phi_S))),
+            "max_abs_dP_S": float(np.max(np.abs(got.P_S - cpu.P_S))), "Phi_S": float(got.Phi_S[-1]),
+            "samples": int(zk.shape[0]), "bound": 1e-10,
+            "reference": "oracle (C++ restatement of the Fortran path) on the same vectors"}
 
 
 class Clocks:
@@ -546,8 +573,8 @@ def main():
         cb = dict(vals[0])
         cb["value"] = v
         line = dict(base, impl="reference", value=v, ms_per_step=None, scaling="weak",
-                    config={"workload": "large pair dim 55296, anisotropic, window "
-                            f"{args.window_ns:g} ns", "samples_per_step": cb["sample"]},
+                    config={"workload": workload_name(args, sim.N_samples, sim.N_krylov, sim.tol),
+                            "samples_per_step": cb["sample"]},
                     cpu_baseline=cb,
                     e2e={"value": v, "unit": "sample-steps/s", "h2d_bytes_per_step": 0,
                          "d2h_bytes_per_step": 0})
@@ -568,14 +595,13 @@ def main():
     ach_gbs = (by / max(nl, 1)) / avg_s / 1e9 if nl else None
     ach_tf = (fl / max(nl, 1)) / avg_s / 1e12 if nl else None
     cpu = None
+    accuracy = None
     if not args.no_cpu:
         cpu = cpu_leg(args, r["sysp"], r["B"], r["sim"], host_cores())
+        accuracy = accuracy_check(r["sysp"], r["B"], r["sim"], *cpu_leg.last)
     share = {k: round(v[0] / max(1e-9, sum(x[0] for x in prof.values())), 4) for k, v in prof.items()}
     line = dict(base, value=r["value"], ms_per_step=r["ms"], scaling="weak",
-                config={"workload": f"large pair dim 55296 (A: 2x14N+5x1H, B: 14N+4x1H), anisotropic "
-                                    f"hyperfine, tilted B 0.05 mT, J 0.01 mT, D -0.4 mT; M={r['M']}, "
-                                    f"m={r['sim'].N_krylov}, tol={r['sim'].tol:g}, dt 1 ns, window "
-                                    f"{args.window_ns:g} ns",
+                config={"workload": workload_name(args, r["M"], r["sim"].N_krylov, r["sim"].tol),
                         "samples": r["M"], "dt_steps_per_sample": r["steps_per_sample"],
                         "krylov_builds_per_step": r["builds"] / args.steps,
                         "krylov_method": args.method,
@@ -594,7 +620,8 @@ def main():
                                    "frac": (ach_tf * 1e12 / r["fp64_peak"]) if ach_tf else None,
                                    "peak_source": "measured DFMA probe (spc_fp64_peak)"}},
                 kernel_share=share, batched=r["batched"], adjoint=r["adjoint"],
-                batched_adjoint=r["batch_adjoint"], symmetry=r["symmetry"], cpu_baseline=cpu)
+                batched_adjoint=r["batch_adjoint"], symmetry=r["symmetry"], cpu_baseline=cpu,
+                accuracy=accuracy)
     print(json.dumps(line))
 
 

@@ -182,3 +182,45 @@ def test_two_rank_sharding_matches_single_process(tmp_path, oracle):
     got = np.load(out)
     for i, k in enumerate(("P_S", "P_T0", "P_Tp", "P_Tm")):
         assert np.max(np.abs(got[i] - ref[k])) < 1e-14
+
+
+def test_batch_marshalling_converts_each_system_once_and_keeps_fields():
+    import ctypes as C
+    from spin_dynamics_gb300 import workloads as W
+    from spin_dynamics_gb300.dynamics import make_system, make_systems
+    a, b = W.small_pair(), W.notebook_pair()
+    systems = [a, a, b, a]
+    fields = [0.05, np.array([0.01, 0.02, 0.03]), 0.1, np.array([0.0, 0.0, -0.2])]
+    arr, keep = make_systems(systems, fields)
+    assert len(keep[0]) == 2  # one template per distinct system object
+    for st, sy, f in zip(arr, systems, fields):
+        ref, _ = make_system(sy, f)
+        for name, _t in ref._fields_:
+            x, y = getattr(st, name), getattr(ref, name)
+            if name in ("mult1", "mult2", "A1", "A2", "gamma1", "gamma2"):
+                n = 9 * (ref.n_nuc1 if name == "A1" else ref.n_nuc2) if name in ("A1", "A2") else \
+                    (ref.n_nuc1 if name.endswith("1") else ref.n_nuc2)
+                if bool(x) != bool(y):
+                    raise AssertionError(name)
+                if x:
+                    assert [x[i] for i in range(n)] == [y[i] for i in range(n)], name
+            elif name in ("B", "D"):
+                assert list(x) == list(y), name
+            else:
+                assert x == y, name
+
+
+def test_torch_parameter_vector_round_trip():
+    torch = pytest.importorskip("torch")
+    from spin_dynamics_gb300 import workloads as W
+    from spin_dynamics_gb300.torch_ops import pack_params, unpack_params
+    s, B = W.large_pair()
+    v = pack_params(s, B)
+    assert v.dtype == torch.float64 and v.numel() == 15 + 9 * 12
+    s2, B2 = unpack_params(s, v.numpy())
+    assert np.array_equal(B2, B)
+    for a1, a2 in zip(s.e1.A + s.e2.A, s2.e1.A + s2.e2.A):
+        assert np.array_equal(np.asarray(a1), a2)
+    assert np.array_equal(np.asarray(s.D), s2.D) and s2.J == s.J and s2.kS == s.kS
+    with pytest.raises(ValueError):
+        unpack_params(s, v.numpy()[:-1])
