@@ -535,12 +535,18 @@ def adjoint_leg(args, sampler, plain_value):
         g, t_grad = timed(grad)
         st = sampler.stats()
         y, t_fwd = timed(fwd)
+        # the same with the checkpoint spacing chosen by device memory (fewest recomputed steps)
+        _, t_auto = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=args.adjoint_quad,
+                                                         checkpoint_every=0))
+        kept_auto = bool(sampler.stats()["rounds"])
     finally:
         sampler.set_krylov(args.method)
     steps = st["sample_steps"] // M
     work = M * steps
     return {"value": work / t_grad, "unit": "sample-steps/s", "seconds": t_grad,
             "stepwise_forward_value": work / t_fwd, "cost_vs_stepwise_forward": t_grad / t_fwd,
+            "cost_vs_stepwise_forward_memory_sized_checkpoints": t_auto / t_fwd,
+            "memory_sized_node_states_kept": kept_auto,
             "cost_vs_plain_forward": t_grad / (work / plain_value),
             "params": int(g.raw.size), "samples": M, "dt_steps": int(steps), "krylov": m,
             "krylov_method": method, "quadrature_nodes": args.adjoint_quad,

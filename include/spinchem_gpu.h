@@ -233,9 +233,9 @@ int spc_yield_gradient_size(const spc_system* sys);
  *   n_quad           Gauss-Legendre nodes per step for the derivative of
  *                    exp(-i H dt) (1..16; 6 gives ~1e-8 relative error at
  *                    ||H|| dt ~ 5)
- *   checkpoint_every forward states kept every this many steps (0 = the
- *                    largest spacing that fits in device memory: the fewest
- *                    recomputed steps)
+ *   checkpoint_every forward states kept every this many steps (0 = among
+ *                    the spacings that fit in device memory, the one that
+ *                    recomputes the fewest steps)
  *   yields           2 doubles: Phi_S, Phi_T
  *   grad             NULL: yields only (the forward sweep, one Krylov build
  *                    per sample and step); else spc_yield_gradient_size(sys) doubles:

@@ -343,8 +343,18 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
       return sb * ((double)m + 4.0 + (nsteps / k + 1) + k + 1.0 + (keep ? (double)k * nq : (double)nq));
     };
     if (K == 0) {
-      for (int k = nsteps; k >= 1 && K == 0; --k)
-        if (need(k, true) <= avail) K = k;
+      // among the spacings whose states fit, the one that recomputes the
+      // fewest steps (all but the last segment are recomputed), the larger
+      // on a tie
+      int64_t best = -1;
+      for (int k = nsteps; k >= 1; --k) {
+        if (need(k, true) > avail) continue;
+        const int64_t recomputed = (int64_t)((nsteps - 1) / k) * k;
+        if (best < 0 || recomputed < best) {
+          best = recomputed;
+          K = k;
+        }
+      }
       if (K)
         cache = true;
       else

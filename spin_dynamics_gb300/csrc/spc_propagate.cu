@@ -1091,16 +1091,24 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
 
   const size_t proj_smem = sizeof(double2) * 4 * m * PROJ_NC;
   CK(set_expm_smem(m));
-  // combinations per thread (instantiated counts) and threads per CTA
-  const int maxc_need = (ncombo + 255) / 256;
+  // combinations per thread (an instantiated count) and threads per CTA (a
+  // multiple of 32, at most 256): the pair with the fewest padded slots, the
+  // smaller count on a tie (every slot, used or not, issues its DFMAs)
   static const int kProjMaxc[] = {1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 16, 20, 24};
-  int maxc = 24;
-  for (int c : kProjMaxc)
-    if (c >= maxc_need) {
-      maxc = c;
-      break;
+  int maxc = 24, proj_threads = 256;
+  {
+    int64_t best = -1;
+    for (int c : kProjMaxc) {
+      const int th = ((ncombo + c - 1) / c + 31) / 32 * 32;
+      if (th > 256) continue;
+      const int64_t slots = (int64_t)c * th;
+      if (best < 0 || slots < best) {
+        best = slots;
+        maxc = c;
+        proj_threads = th;
+      }
     }
-  const int proj_threads = std::min(256, ((ncombo + maxc - 1) / maxc + 31) / 32 * 32);
+  }
   const void* proj_fn = nullptr;
   switch (maxc) {
     case 1: proj_fn = (const void*)k_proj<1>; break;
