@@ -74,7 +74,8 @@ def build_cli() -> str:
                                                            os.path.getmtime(LIB)):
         return CLI
     cxx = shutil.which(os.environ.get("CXX", "g++")) or "g++"
-    cmd = [cxx, "-O2", "-std=c++17", CLI_SRC, "-o", CLI, "-L", OUT, "-lspinchem_gpu",
+    # no FMA contraction: the weighted block sums round as the Python driver's
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", CLI_SRC, "-o", CLI, "-L", OUT, "-lspinchem_gpu",
            "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -19,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <limits>
 #include <map>
 #include <sstream>
 #include <string>
@@ -296,6 +297,386 @@ Result run_dynamics(spc_handle* h, const Sys& sys, const Sim& sim, double B) {
   return r;
 }
 
+// ---------------------------------------------------------------------------
+// symmetry_dynamics (src/symmetry.f90:16-139) with the moment matching of
+// src/moments.f90:15-240: equivalent spin-1/2 nuclei (1H) of each radical form
+// groups; every combination of the groups' total spins is a block (an
+// ordinary radical pair whose "nuclei" are the groups, multiplicity 2I+1),
+// propagated together through the batch ABI, weighted by
+// prod C(n, (n+k-1)/2) 2k/(n+k+1) * Z_block / Z and summed.
+
+const double GAMMA_1H = 0.26752218708;   // src/spinsys.f90:18
+const double GAMMA_14N = 0.0193297792;   // src/spinsys.f90:19
+
+// Eigenvalues (ascending) and eigenvectors (columns of V, row-major n x n) of
+// a small symmetric matrix by cyclic Jacobi rotations.
+void jacobi_eig(int n, std::vector<double> A, std::vector<double>& w, std::vector<double>& V) {
+  V.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) V[i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        tot += A[i * n + j] * A[i * n + j];
+        if (i != j) off += A[i * n + j] * A[i * n + j];
+      }
+    if (off <= 1e-32 * tot || off == 0.0) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[p * n + q];
+        if (apq == 0.0) continue;
+        // rotation angle zeroing A[p][q]: tan(2 phi) = 2 apq / (aqq - app)
+        const double tau = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+        const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+        const double c = 1.0 / std::sqrt(1.0 + t * t), sn = t * c;
+        for (int k = 0; k < n; ++k) {  // A <- A R (columns p, q)
+          const double akp = A[k * n + p], akq = A[k * n + q];
+          A[k * n + p] = c * akp - sn * akq;
+          A[k * n + q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // A <- R^T A (rows p, q)
+          const double apk = A[p * n + k], aqk = A[q * n + k];
+          A[p * n + k] = c * apk - sn * aqk;
+          A[q * n + k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = V[k * n + p], vkq = V[k * n + q];
+          V[k * n + p] = c * vkp - sn * vkq;
+          V[k * n + q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return A[a * n + a] < A[b * n + b]; });
+  w.resize(n);
+  std::vector<double> Vs((size_t)n * n);
+  for (int c = 0; c < n; ++c) {
+    w[c] = A[idx[c] * n + idx[c]];
+    for (int r = 0; r < n; ++r) Vs[r * n + c] = V[r * n + idx[c]];
+  }
+  V.swap(Vs);
+}
+
+// quad_rule (src/moments.f90:97-158): the N-point Gauss rule of the discrete
+// measure (W_init, X_init) by Stieltjes/Lanczos; nodes ascending.
+void quad_rule(const std::vector<double>& Wi, const std::vector<double>& Xi, int N, std::vector<double>& W,
+               std::vector<double>& X) {
+  const size_t L = Xi.size();
+  std::vector<double> q(L), P(L * N), w(N), x(N);
+  for (size_t i = 0; i < L; ++i) q[i] = std::sqrt(Wi[i]);
+  for (int k = 0; k < N; ++k) {
+    double q2 = 0.0;
+    for (double v : q) q2 += v * v;
+    q2 = std::sqrt(q2);
+    if (q2 == 0.0) stop("quad_rule 1");
+    for (size_t i = 0; i < L; ++i) P[i * N + k] = q[i] / q2;
+    for (size_t i = 0; i < L; ++i) q[i] = Xi[i] * P[i * N + k];
+    for (int j = k; j >= 0; --j) {
+      double pq = 0.0;
+      for (size_t i = 0; i < L; ++i) pq += P[i * N + j] * q[i];
+      if (j == k) {
+        w[k] = q2;
+        x[k] = pq;
+      }
+      for (size_t i = 0; i < L; ++i) q[i] -= pq * P[i * N + j];
+    }
+  }
+  std::vector<double> T((size_t)N * N, 0.0), V;
+  for (int i = 0; i < N; ++i) {
+    T[i * N + i] = x[i];
+    if (i + 1 < N) T[i * N + i + 1] = T[(i + 1) * N + i] = w[i + 1];  // cshift(W, 1)
+  }
+  jacobi_eig(N, T, X, V);
+  W.resize(N);
+  for (int k = 0; k < N; ++k) W[k] = (w[0] * V[k]) * (w[0] * V[k]);
+}
+
+// newton (src/moments.f90:182-240): sum_j n_j a_j^k = sum_j w_j aw_j^k, k = 1..M.
+int newton(const std::vector<double>& aw, const std::vector<double>& wb, std::vector<double>& a,
+           const std::vector<double>& nb, int M) {
+  double dap = 0.0;
+  for (int it = 1; it <= 30; ++it) {
+    std::vector<double> f(M), g((size_t)M * M);
+    for (int k = 1; k <= M; ++k) {
+      double s1 = 0.0, s2 = 0.0;
+      for (int j = 0; j < M; ++j) {
+        s1 += nb[j] * std::pow(a[j], k);
+        s2 += wb[j] * std::pow(aw[j], k);
+      }
+      f[k - 1] = s1 - s2;
+      for (int j = 0; j < M; ++j) g[(k - 1) * M + j] = k * nb[j] * std::pow(a[j], k - 1);
+    }
+    // g q = f by Gaussian elimination with partial pivoting
+    std::vector<double> qv = f;
+    for (int c = 0; c < M; ++c) {
+      int pr = c;
+      for (int r = c + 1; r < M; ++r)
+        if (std::fabs(g[r * M + c]) > std::fabs(g[pr * M + c])) pr = r;
+      if (g[pr * M + c] == 0.0) return 1;
+      if (pr != c) {
+        for (int j = 0; j < M; ++j) std::swap(g[c * M + j], g[pr * M + j]);
+        std::swap(qv[c], qv[pr]);
+      }
+      for (int r = c + 1; r < M; ++r) {
+        const double l = g[r * M + c] / g[c * M + c];
+        for (int j = c; j < M; ++j) g[r * M + j] -= l * g[c * M + j];
+        qv[r] -= l * qv[c];
+      }
+    }
+    for (int c = M - 1; c >= 0; --c) {
+      double acc = qv[c];
+      for (int j = c + 1; j < M; ++j) acc -= g[c * M + j] * qv[j];
+      qv[c] = acc / g[c * M + c];
+    }
+    double a_abs = 0.0, d_abs = 0.0;
+    for (int j = 0; j < M; ++j) {
+      a_abs += std::fabs(a[j]);
+      d_abs += std::fabs(qv[j]);
+    }
+    std::vector<double> a_old = a;
+    for (int j = 0; j < M; ++j) a[j] -= qv[j];
+    const double da = d_abs / a_abs;
+    if (da > 1.0) return 1;
+    if (1.0 + da == 1.0) return 0;
+    if (it > 1 && da >= dap) {
+      a = a_old;
+      return 0;
+    }
+    dap = da;
+  }
+  return 2;
+}
+
+// shrink (src/moments.f90:15-95): M groups (couplings, sizes) matching the
+// moments of the couplings a.
+void shrink(const std::vector<double>& a, int M, std::vector<double>& a_bar, std::vector<int>& n_bar) {
+  const int N = (int)a.size();
+  if (M >= N) stop("Error: Symetry reduction requires M<N");
+  std::vector<double> wb, aw;
+  quad_rule(std::vector<double>(N, 1.0), a, M, wb, aw);
+  std::vector<int> nfloor(M);
+  int fsum = 0;
+  for (int i = 0; i < M; ++i) {
+    nfloor[i] = (int)wb[i];
+    fsum += nfloor[i];
+  }
+  const int ndiff = N - fsum;
+  double dmom = std::numeric_limits<double>::max();
+  bool found = false;
+  for (int ib = 0; ib < (1 << M); ++ib) {
+    if (__builtin_popcount((unsigned)ib) != ndiff) continue;
+    std::vector<double> nt(M), at = aw;
+    for (int i = 0; i < M; ++i) nt[i] = nfloor[i] + ((ib >> i) & 1);
+    if (newton(aw, wb, at, nt, M) != 0) continue;
+    double emom = 0.0;
+    for (int k = 1; k <= M + 1; ++k) {
+      double s1 = 0.0, s2 = 0.0;
+      for (double v : at) s1 += std::pow(v, k);
+      for (double v : a) s2 += std::pow(v, k);
+      emom += std::fabs(s1 - s2);
+    }
+    if (emom < dmom) {
+      dmom = emom;
+      a_bar = at;
+      n_bar.assign(M, 0);
+      for (int i = 0; i < M; ++i) n_bar[i] = (int)nt[i];
+      found = true;
+    }
+  }
+  if (!found) stop("Error: moment matching found no integer group sizes");
+}
+
+struct Groups {
+  std::vector<double> a;  // group couplings
+  std::vector<int> n;     // group sizes
+  std::vector<int> other; // explicit nuclei (indices)
+};
+
+double a_iso(const Electron& e, int i) {
+  const double* A = &e.A[9 * (size_t)i];
+  return ((A[0] + A[4]) + A[8]) / 3.0;
+}
+
+Groups radical_groups(const Electron& e, int M) {
+  Groups G;
+  std::vector<double> a;
+  for (size_t i = 0; i < e.gI.size(); ++i) {
+    if (e.gI[i] == 2)
+      a.push_back(a_iso(e, (int)i));
+    else
+      G.other.push_back((int)i);
+  }
+  if (a.empty() || M == 0) return G;
+  std::vector<double> vals = a;
+  std::sort(vals.begin(), vals.end());
+  vals.erase(std::unique(vals.begin(), vals.end()), vals.end());
+  if ((int)vals.size() == M) {  // exactly M distinct couplings: exact groups
+    for (double v : vals) {
+      G.a.push_back(v);
+      G.n.push_back((int)std::count(a.begin(), a.end(), v));
+    }
+  } else {
+    shrink(a, M, G.a, G.n);
+  }
+  return G;
+}
+
+int64_t n_choose_r(int64_t n, int64_t r) {
+  if (r < 0 || r > n) return 0;
+  int64_t c = 1;
+  for (int64_t i = 1; i <= r; ++i) c = c * (n - r + i) / i;
+  return c;
+}
+
+struct Block {
+  double w;
+  Electron e1, e2;          // the block's radicals: groups then explicit nuclei
+  std::vector<double> gam1, gam2;
+  long Z;
+};
+
+std::vector<Block> blocks(const Sys& sys, int M1, int M2) {
+  const Groups G1 = radical_groups(sys.e1, M1), G2 = radical_groups(sys.e2, M2);
+  std::vector<int> n = G1.n;
+  n.insert(n.end(), G2.n.begin(), G2.n.end());
+  // every combination of group multiplicities k = 2j + 1 + n mod 2, the
+  // first group fastest (cartesian_product, src/symmetry.f90:171-208)
+  std::vector<std::vector<int>> opts(n.size());
+  for (size_t i = 0; i < n.size(); ++i)
+    for (int j = 0; j <= n[i] / 2; ++j) opts[i].push_back(2 * j + 1 + n[i] % 2);
+  std::vector<std::vector<int>> combos;
+  std::vector<size_t> pos(n.size(), 0);
+  while (true) {
+    std::vector<int> c(n.size());
+    for (size_t i = 0; i < n.size(); ++i) c[i] = opts[i][pos[i]];
+    combos.push_back(c);
+    size_t i = 0;
+    while (i < n.size() && ++pos[i] == opts[i].size()) pos[i++] = 0;
+    if (i == n.size()) break;
+  }
+  // stable order by block dimension (sort_col_prod, src/utils.f90:25-50)
+  std::vector<int64_t> zc(combos.size(), 1);
+  for (size_t c = 0; c < combos.size(); ++c)
+    for (int k : combos[c]) zc[c] *= k;
+  std::vector<size_t> order(combos.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return zc[a] < zc[b]; });
+  int64_t z_expl = 1, z_full = sys.e1.Z() * sys.e2.Z();
+  for (int i : G1.other) z_expl *= sys.e1.gI[i];
+  for (int i : G2.other) z_expl *= sys.e2.gI[i];
+  auto default_gamma = [](int g) { return g == 3 ? GAMMA_14N : GAMMA_1H; };
+  std::vector<Block> out;
+  for (size_t oi : order) {
+    const std::vector<int>& K = combos[oi];
+    int64_t w_ij = 1;
+    for (size_t i = 0; i < n.size(); ++i) {
+      const int64_t ni = n[i], ki = K[i];
+      w_ij = w_ij * (n_choose_r(ni, (ni + ki - 1) / 2) * (2 * ki) / (ni + ki + 1));
+    }
+    Block b;
+    const int64_t Zb = zc[oi] * z_expl;
+    b.w = (double)(w_ij * Zb) / (double)z_full;
+    b.Z = (long)Zb;
+    auto radical = [&](const Electron& e, const Groups& G, size_t k0, Electron& re, std::vector<double>& gam) {
+      re.g = e.g;
+      for (size_t i = 0; i < G.a.size(); ++i) {
+        re.gI.push_back(K[k0 + i]);
+        const double a9[9] = {G.a[i], 0, 0, 0, G.a[i], 0, 0, 0, G.a[i]};
+        re.A.insert(re.A.end(), a9, a9 + 9);
+        gam.push_back(GAMMA_1H);
+      }
+      for (int i : G.other) {
+        re.gI.push_back(e.gI[i]);
+        re.A.insert(re.A.end(), e.A.begin() + 9 * (size_t)i, e.A.begin() + 9 * (size_t)i + 9);
+        gam.push_back(default_gamma(e.gI[i]));
+      }
+    };
+    radical(sys.e1, G1, 0, b.e1, b.gam1);
+    radical(sys.e2, G2, G1.a.size(), b.e2, b.gam2);
+    out.push_back(std::move(b));
+  }
+  return out;
+}
+
+struct Observed {
+  std::vector<double> PS, PT0, PTp, PTm;
+};
+
+// symmetrised_dynamics for one field: every block with weight >= block_tol
+// (from the restart block on) in one batched propagation, weighted sum in
+// block order, yields, output files.
+void symmetrised_dynamics(spc_handle* h, const Sys& sys, const Sim& sim, double B, const std::string& folder) {
+  std::vector<Block> bl = blocks(sys, sim.M1, sim.M2);
+  std::vector<uint64_t> seeds(std::max<size_t>(1, 2 * bl.size()));
+  check(spc_rng_stream(sim.seed[0], sim.seed[1], (int)(2 * bl.size()), seeds.data()));
+  const int start = sim.isRestart ? sim.restart : 1;
+  std::vector<size_t> sel;
+  for (size_t i = 0; i < bl.size(); ++i)
+    if ((int)i + 1 >= start && bl[i].w >= sim.block_tol) sel.push_back(i);
+  int which = sim.init_state == "singlet" ? 0 : sim.init_state == "T0" ? 1 : sim.init_state == "Tp" ? 2
+            : sim.init_state == "Tm" ? 3 : -1;
+  if (which < 0) stop("Error: Invalid initial radical pair state entered.");
+  double theta[8], pop[4];
+  check(spc_init_el_state(which, theta, pop));
+  const int T = spc_num_time_points(sim.dt, sim.t_end);
+  if (T < 1) stop("Error: Propagation timestep is missing");
+  Observed res{std::vector<double>(T, 0.0), std::vector<double>(T, 0.0), std::vector<double>(T, 0.0),
+               std::vector<double>(T, 0.0)};
+  if (!sel.empty()) {
+    std::vector<spc_system> systems(sel.size());
+    std::vector<int> M(sel.size(), sim.N_samples);
+    std::vector<double> zk;
+    for (size_t j = 0; j < sel.size(); ++j) {
+      const Block& b = bl[sel[j]];
+      spc_system& s = systems[j];
+      s = spc_system{};
+      s.n_nuc1 = (int)b.e1.gI.size();
+      s.n_nuc2 = (int)b.e2.gI.size();
+      s.mult1 = b.e1.gI.data();
+      s.mult2 = b.e2.gI.data();
+      s.A1 = b.e1.A.data();
+      s.A2 = b.e2.A.data();
+      s.gamma1 = b.gam1.data();
+      s.gamma2 = b.gam2.data();
+      s.B[2] = B;
+      s.J = sys.J;
+      std::memcpy(s.D, sys.D, sizeof(s.D));
+      s.kS = sys.kS;
+      s.kT = sys.kT;
+      const size_t off = zk.size();
+      zk.resize(off + 2 * (size_t)b.Z * sim.N_samples);
+      const size_t i = sel[j];
+      check(spc_seeded_samples((int64_t)seeds[2 * i], (int64_t)seeds[2 * i + 1], (int)b.Z, sim.N_samples, 0,
+                               zk.data() + off));
+    }
+    check(spc_build_h_batch(h, (int)systems.size(), systems.data(), SPC_H_REFERENCE));
+    std::vector<double> out(sel.size() * 4 * (size_t)T);
+    check(spc_trace_sampling_batch(h, (int)sel.size(), nullptr, M.data(), theta, pop, zk.data(), sim.dt,
+                                   sim.t_end, sim.N_krylov, sim.tol, out.data(), T));
+    for (size_t j = 0; j < sel.size(); ++j) {
+      const double w = bl[sel[j]].w;
+      const double* o = &out[j * 4 * (size_t)T];
+      for (int t = 0; t < T; ++t) {  // res%scale(w) then res%update
+        res.PS[t] += o[t] * w;
+        res.PT0[t] += o[T + t] * w;
+        res.PTp[t] += o[2 * T + t] * w;
+        res.PTm[t] += o[3 * T + t] * w;
+      }
+    }
+  }
+  std::vector<double> phiS(T / 2), phiT(T / 2), iden(T);
+  check(spc_kinetics(T, res.PS.data(), res.PT0.data(), res.PTp.data(), res.PTm.data(), sim.dt, sys.kS, sys.kT,
+                     phiS.data(), phiT.data(), iden.data()));
+  write_data(res.PS, folder, "S_prob.data");
+  write_data(res.PTp, folder, "Tp_prob.data");
+  write_data(res.PT0, folder, "T0_prob.data");
+  write_data(res.PTm, folder, "Tm_prob.data");
+  write_data(iden, folder, "total_prob.data");
+  write_data(phiS, folder, "S_yield.data");
+  write_data(phiT, folder, "T_yield.data");
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -326,8 +707,7 @@ int main(int argc, char** argv) {
       write_data(r.PTm, folder, "Tm_prob.data");
     } else if (sim.type == "symmetry_dynamics") {
       std::printf(" %g\n", B);
-      stop("Error: symmetry_dynamics runs through the Python layer "
-           "(python -m spin_dynamics_gb300 input.ini)");
+      symmetrised_dynamics(h, sys, sim, B, folder);
     } else if (sim.type == "semi_classical") {
       std::printf(" method not yet implemented\n");
     } else {
