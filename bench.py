@@ -78,6 +78,8 @@ def parse():
     p.add_argument("--adjoint-window-ns", type=float, default=20.0)
     p.add_argument("--adjoint-checkpoint", type=int, default=10)
     p.add_argument("--adjoint-quad", type=int, default=6)
+    p.add_argument("--adjoint-krylov", type=int, default=16,
+                   help="Krylov dimension of the stepwise model (one basis per dt step)")
     return p.parse_args()
 
 
@@ -511,7 +513,7 @@ def adjoint_leg(args, sampler, plain_value):
     sysp, B = W.large_pair()
     dt = 1.0 * 176.08596 / 1000
     t_end = args.adjoint_window_ns * 176.08596 / 1000
-    M, m = args.adjoint_samples, args.krylov
+    M, m = args.adjoint_samples, args.adjoint_krylov
     zk = W.random_phase_samples(sysp.Z, M, seed=11)
     method = "lanczos" if args.method in ("auto", "lanczos") and sysp.kS == sysp.kT else "mgs"
     sampler.set_krylov(method)
@@ -539,6 +541,8 @@ def adjoint_leg(args, sampler, plain_value):
         _, t_auto = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=args.adjoint_quad,
                                                          checkpoint_every=0))
         kept_auto = bool(sampler.stats()["rounds"])
+        # the stepwise model's accuracy at this m: the same forward at m = 30
+        y30 = sampler.stepwise_yields(sysp, B, zk, dt, t_end, 30)
     finally:
         sampler.set_krylov(args.method)
     steps = st["sample_steps"] // M
@@ -552,7 +556,8 @@ def adjoint_leg(args, sampler, plain_value):
             "krylov_method": method, "quadrature_nodes": args.adjoint_quad,
             "checkpoint_every": args.adjoint_checkpoint, "node_states_kept": bool(st["rounds"]),
             "krylov_builds": int(st["krylov_builds"]), "kernel_launches": int(st["kernel_launches"]),
-            "Phi_S": g.Phi_S, "Phi_S_forward_only": y[0], "kernel_breakdown": breakdown,
+            "Phi_S": g.Phi_S, "Phi_S_forward_only": y[0], "Phi_S_stepwise_m30": y30[0],
+            "abs_dPhi_S_vs_m30": abs(y[0] - y30[0]), "kernel_breakdown": breakdown,
             "workload": "large pair dim 55296 (anisotropic), gradient of Phi_S over B, J, D, kS, kT "
                         "and every hyperfine tensor element; h2d of the sample vectors inside"}
 
