@@ -226,11 +226,14 @@ def run_ours(args, rank, world, local_rank):
     steps_per_sample = int(round(sim.t_end / sim.dt))
     sampler = TraceSampler(local_rank)
     sampler.set_krylov(args.method)
-    stream = torch.cuda.current_stream()
-    sampler.set_stream(stream.cuda_stream)
     zk_host = W.random_phase_samples(sysp.Z, M, seed=7 + rank)
     zk_dev = torch.from_numpy(zk_host).to(f"cuda:{local_rank}")
     out_dev = torch.empty(4 * T, dtype=torch.float64, device=f"cuda:{local_rank}")
+    # one stream for the library's launches and the timing events
+    stream = torch.cuda.Stream(f"cuda:{local_rank}")
+    stream.wait_stream(torch.cuda.current_stream())
+    torch.cuda.set_stream(stream)
+    sampler.set_stream(stream.cuda_stream)
 
     def step_device():
         sampler.build_h(sysp, B, "general")

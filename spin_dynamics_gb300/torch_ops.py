@@ -1,4 +1,5 @@
-"""torch.autograd binding of the radical-pair yields.
+"""PyTorch binding: trace sampling on CUDA tensors, and a torch.autograd
+binding of the radical-pair yields.
 
 `yield_objective(params, ...)` returns wS*Phi_S + wT*Phi_T of the stepwise
 trace-sampling propagation as a 0-d float64 tensor whose backward is the
@@ -74,4 +75,64 @@ def yield_objective(params: torch.Tensor, sampler: TraceSampler, template: SysPa
     return _Yield.apply(params, sampler, template, zkets, dt, t_end, m, n_quad, checkpoint_every, wS, wT)
 
 
-__all__ = ["pack_params", "unpack_params", "yield_objective"]
+def _device_samples(zkets: torch.Tensor) -> torch.Tensor:
+    if not (isinstance(zkets, torch.Tensor) and zkets.is_cuda and zkets.dtype == torch.complex128):
+        raise TypeError("zkets must be a CUDA complex128 tensor (samples x Z)")
+    return zkets.contiguous()
+
+
+_SIDE = {}
+
+
+def _ordered_call(sampler: TraceSampler, device, tensors, fn) -> None:
+    """Run fn (library launches) on a torch stream of this module that waits
+    for the caller's current stream first and that the caller's stream waits
+    for afterwards, so the call is ordered like a torch op on any stream
+    (including the legacy default stream, which the library's own
+    non-blocking stream would not be ordered against)."""
+    cur = torch.cuda.current_stream(device)
+    side = _SIDE.get(device)
+    if side is None:
+        side = _SIDE[device] = torch.cuda.Stream(device)
+    side.wait_stream(cur)
+    sampler.set_stream(side.cuda_stream)
+    fn()
+    for t in tensors:
+        t.record_stream(side)
+    cur.wait_stream(side)
+
+
+def trace_sampling(sampler: TraceSampler, zkets: torch.Tensor, dt: float, t_end: float, m: int, tol: float,
+                   init_state: str = "singlet") -> torch.Tensor:
+    """Trace sampling of the handle's Hamiltonian on device-resident sample
+    vectors (samples x Z, complex128, CUDA): returns a (4, T) float64 tensor
+    on the same device, rows P_S, P_T0, P_Tp, P_Tm, ordered after the
+    caller's current stream's earlier work and before its later work
+    (spc_trace_sampling_device); no host copies."""
+    from .dynamics import num_time_points
+    zk = _device_samples(zkets)
+    T = num_time_points(dt, t_end)
+    out = torch.empty(4 * T, dtype=torch.float64, device=zk.device)
+    _ordered_call(sampler, zk.device, (zk, out), lambda: sampler.trace_sampling_device(
+        zk.data_ptr(), zk.shape[0], dt, t_end, m, tol, out.data_ptr(), init_state))
+    return out.view(4, T)
+
+
+def trace_sampling_batch(sampler: TraceSampler, zkets_list, dt: float, t_end: float, m: int, tol: float,
+                         init_state: str = "singlet", job_sys=None) -> torch.Tensor:
+    """Batched trace sampling of the handle's batch store (build it with
+    TraceSampler.build_h_batch) on device-resident sample tensors, one per
+    job: returns a (jobs, 4, T) float64 tensor on the same device, ordered
+    like trace_sampling (spc_trace_sampling_batch_device)."""
+    from .dynamics import num_time_points
+    zks = [_device_samples(z) for z in zkets_list]
+    dev = zks[0].device
+    flat = torch.cat([z.reshape(-1) for z in zks])
+    T = num_time_points(dt, t_end)
+    out = torch.empty(len(zks) * 4 * T, dtype=torch.float64, device=dev)
+    _ordered_call(sampler, dev, (flat, out), lambda: sampler.trace_sampling_batch_device(
+        flat.data_ptr(), [z.shape[0] for z in zks], dt, t_end, m, tol, out.data_ptr(), init_state, job_sys))
+    return out.view(len(zks), 4, T)
+
+
+__all__ = ["pack_params", "unpack_params", "yield_objective", "trace_sampling", "trace_sampling_batch"]

@@ -129,3 +129,28 @@ def test_autotuned_krylov_dimension(sampler, oracle):
     for s, f, zk, g in zip(systems, fields, zks, got):
         rp, col, val = iso_csr(oracle, s, f)
         _check(g, oracle.trace_sampling(rp, col, val, zk, DT, 15 * DT, best, 1e-6))
+
+
+def test_torch_tensor_entry_points(sampler, oracle):
+    """torch_ops.trace_sampling / trace_sampling_batch on CUDA tensors give
+    the host path's populations."""
+    import torch
+    from spin_dynamics_gb300 import torch_ops
+    s = W.small_pair()
+    zk = W.random_phase_samples(s.Z, 9, seed=5)
+    sampler.build_h(s, 0.05, "reference")
+    host = sampler.trace_sampling(zk, DT, 20 * DT, 10, 1e-6)
+    dev = torch_ops.trace_sampling(sampler, torch.from_numpy(zk).cuda(), DT, 20 * DT, 10, 1e-6)
+    torch.cuda.synchronize()
+    assert dev.is_cuda and dev.shape == (4, len(host.P_S))
+    assert np.array_equal(dev.cpu().numpy()[0], host.P_S) and np.array_equal(dev.cpu().numpy()[3], host.P_Tm)
+    nb = W.notebook_pair()
+    zb = W.random_phase_samples(nb.Z, 4, seed=6)
+    sampler.build_h_batch([nb, s], [0.1, 0.05], "reference")
+    got = torch_ops.trace_sampling_batch(sampler, [torch.from_numpy(zb).cuda(), torch.from_numpy(zk).cuda()],
+                                         DT, 20 * DT, 10, 1e-6)
+    ref = sampler.trace_sampling_batch([zb, zk], DT, 20 * DT, 10, 1e-6)
+    for j in range(2):
+        assert np.array_equal(got[j].cpu().numpy()[0], ref[j].P_S)
+    with pytest.raises(TypeError):
+        torch_ops.trace_sampling(sampler, torch.from_numpy(zk), DT, 20 * DT, 10, 1e-6)
