@@ -242,3 +242,40 @@ def test_field_gradient_of_a_spin2_group(sampler):
     assert abs(got.Phi_S - phi(v0)) <= 1e-12
     err = np.abs(got.raw[:15] - ref)
     assert np.max(err) <= 2e-7 * np.max(np.abs(ref)), (np.argmax(err), got.raw[:15], ref)
+
+
+def test_gradient_argument_and_capacity_errors(sampler):
+    """Errors come back as status codes with messages: bad arguments, a
+    multiplicity the full gradient set does not take, Lanczos with unequal
+    rates, and a request larger than device memory (refused by the memory
+    plan before anything is allocated or launched)."""
+    from spin_dynamics_gb300._native import SpcError
+    from spin_dynamics_gb300.spinsys import GAMMA_1H
+    s = aniso_pair([2], [2], seed=1, kS=0.02, kT=0.01)
+    zk = W.random_phase_samples(s.Z, 3, seed=1)
+    for kw in ({"m": 0}, {"m": 49}, {"n_quad": 0}, {"n_quad": 17}, {"checkpoint_every": -1}):
+        args = dict(m=8, n_quad=4, checkpoint_every=0)
+        args.update(kw)
+        with pytest.raises(SpcError):
+            sampler.yield_gradient(s, [0, 0, 0.1], zk, DT, 6 * DT, args["m"], n_quad=args["n_quad"],
+                                   checkpoint_every=args["checkpoint_every"])
+    with pytest.raises(SpcError, match="must be positive"):
+        sampler.yield_gradient(s, [0, 0, 0.1], zk, -DT, 6 * DT, 8)
+    s5 = SysParam(e1=Electron(g_I=[5], A=[np.eye(3) * 0.4], gamma_I=[GAMMA_1H]),
+                  e2=Electron(g_I=[2], A=[np.eye(3) * 0.3]), kS=0.02, kT=0.02)
+    z5 = W.random_phase_samples(s5.Z, 2, seed=2)
+    with pytest.raises(SpcError, match="multiplicity"):
+        sampler.yield_gradient(s5, [0, 0, 0.1], z5, DT, 6 * DT, 8)
+    sampler.yield_gradient_batch([s5], [[0, 0, 0.1]], [z5], DT, 6 * DT, 8, hyperfine=False)  # field set: fine
+    sampler.set_krylov("lanczos")
+    try:
+        with pytest.raises(SpcError, match="Lanczos"):
+            sampler.yield_gradient(s, [0, 0, 0.1], zk, DT, 6 * DT, 8)
+    finally:
+        sampler.set_krylov("mgs")
+    big, B = W.large_pair()
+    zbig = W.random_phase_samples(big.Z, 1, seed=3)
+    # a checkpoint every step over 20,000 steps: ~20,000 states of 28 MB (one
+    # 32-sample tile of dim 55296), far above the device's memory
+    with pytest.raises(SpcError, match="device memory"):
+        sampler.yield_gradient(big, B, zbig, DT, 20000 * DT, 8, checkpoint_every=1)
