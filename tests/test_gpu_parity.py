@@ -1,6 +1,6 @@
 """Parity of the CUDA path (through the C ABI) with the CPU oracle.
 
-Tolerance: the spec bar is |delta Phi_S| <= 1e-10 absolute. Every
+Tolerance: the singlet yield must agree to |delta Phi_S| <= 1e-10 absolute. Every
 population array and the Simpson yields are held to ABS_TOL = 1e-10; the
 Hamiltonian assembly (integer structure and the values, which are rounded at
 the same points on both sides) must be bit-exact.
