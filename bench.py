@@ -71,6 +71,7 @@ def parse():
     p.add_argument("--no-batch-adjoint", action="store_true", help="skip the batched-adjoint leg")
     p.add_argument("--batch-adjoint-window-ns", type=float, default=10.0)
     p.add_argument("--no-symmetry", action="store_true", help="skip the symmetry-block leg")
+    p.add_argument("--no-small", action="store_true", help="skip the small-pair (dim 288) leg")
     p.add_argument("--sym-samples", type=int, default=32)
     p.add_argument("--sym-window-ns", type=float, default=4.0)
     p.add_argument("--sym-directions", type=int, default=2)
@@ -307,10 +308,11 @@ def run_ours(args, rank, world, local_rank):
     adjoint = None if args.no_adjoint else adjoint_leg(args, sampler, value / world)
     batch_adjoint = None if args.no_batch_adjoint else batched_adjoint_leg(args, sampler, local_rank)
     symmetry = None if args.no_symmetry else symmetry_leg(args, sampler)
+    small = None if args.no_small else small_leg(args, sampler)
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
     return dict(ms=ms, value=value, e2e=e2e, batched=batched, adjoint=adjoint, batch_adjoint=batch_adjoint,
-                symmetry=symmetry,
+                symmetry=symmetry, small=small,
                 prof=prof, clocks=clk.summary(), launches=launches,
                 builds=builds, fallbacks=fallbacks, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
                 sysp=sysp, B=B, sim=sim)
@@ -460,6 +462,48 @@ def batched_adjoint_leg(args, sampler, local_rank):
             "params_per_job": [int(min(g.raw.size for g in gb)), int(max(g.raw.size for g in gb))],
             "workload": "uneven pairs x orientations: Phi_S and dPhi_S/d(B, J, D, kS, kT, every "
                         "hyperfine element) per job"}
+
+
+def small_leg(args, sampler):
+    """The small pair (dim 288: A = 1H, 1H, 14N; B = 14N, 1H; isotropic,
+    B = 0.05 mT along z), M = 64, 5 us at dt = 1 ns, m = 20, tol 1e-5 - the
+    workload the reference runs on CPU - through spc_build_h +
+    spc_trace_sampling (host vectors in, populations out), against the oracle
+    on all host cores on the same vectors."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    sysp, sim = W.small_pair(), W.small_sim(M=64, t_end_ns=5000.0)
+    zk = W.random_phase_samples(sysp.Z, sim.N_samples, seed=21)
+    steps = int(round(sim.t_end / sim.dt))
+
+    def gpu():
+        sampler.build_h(sysp, 0.05, "reference")
+        return sampler.trace_sampling(zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol)
+
+    breakdown = profiled(sampler, gpu)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    got = gpu()
+    torch.cuda.synchronize()
+    t_gpu = time.perf_counter() - t0
+    st = sampler.stats()
+    pyoracle.build()
+    e1, e2 = sysp.e1, sysp.e2
+    rp, col, val = pyoracle.build_h_iso(e1.g_I, e1.a_iso, e2.g_I, e2.a_iso, 0.05, sysp.J, sysp.D, sysp.kS,
+                                        sysp.kT)
+    threads = host_cores()
+    t0 = time.perf_counter()
+    ref = pyoracle.trace_sampling(rp, col, val, zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol, fast=True,
+                                  threads=threads)
+    t_cpu = time.perf_counter() - t0
+    work = sim.N_samples * steps
+    return {"value": work / t_gpu, "unit": "sample-steps/s", "seconds": t_gpu, "rounds": int(st["rounds"]),
+            "kernel_launches": int(st["kernel_launches"]), "cpu_value": work / t_cpu, "cpu_cores": threads,
+            "max_abs_dP_S_vs_oracle": float(np.max(np.abs(got.P_S - ref["P_S"]))), "kernel_breakdown": breakdown,
+            "workload": "small pair dim 288 (isotropic), M=64, 5 us at dt 1 ns, m=20, tol 1e-5"}
 
 
 def symmetry_leg(args, sampler):
@@ -634,7 +678,7 @@ def main():
                                    "frac": (ach_tf * 1e12 / r["fp64_peak"]) if ach_tf else None,
                                    "peak_source": "measured DFMA probe (spc_fp64_peak)"}},
                 kernel_share=share, batched=r["batched"], adjoint=r["adjoint"],
-                batched_adjoint=r["batch_adjoint"], symmetry=r["symmetry"], cpu_baseline=cpu,
+                batched_adjoint=r["batch_adjoint"], symmetry=r["symmetry"], small=r["small"], cpu_baseline=cpu,
                 accuracy=accuracy)
     print(json.dumps(line))
 

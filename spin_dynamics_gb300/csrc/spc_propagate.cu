@@ -860,6 +860,99 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// The same dt loop with one sample per 128-thread CTA (m <= 32), for rounds
+// with few samples in flight: a warp-wide DFMA occupies one SM sub-partition
+// for many cycles, so one warp per sample leaves three of an SM's four FP64
+// units idle. Every product (E c and the four projector forms) is split over
+// the four warps by column ranges; the partial sums are added in warp order
+// through shared memory, and warp X finishes projector X.
+__global__ void __launch_bounds__(128)
+    k_dtloop_mw(int m, int nslots, int T, const TileInfo* __restrict__ tiles,
+                const int* __restrict__ map, const int* __restrict__ skip,
+                const double2* __restrict__ Aexp, const double2* __restrict__ proj,
+                double2* __restrict__ cvec, double* __restrict__ tt, int* __restrict__ kk,
+                int* __restrict__ done, double* __restrict__ obs, double dt, double t_end, double tol,
+                long long* __restrict__ nsteps, int* __restrict__ err) {
+  __shared__ double2 c[32];
+  __shared__ double2 part[4][32];
+  __shared__ double2 vpart[4][4][32];
+  __shared__ double s_c2, s_cm2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x;
+  if (w >= nslots || map[w] < 0 || skip[w]) return;  // whole CTA
+  const int s = map[w];
+  const size_t mm = (size_t)m * m;
+  const double2* E = Aexp + (size_t)w * mm;
+  const double2* PX = proj + (size_t)w * 4 * mm;
+  const int me = tiles[w / SPC_LANES].m;
+  const int j0 = (me * warp) / 4, j1 = (me * (warp + 1)) / 4;  // this warp's columns
+  const bool l0 = lane < me;
+  if (warp == 0) c[lane] = l0 ? cvec[(size_t)w * m + lane] : cz();
+  __syncthreads();
+  double t = tt[s];
+  int k = kk[s];
+  double c2 = 1.0, cm2 = 0.0;
+  double* o = obs + (size_t)s * 4 * T;
+  const int slot[4] = {2, 0, 1, 3};  // proj type -> obs slot
+  long long steps = 0;
+  while (cm2 <= tol * c2 && t < t_end) {
+    // n = E c over this warp's columns
+    double2 a = cz();
+    if (l0)
+      for (int j = j0; j < j1; ++j) a = cfma(E[lane + j * m], c[j], a);
+    part[warp][lane] = a;
+    __syncthreads();
+    if (warp == 0) {
+      double2 n = cadd(cadd(cadd(part[0][lane], part[1][lane]), part[2][lane]), part[3][lane]);
+      if (!l0) n = cz();
+      c[lane] = n;
+      __syncwarp();
+      const double nn = warp_sum(fma(n.x, n.x, n.y * n.y));
+      if (lane == 0) {
+        s_c2 = nn;
+        const double2 cmv = c[me - 1];
+        s_cm2 = cmv.x * cmv.x + cmv.y * cmv.y;
+      }
+    }
+    __syncthreads();
+    if (k >= T) {
+      if (threadIdx.x == 0) atomicExch(err, 1);
+      break;
+    }
+    // projector forms: partial P_X n over this warp's columns, all four types
+    for (int ty = 0; ty < 4; ++ty) {
+      const double2* P = PX + ty * mm;
+      double2 v = cz();
+      if (l0)
+        for (int j = j0; j < j1; ++j) v = cfma(P[lane + j * m], c[j], v);
+      vpart[warp][ty][lane] = v;
+    }
+    __syncthreads();
+    {
+      const int ty = warp;
+      const double2 v = cadd(cadd(cadd(vpart[0][ty][lane], vpart[1][ty][lane]), vpart[2][ty][lane]),
+                             vpart[3][ty][lane]);
+      const double2 n = c[lane];
+      double term = l0 ? fma(n.x, v.x, n.y * v.y) : 0.0;
+      term = warp_sum(term);
+      if (lane == 0) o[slot[ty] * T + k] = term;
+    }
+    c2 = s_c2;
+    cm2 = s_cm2;
+    t = t + dt;
+    k = k + 1;
+    steps++;
+  }
+  __syncthreads();
+  if (warp == 0 && l0) cvec[(size_t)w * m + lane] = c[lane];
+  if (threadIdx.x == 0) {
+    tt[s] = t;
+    kk[s] = k;
+    done[s] = (t < t_end) ? 0 : 1;
+    atomicAdd((unsigned long long*)nsteps, (unsigned long long)steps);
+  }
+}
+
 // psi[:, scol] = Q c for the tile of a pass item (src/qm_dynamics.f90:365)
 __global__ void __launch_bounds__(256)
     k_psi_update(const TileInfo* __restrict__ tiles, const int2* __restrict__ items, int m,
@@ -1361,7 +1454,10 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
         if (map[w] >= 0 && flag_h[w]) failed.push_back(map[w]);
     }
     pe = h->prof.begin(st);
-    if (m <= 8)
+    if (m <= 32 && (int64_t)list.size() * 2 <= (int64_t)h->sm_count * 4)
+      k_dtloop_mw<<<nslots, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj, d_c, d_t, d_k,
+                                          d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
+    else if (m <= 8)
       k_dtloop_packed<8><<<(nslots + 15) / 16, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj,
                                                               d_c, d_t, d_k, d_done, d_obs, dt, t_end, tol,
                                                               d_nsteps, d_err);
