@@ -287,6 +287,14 @@ int spc_autotune_krylov(spc_handle* h, int n_jobs, const int* job_sys, const int
  * basis through the projector Grams (their sum is Q^H Q). */
 int spc_set_krylov(spc_handle* h, int method);
 
+/* Replay each build round of a propagation as a CUDA graph (1, the
+ * default) or launch its kernels one by one (0). The launches of a round are
+ * captured when a work-plan shape occurs for the second time within a call
+ * and replayed while it repeats (small systems run hundreds of rounds of one
+ * shape); results are identical either way. Not used while kernel profiling
+ * is on. */
+int spc_set_graphs(spc_handle* h, int enable);
+
 /* Counters of the last propagation call on this handle. */
 int spc_get_stats(const spc_handle* h, spc_stats* out);
 

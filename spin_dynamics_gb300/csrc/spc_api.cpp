@@ -409,6 +409,12 @@ int spc_autotune_krylov(spc_handle* h, int n_jobs, const int* job_sys, const int
   return rc;
 }
 
+int spc_set_graphs(spc_handle* h, int enable) {
+  if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
+  h->h.use_graphs = enable != 0;
+  return SPC_OK;
+}
+
 int spc_set_profiling(spc_handle* h, int enable) {
   if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
   h->h.prof.on = enable != 0;

@@ -127,6 +127,8 @@ struct Handle {
   } hb;
   // Krylov method: 0 full MGS (the reference's get_krylov), 1 Lanczos, 2 auto
   int krylov_method = 0;
+  // replay each build round's launches as a captured CUDA graph
+  bool use_graphs = true;
   // H_eff = (Hermitian) - i*kappa*1 for the current Hamiltonian: Lanczos applies
   bool herm_shift = false;
   bool lanczos_active() const {

@@ -33,6 +33,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <set>
 #include <vector>
 
 #include "spc_common.cuh"
@@ -1242,6 +1244,13 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   bool lanczos_ok = h->krylov_method == 1 || h->krylov_method == 2;
   for (const JobSpec& j : jobs) lanczos_ok = lanczos_ok && j.herm_shift;
   std::vector<char> hplan;
+  // round graphs of this call: plan shape -> (executable graph, launches in it)
+  struct GraphCache : std::map<std::vector<int64_t>, std::pair<cudaGraphExec_t, int64_t>> {
+    ~GraphCache() {
+      for (auto& kv : *this) cudaGraphExecDestroy(kv.second.first);
+    }
+  } graph_cache;
+  std::set<std::vector<int64_t>> shapes_seen;
 
   // One build round for the samples in `list` (global indices, job order):
   // Krylov basis (Lanczos or full MGS), expm, projectors; then the dt loop and
@@ -1318,84 +1327,6 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     std::memcpy(hplan.data() + off_map, map.data(), sizeof(int) * nslots);
     std::memcpy(hplan.data() + off_scol, scol.data(), sizeof(int) * nslots);
     CK(cudaMemcpyAsync(plan, hplan.data(), plan_bytes, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(d_A, 0, sizeof(double2) * mm * nslots, st));
-    CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * nslots, st));
-    PassArgs pa{};
-    pa.tiles = d_tiles;
-    pa.items = d_items_p;
-    pa.m = m;
-    pa.Q = d_Q;
-    pa.P = d_P;
-    pa.psi = d_psi;
-    pa.map = d_map;
-    pa.scol = d_scol;
-    pa.coef = d_coef;
-    pa.rbeta = d_rb;
-    pa.Ahess = d_A;
-    pa.cvec = d_c;
-    pa.partial = d_part;
-    pa.counters = d_cnt;
-    pa.lanczos = lanczos ? 1 : 0;
-    int64_t nnz_work = 0;
-    for (const TileInfo& ti : tiles) nnz_work += (int64_t)(jobs[ti.job].nnz);
-    int pe = h->prof.begin(st);
-    k_rowpass<PASS_NORM_GATHER><<<nip, blk, 0, st>>>(pa);
-    h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
-    pe = h->prof.begin(st);
-    k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 1, 0, d_rb, d_Q);
-    h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
-    h->count_launch(2);
-    for (int i = 0; i < m; ++i) {
-      pe = h->prof.begin(st);
-      k_spmm<<<nis, blk, 0, st>>>(d_tiles, d_items_s, d_map, i, d_Q, d_P);
-      // algorithmic traffic: H once per tile, X once, Y once
-      h->prof.end(st, pe, PK_SPMM, 8.0 * (double)nnz_work * SPC_LANES,
-                  20.0 * (double)nnz_work + 32.0 * elems);
-      h->count_launch();
-      pa.col_i = i;
-      // MGS (get_krylov :453-456) projects p on Q_0..Q_i in order. Lanczos
-      // (H_eff Hermitian up to -i*kappa) needs only Q_{i-1} (coefficient
-      // beta_{i-1}, already in coef) and Q_i.
-      int j0 = 0;
-      if (lanczos && i > 0) {
-        j0 = i - 1;
-      } else {
-        pa.row_j = 0;
-        pa.jx = 0;
-        pe = h->prof.begin(st);
-        k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
-        h->prof.end(st, pe, PK_DOT, 8.0 * elems, 32.0 * elems);
-        h->count_launch();
-      }
-      for (int j = j0; j < i; ++j) {
-        pa.jx = j;
-        pa.jn = j + 1;
-        pa.row_j = j + 1;
-        pe = h->prof.begin(st);
-        k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
-        h->prof.end(st, pe, PK_AXPY_DOT, 16.0 * elems, 64.0 * elems);
-        h->count_launch();
-      }
-      if (i < m - 1) {
-        pa.jx = i;
-        pa.row_j = i + 1;
-        pe = h->prof.begin(st);
-        k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
-        h->prof.end(st, pe, PK_AXPY_NORM, 12.0 * elems, 48.0 * elems);
-        pe = h->prof.begin(st);
-        k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 0, i + 1, d_rb,
-                                     d_Q);
-        h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
-        h->count_launch(2);
-      }
-    }
-    double zsum = 0.0;  // sum over active slots of Z
-    for (size_t c = 0; c < map.size(); ++c)
-      if (map[c] >= 0) zsum += tiles[c / SPC_LANES].n / 4;
-    pe = h->prof.begin(st);
-    launch_expm(m, nslots, d_tiles, d_map, d_A, d_E, dt, d_err, st);
-    h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * list.size(),
-                32.0 * (double)mm * list.size());
     // projector splits: rows per split `rps` minimising the estimated time
     // (all rows plus a per-CTA overhead of 32 rows, over the resident CTAs,
     // plus the longest CTA); each sample takes ceil(Z/rps) splits, at most
@@ -1426,54 +1357,171 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
       }
       for (int64_t z : zact) ns = std::max(ns, proj_splits(nsplit_max, rps, z));
     }
-    const dim3 pgrid(nslots, ns);
-    pe = h->prof.begin(st);
-    {
-      void* args[] = {(void*)&d_tiles, (void*)&d_map, (void*)&m, (void*)&ncombo, (void*)&d_combos,
-                      (void*)&d_Q, (void*)&ns, (void*)&rps, (void*)&d_ppart};
-      CK(cudaLaunchKernel(proj_fn, pgrid, dim3(proj_threads), args, proj_smem, st));
-    }
-    h->prof.end(st, pe, PK_PROJ, 8.0 * (double)ncombo * zsum + 4.0 * (double)m * zsum,
-                64.0 * (double)m * zsum);
-    {
-      const int64_t tot = (int64_t)nslots * ncombo;
+    // every launch of the round; captured as a CUDA graph per plan shape
+    // within this call and replayed (the plan itself lives in device memory
+    // and is copied before each round)
+    auto enqueue = [&]() -> int {
+      CK(cudaMemsetAsync(d_A, 0, sizeof(double2) * mm * nslots, st));
+      CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * nslots, st));
+      PassArgs pa{};
+      pa.tiles = d_tiles;
+      pa.items = d_items_p;
+      pa.m = m;
+      pa.Q = d_Q;
+      pa.P = d_P;
+      pa.psi = d_psi;
+      pa.map = d_map;
+      pa.scol = d_scol;
+      pa.coef = d_coef;
+      pa.rbeta = d_rb;
+      pa.Ahess = d_A;
+      pa.cvec = d_c;
+      pa.partial = d_part;
+      pa.counters = d_cnt;
+      pa.lanczos = lanczos ? 1 : 0;
+      int64_t nnz_work = 0;
+      for (const TileInfo& ti : tiles) nnz_work += (int64_t)(jobs[ti.job].nnz);
+      int pe = h->prof.begin(st);
+      k_rowpass<PASS_NORM_GATHER><<<nip, blk, 0, st>>>(pa);
+      h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
       pe = h->prof.begin(st);
-      k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(d_tiles, nslots, d_map, m, ncombo, ns, rps, d_combos,
-                                                             d_ppart, d_proj);
-      h->prof.end(st, pe, PK_PROJ_REDUCE, 2.0 * tot * ns, 16.0 * tot * (ns + 1));
-      h->count_launch(3);
+      k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 1, 0, d_rb, d_Q);
+      h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
+      h->count_launch(2);
+      for (int i = 0; i < m; ++i) {
+        pe = h->prof.begin(st);
+        k_spmm<<<nis, blk, 0, st>>>(d_tiles, d_items_s, d_map, i, d_Q, d_P);
+        // algorithmic traffic: H once per tile, X once, Y once
+        h->prof.end(st, pe, PK_SPMM, 8.0 * (double)nnz_work * SPC_LANES,
+                    20.0 * (double)nnz_work + 32.0 * elems);
+        h->count_launch();
+        pa.col_i = i;
+        // MGS (get_krylov :453-456) projects p on Q_0..Q_i in order. Lanczos
+        // (H_eff Hermitian up to -i*kappa) needs only Q_{i-1} (coefficient
+        // beta_{i-1}, already in coef) and Q_i.
+        int j0 = 0;
+        if (lanczos && i > 0) {
+          j0 = i - 1;
+        } else {
+          pa.row_j = 0;
+          pa.jx = 0;
+          pe = h->prof.begin(st);
+          k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
+          h->prof.end(st, pe, PK_DOT, 8.0 * elems, 32.0 * elems);
+          h->count_launch();
+        }
+        for (int j = j0; j < i; ++j) {
+          pa.jx = j;
+          pa.jn = j + 1;
+          pa.row_j = j + 1;
+          pe = h->prof.begin(st);
+          k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
+          h->prof.end(st, pe, PK_AXPY_DOT, 16.0 * elems, 64.0 * elems);
+          h->count_launch();
+        }
+        if (i < m - 1) {
+          pa.jx = i;
+          pa.row_j = i + 1;
+          pe = h->prof.begin(st);
+          k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
+          h->prof.end(st, pe, PK_AXPY_NORM, 12.0 * elems, 48.0 * elems);
+          pe = h->prof.begin(st);
+          k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 0, i + 1, d_rb,
+                                       d_Q);
+          h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
+          h->count_launch(2);
+        }
+      }
+      double zsum = 0.0;  // sum over active slots of Z
+      for (size_t c = 0; c < map.size(); ++c)
+        if (map[c] >= 0) zsum += tiles[c / SPC_LANES].n / 4;
+      pe = h->prof.begin(st);
+      launch_expm(m, nslots, d_tiles, d_map, d_A, d_E, dt, d_err, st);
+      h->prof.end(st, pe, PK_EXPM, 8.0 * (double)mm * m * 9.0 * list.size(),
+                  32.0 * (double)mm * list.size());
+      const dim3 pgrid(nslots, ns);
+      pe = h->prof.begin(st);
+      {
+        void* args[] = {(void*)&d_tiles, (void*)&d_map, (void*)&m, (void*)&ncombo, (void*)&d_combos,
+                        (void*)&d_Q, (void*)&ns, (void*)&rps, (void*)&d_ppart};
+        CK(cudaLaunchKernel(proj_fn, pgrid, dim3(proj_threads), args, proj_smem, st));
+      }
+      h->prof.end(st, pe, PK_PROJ, 8.0 * (double)ncombo * zsum + 4.0 * (double)m * zsum,
+                  64.0 * (double)m * zsum);
+      {
+        const int64_t tot = (int64_t)nslots * ncombo;
+        pe = h->prof.begin(st);
+        k_proj_reduce<<<(int)((tot + 255) / 256), 256, 0, st>>>(d_tiles, nslots, d_map, m, ncombo, ns, rps, d_combos,
+                                                               d_ppart, d_proj);
+        h->prof.end(st, pe, PK_PROJ_REDUCE, 2.0 * tot * ns, 16.0 * tot * (ns + 1));
+        h->count_launch(3);
+      }
+      if (lanczos) {
+        // G = Q^H Q = Tp + S + T0 + Tm; a basis that drifted from orthonormal
+        // beyond ORTHO_TOL is rebuilt with full MGS
+        k_ortho_check<<<nslots, 128, 0, st>>>(m, d_tiles, d_map, d_proj, ORTHO_TOL, d_flag);
+        h->count_launch();
+      }
+      pe = h->prof.begin(st);
+      if (m <= 32 && (int64_t)list.size() * 2 <= (int64_t)h->sm_count * 4)
+        k_dtloop_mw<<<nslots, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj, d_c, d_t, d_k,
+                                            d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
+      else if (m <= 8)
+        k_dtloop_packed<8><<<(nslots + 15) / 16, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj,
+                                                                d_c, d_t, d_k, d_done, d_obs, dt, t_end, tol,
+                                                                d_nsteps, d_err);
+      else if (m <= 16)
+        k_dtloop_packed<16><<<(nslots + 7) / 8, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj,
+                                                               d_c, d_t, d_k, d_done, d_obs, dt, t_end, tol,
+                                                               d_nsteps, d_err);
+      else
+        k_dtloop<<<(nslots + 3) / 4, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj, d_c, d_t,
+                                                   d_k, d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
+      h->prof.end(st, pe, PK_DTLOOP, 0.0, 0.0);
+      pe = h->prof.begin(st);
+      k_psi_update<<<nip, blk, 0, st>>>(d_tiles, d_items_p, m, d_map, d_scol, d_flag, d_Q, d_c, d_psi);
+      h->prof.end(st, pe, PK_PSI, 8.0 * m * elems, 16.0 * (m + 1) * elems);
+      h->count_launch(2);
+      CK(cudaGetLastError());
+      return SPC_OK;
+    };
+    // a shape is captured the second time it occurs (calls whose rounds never
+    // repeat a shape pay no capture)
+    const std::vector<int64_t> key = {nip, nis, nslots, ns, rps, lanczos ? 1 : 0, (int64_t)list.size()};
+    const bool graphs = h->use_graphs && !h->prof.on && !shapes_seen.insert(key).second;
+    if (graphs) {
+      auto itg = graph_cache.find(key);
+      if (itg == graph_cache.end()) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int64_t l0 = h->launches;
+        const int rc = enqueue();
+        const cudaError_t ec = cudaStreamEndCapture(st, &g);
+        if (rc) {
+          if (g) cudaGraphDestroy(g);
+          return rc;
+        }
+        if (ec != cudaSuccess) return set_error(SPC_ERR_CUDA, "round capture failed: %s", cudaGetErrorString(ec));
+        const cudaError_t ei = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) return set_error(SPC_ERR_CUDA, "round graph instantiation failed: %s",
+                                               cudaGetErrorString(ei));
+        itg = graph_cache.emplace(key, std::make_pair(ge, h->launches - l0)).first;
+        h->launches = l0;  // counted when the graph runs
+      }
+      CK(cudaGraphLaunch(itg->second.first, st));
+      h->count_launch((int)itg->second.second);
+    } else {
+      const int rc = enqueue();
+      if (rc) return rc;
     }
     if (lanczos) {
-      // G = Q^H Q = Tp + S + T0 + Tm; a basis that drifted from orthonormal
-      // beyond ORTHO_TOL is rebuilt with full MGS
-      k_ortho_check<<<nslots, 128, 0, st>>>(m, d_tiles, d_map, d_proj, ORTHO_TOL, d_flag);
-      h->count_launch();
       CK(cudaMemcpyAsync(flag_h.data(), d_flag, sizeof(int) * nslots, cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
       for (int w = 0; w < nslots; ++w)
         if (map[w] >= 0 && flag_h[w]) failed.push_back(map[w]);
     }
-    pe = h->prof.begin(st);
-    if (m <= 32 && (int64_t)list.size() * 2 <= (int64_t)h->sm_count * 4)
-      k_dtloop_mw<<<nslots, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj, d_c, d_t, d_k,
-                                          d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
-    else if (m <= 8)
-      k_dtloop_packed<8><<<(nslots + 15) / 16, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj,
-                                                              d_c, d_t, d_k, d_done, d_obs, dt, t_end, tol,
-                                                              d_nsteps, d_err);
-    else if (m <= 16)
-      k_dtloop_packed<16><<<(nslots + 7) / 8, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj,
-                                                             d_c, d_t, d_k, d_done, d_obs, dt, t_end, tol,
-                                                             d_nsteps, d_err);
-    else
-      k_dtloop<<<(nslots + 3) / 4, 128, 0, st>>>(m, nslots, T, d_tiles, d_map, d_flag, d_E, d_proj, d_c, d_t,
-                                                 d_k, d_done, d_obs, dt, t_end, tol, d_nsteps, d_err);
-    h->prof.end(st, pe, PK_DTLOOP, 0.0, 0.0);
-    pe = h->prof.begin(st);
-    k_psi_update<<<nip, blk, 0, st>>>(d_tiles, d_items_p, m, d_map, d_scol, d_flag, d_Q, d_c, d_psi);
-    h->prof.end(st, pe, PK_PSI, 8.0 * m * elems, 16.0 * (m + 1) * elems);
-    h->count_launch(2);
-    CK(cudaGetLastError());
     return SPC_OK;
   };
 

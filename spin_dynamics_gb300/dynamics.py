@@ -196,6 +196,11 @@ class TraceSampler:
     def set_stream(self, stream_ptr: int) -> None:
         nat.check(nat.lib().spc_set_stream(self._h, C.c_void_p(stream_ptr)))
 
+    def set_graphs(self, enable: bool) -> None:
+        """Replay each build round as a captured CUDA graph (default) or
+        launch its kernels one by one; results are identical."""
+        nat.check(nat.lib().spc_set_graphs(self._h, 1 if enable else 0))
+
     def set_krylov(self, method: str) -> None:
         """'mgs' (full modified Gram-Schmidt, the reference's get_krylov),
         'lanczos' (kS == kT only) or 'auto' (Lanczos when it applies)."""

@@ -218,3 +218,34 @@ def test_exact_krylov_breakdown_gives_the_exact_answer(sampler, oracle):
     n = int(np.ceil(30 * dt / dt)) + 1
     t = np.arange(n) * dt
     assert np.max(np.abs(got.P_S[:n] - (5 / 8 + 3 / 8 * np.cos(a * t)))) < 1e-12
+
+
+@pytest.mark.parametrize("method", ["mgs", "auto"])
+def test_graph_replay_equals_direct_launches(sampler, method):
+    """Rounds replayed as captured CUDA graphs give the same bits as the
+    same launches issued one by one (single job and a batch)."""
+    DT = 1.0 * GAMMA_E / 1000
+    s = W.small_pair()
+    zk = W.random_phase_samples(s.Z, 40, seed=12)
+    nb = W.notebook_pair()
+    nb.kS = nb.kT = s.kS
+    zb = W.random_phase_samples(nb.Z, 7, seed=13)
+    out = {}
+    sampler.set_krylov(method)
+    try:
+        for graphs in (False, True):
+            sampler.set_graphs(graphs)
+            sampler.build_h(s, 0.05, "reference")
+            one = sampler.trace_sampling(zk, DT, 120 * DT, 12, 1e-6)
+            sampler.build_h_batch([nb, s], [0.1, 0.05], "reference")
+            many = sampler.trace_sampling_batch([zb, zk], DT, 120 * DT, 12, 1e-6)
+            out[graphs] = (one, many, sampler.stats()["rounds"])
+    finally:
+        sampler.set_graphs(True)
+        sampler.set_krylov("mgs")
+    (a1, am, _), (b1, bm, rounds) = out[False], out[True]
+    assert rounds > 2
+    for k in ("P_S", "P_T0", "P_Tp", "P_Tm"):
+        assert np.array_equal(getattr(a1, k), getattr(b1, k))
+        for x, y in zip(am, bm):
+            assert np.array_equal(getattr(x, k), getattr(y, k))
