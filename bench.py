@@ -325,19 +325,29 @@ def batched_leg(args, sampler, local_rank):
     jobs as per-instance calls (spc_build_h + spc_trace_sampling_device)."""
     import torch
 
-    from spin_dynamics_gb300.dynamics import num_time_points
+    from spin_dynamics_gb300.dynamics import batch_groups, device_memory, num_time_points, padded_samples
 
     pairs, dirs, systems, fields, zks = uneven_jobs(args)
     Ms = [z.shape[0] for z in zks]
     dt = 1.0 * 176.08596 / 1000
     t_end = args.batch_window_ns * 176.08596 / 1000
     T = num_time_points(dt, t_end)
-    # Krylov dimension by the autotuner (one tile per job, 10 ns), shared by both arms
-    sampler.build_h_batch(systems, fields, "general")
-    m, tune_rates = sampler.autotune_krylov(zks, dt, 10 * dt, 1e-5, candidates=(12, 16, 20, 24, 30, 40))
+    # Krylov dimension by the autotuner (one tile of each of up to 64 evenly
+    # spaced jobs, 10 ns), shared by both arms
+    pick = list(range(0, len(zks), max(1, len(zks) // 64)))
+    sampler.build_h_batch([systems[i] for i in pick], [fields[i] for i in pick], "general")
+    m, tune_rates = sampler.autotune_krylov([zks[i] for i in pick], dt, 10 * dt, 1e-5,
+                                            candidates=(12, 16, 20, 24, 30, 40))
     offs = np.cumsum([0] + [z.size for z in zks])
-    zk_dev = torch.from_numpy(np.concatenate([z.reshape(-1) for z in zks])).to(f"cuda:{local_rank}")
+    zk_dev = torch.empty(int(offs[-1]), dtype=torch.complex128, device=f"cuda:{local_rank}")
+    for k, z in enumerate(zks):  # job by job: no host copy of the whole set
+        zk_dev[int(offs[k]):int(offs[k + 1])].copy_(torch.from_numpy(z.reshape(-1)))
     out_dev = torch.empty(len(zks) * 4 * T, dtype=torch.float64, device=f"cuda:{local_rank}")
+    # consecutive job groups whose bases and states take at most half the
+    # memory left free once the samples and results are resident
+    free, _ = device_memory(local_rank)
+    groups = batch_groups([4 * s.Z * padded_samples(M) for s, M in zip(systems, Ms)],
+                          free * 0.5 / (16.0 * (m + 4)))
     stream = torch.cuda.current_stream()
 
     def per_instance():
@@ -347,8 +357,10 @@ def batched_leg(args, sampler, local_rank):
                                           1e-5, out_dev.data_ptr() + 8 * k * 4 * T)
 
     def batched():
-        sampler.build_h_batch(systems, fields, "general")
-        sampler.trace_sampling_batch_device(zk_dev.data_ptr(), Ms, dt, t_end, m, 1e-5, out_dev.data_ptr())
+        for grp in groups:
+            sampler.build_h_batch([systems[i] for i in grp], [fields[i] for i in grp], "general")
+            sampler.trace_sampling_batch_device(zk_dev.data_ptr() + 16 * int(offs[grp[0]]), [Ms[i] for i in grp],
+                                                dt, t_end, m, 1e-5, out_dev.data_ptr() + 8 * grp[0] * 4 * T)
 
     def timed(fn):
         fn()
@@ -366,14 +378,15 @@ def batched_leg(args, sampler, local_rank):
     t_single = timed(per_instance)
     breakdown = profiled(sampler, batched)
     t_batch = timed(batched)
-    t_build = timed(lambda: sampler.build_h_batch(systems, fields, "general"))
+    t_build = timed(lambda: [sampler.build_h_batch([systems[i] for i in grp], [fields[i] for i in grp], "general")
+                             for grp in groups])
     dims = [4 * s.Z for s in systems]
     return {"value": work / t_batch, "per_instance_value": work / t_single,
             "ratio": t_single / t_batch, "unit": "sample-steps/s", "jobs": len(zks),
             "pairs": len(pairs), "orientations": len(dirs), "dims": [min(dims), max(dims)],
             "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m, "kernel_breakdown": breakdown,
             "seconds": t_batch, "build_seconds": t_build, "per_instance_seconds": t_single,
-            "krylov_autotune_rates": tune_rates,
+            "krylov_autotune_rates": tune_rates, "batches": len(groups),
             "workload": "uneven pairs (2-10 nuclei from 1H/14N, anisotropic) x Fibonacci-sphere "
                         "orientations at 0.05 mT, own Hamiltonian per job"}
 
@@ -403,10 +416,11 @@ def uneven_jobs(args):
     dirs = W.fibonacci_sphere(args.batch_orient)
     systems, fields, zks = [], [], []
     for p, (s, M) in enumerate(pairs):
+        z = W.random_phase_samples(s.Z, M, seed=100 + p)  # shared by the pair's orientations
         for d in dirs:
             systems.append(s)
             fields.append(d)
-            zks.append(W.random_phase_samples(s.Z, M, seed=100 + p))
+            zks.append(z)
     return pairs, dirs, systems, fields, zks
 
 

@@ -287,6 +287,10 @@ int spc_autotune_krylov(spc_handle* h, int n_jobs, const int* job_sys, const int
  * basis through the projector Grams (their sum is Q^H Q). */
 int spc_set_krylov(spc_handle* h, int method);
 
+/* Free and total device memory of `device` in bytes (sizes batches of jobs
+ * that do not fit one call). */
+int spc_mem_info(int device, int64_t* free_bytes, int64_t* total_bytes);
+
 /* Replay each build round of a propagation as a CUDA graph (1, the
  * default) or launch its kernels one by one (0). The launches of a round are
  * captured when a work-plan shape occurs for the second time within a call

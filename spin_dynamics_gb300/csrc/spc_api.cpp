@@ -409,6 +409,20 @@ int spc_autotune_krylov(spc_handle* h, int n_jobs, const int* job_sys, const int
   return rc;
 }
 
+int spc_mem_info(int device, int64_t* free_bytes, int64_t* total_bytes) {
+  if (!free_bytes || !total_bytes) return spc::set_error(SPC_ERR_ARG, "spc_mem_info: null output");
+  int cur = 0;
+  CKR(cudaGetDevice(&cur));
+  CKR(cudaSetDevice(device));
+  size_t f = 0, t = 0;
+  const cudaError_t e = cudaMemGetInfo(&f, &t);
+  cudaSetDevice(cur);
+  if (e != cudaSuccess) return spc::set_error(SPC_ERR_CUDA, "cudaMemGetInfo failed: %s", cudaGetErrorString(e));
+  *free_bytes = (int64_t)f;
+  *total_bytes = (int64_t)t;
+  return SPC_OK;
+}
+
 int spc_set_graphs(spc_handle* h, int enable) {
   if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
   h->h.use_graphs = enable != 0;

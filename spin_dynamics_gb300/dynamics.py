@@ -125,6 +125,34 @@ def seeded_samples(seed: Sequence[int], Z: int, M: int, serial: bool = False) ->
     return out.view(np.complex128).reshape(M, Z)
 
 
+def device_memory(device: int = 0) -> tuple:
+    """(free, total) bytes of a CUDA device (spc_mem_info)."""
+    f, t = C.c_int64(), C.c_int64()
+    nat.check(nat.lib().spc_mem_info(int(device), C.byref(f), C.byref(t)))
+    return f.value, t.value
+
+
+def padded_samples(M: int) -> int:
+    """Sample columns a job occupies on the device (tiles of 32)."""
+    return (M + 31) // 32 * 32
+
+
+def batch_groups(entries, budget: float) -> list:
+    """Consecutive groups of jobs (given their vector entries, rows x padded
+    samples) whose sum stays under `budget` entries; a job larger than the
+    budget forms a group of its own."""
+    groups, cur, tot = [], [], 0
+    for i, x in enumerate(entries):
+        if cur and tot + x > budget:
+            groups.append(cur)
+            cur, tot = [], 0
+        cur.append(i)
+        tot += x
+    if cur:
+        groups.append(cur)
+    return groups
+
+
 @dataclass
 class YieldGradient:
     """Yields and gradient of spc_yield_gradient. Tensors are (row, col)
@@ -297,6 +325,24 @@ class TraceSampler:
             _dptr(out), T))
         out = out.reshape(len(zkets_list), 4, T)
         return [Observables(o[0].copy(), o[1].copy(), o[2].copy(), o[3].copy()) for o in out]
+
+    def trace_sampling_many(self, systems, fields, zkets_list, dt: float, t_end: float, m: int, tol: float,
+                            mode: str = "general", init_state: str = "singlet", memory_fraction: float = 0.5,
+                            device: int = 0) -> list:
+        """Any number of jobs (system, field, samples): split into batches whose
+        Krylov bases and states use at most `memory_fraction` of the device's
+        free memory, each batch one spc_build_h_batch + spc_trace_sampling_batch
+        call. Returns one Observables per job, in job order."""
+        free, _ = device_memory(device)
+        budget = free * memory_fraction / (16.0 * (m + 4))
+        entries = [4 * s.Z * padded_samples(z.shape[0]) for s, z in zip(systems, zkets_list)]
+        out = [None] * len(systems)
+        for grp in batch_groups(entries, budget):
+            self.build_h_batch([systems[i] for i in grp], [fields[i] for i in grp], mode)
+            res = self.trace_sampling_batch([zkets_list[i] for i in grp], dt, t_end, m, tol, init_state)
+            for i, r in zip(grp, res):
+                out[i] = r
+        return out
 
     def trace_sampling_batch_device(self, zk_ptr: int, M, dt: float, t_end: float, m: int,
                                     tol: float, out_ptr: int, init_state: str = "singlet",

@@ -255,34 +255,11 @@ def _block_vectors(sel, sim: SimParam, exact_blocks: bool):
     return [dynamics.seeded_samples(seed, Zb, sim.N_samples) for _, _, _, Zb, seed in sel]
 
 
-def _chunks(rows_x_samples, budget_entries):
-    """Split jobs (list of rows * samples) into consecutive groups whose sum
-    stays under budget_entries (at least one job per group)."""
-    groups, cur, tot = [], [], 0
-    for i, x in enumerate(rows_x_samples):
-        if cur and tot + x > budget_entries:
-            groups.append(cur)
-            cur, tot = [], 0
-        cur.append(i)
-        tot += x
-    if cur:
-        groups.append(cur)
-    return groups
-
-
-def _padded(M: int) -> int:
-    """Sample columns a job occupies on the device (tiles of 32)."""
-    return (M + 31) // 32 * 32
-
-
 def _budget_entries(states_per_entry: float) -> float:
     """Vector entries (rows x samples) a batch may hold: a third of the free
     device memory over `states_per_entry` complex states per entry."""
-    try:
-        import torch
-        free, _ = torch.cuda.mem_get_info()
-    except Exception:
-        free = 16 << 30
+    from .dynamics import device_memory
+    free, _ = device_memory()
     return max(1.0, free / 3.0 / (16.0 * states_per_entry))
 
 
@@ -298,13 +275,14 @@ def symmetrised_dynamics(sys_: SysParam, sim: SimParam, out: Optional[str] = Non
     Hamiltonian (anisotropic explicit nuclei, tilted field); by default the
     reference's builder with the field -w along z."""
     from . import dynamics
+    from .dynamics import batch_groups, padded_samples
     sp = sampler or dynamics.default_sampler()
     sel = _selected(sys_, sim)
     zks = _block_vectors(sel, sim, exact_blocks)
     T = dynamics.num_time_points(sim.dt, sim.t_end)
     res = Observables.zeros(T)
-    sizes = [4 * Zb * _padded(z.shape[0]) for (_, _, _, Zb, _), z in zip(sel, zks)]
-    for grp in _chunks(sizes, _budget_entries(sim.N_krylov + 4)):
+    sizes = [4 * Zb * padded_samples(z.shape[0]) for (_, _, _, Zb, _), z in zip(sel, zks)]
+    for grp in batch_groups(sizes, _budget_entries(sim.N_krylov + 4)):
         systems = [sel[j][2] for j in grp]
         if field is None:
             sp.build_h_batch(systems, [-s.e1.w for s in systems], "reference")
@@ -334,6 +312,7 @@ def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, d
     the derivatives with respect to the polar and azimuthal angles theta, phi
     of the field."""
     from . import dynamics
+    from .dynamics import batch_groups, padded_samples
     sp = sampler or dynamics.default_sampler()
     B = np.asarray(B, float).reshape(3)
     if directions is None:
@@ -345,9 +324,9 @@ def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, d
     jobs = [(f, j) for f in range(len(fields)) for j in range(len(sel))]
     acc = [dict(Phi_S=0.0, Phi_T=0.0, B=np.zeros(3), J=0.0, D=np.zeros((3, 3)), kS=0.0, kT=0.0)
            for _ in fields]
-    sizes = [4 * sel[j][3] * _padded(zks[j].shape[0]) for _, j in jobs]
+    sizes = [4 * sel[j][3] * padded_samples(zks[j].shape[0]) for _, j in jobs]
     # states per vector entry held by the sweep: basis, checkpoints, segment, node states
-    for grp in _chunks(sizes, _budget_entries(sim.N_krylov + 6 + 8 * (n_quad + 1))):
+    for grp in batch_groups(sizes, _budget_entries(sim.N_krylov + 6 + 8 * (n_quad + 1))):
         systems = [sel[jobs[q][1]][2] for q in grp]
         got = sp.yield_gradient_batch(systems, [fields[jobs[q][0]] for q in grp], [zks[jobs[q][1]] for q in grp],
                                       sim.dt, sim.t_end, sim.N_krylov, n_quad=n_quad,

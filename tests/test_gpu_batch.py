@@ -154,3 +154,25 @@ def test_torch_tensor_entry_points(sampler, oracle):
         assert np.array_equal(got[j].cpu().numpy()[0], ref[j].P_S)
     with pytest.raises(TypeError):
         torch_ops.trace_sampling(sampler, torch.from_numpy(zk), DT, 20 * DT, 10, 1e-6)
+
+
+def test_job_runner_splits_by_device_memory(sampler, oracle, monkeypatch):
+    """trace_sampling_many with a memory budget of a few jobs: several
+    batches, every job against the oracle, in job order."""
+    from spin_dynamics_gb300 import dynamics
+
+    systems = [W.small_pair(), W.notebook_pair(), W.small_pair(), W.notebook_pair(), W.small_pair()]
+    fields = [0.05, 0.2, 0.3, 0.1, 0.15]
+    Ms = [40, 6, 33, 9, 64]
+    zks = [W.random_phase_samples(s.Z, M, seed=30 + i) for i, (s, M) in enumerate(zip(systems, Ms))]
+    m, t_end = 12, 20 * DT
+    # free memory of two dim-288 jobs' bases and states at this m and fraction
+    fake_free = 2 * 288 * 64 * 16.0 * (m + 4) / 0.5
+    monkeypatch.setattr(dynamics, "device_memory", lambda device=0: (fake_free, fake_free))
+    entries = [4 * s.Z * dynamics.padded_samples(M) for s, M in zip(systems, Ms)]
+    assert len(dynamics.batch_groups(entries, fake_free * 0.5 / (16.0 * (m + 4)))) >= 3
+    got = sampler.trace_sampling_many(systems, fields, zks, DT, t_end, m, 1e-6, mode="reference")
+    assert len(got) == len(systems)
+    for s, f, zk, g in zip(systems, fields, zks, got):
+        rp, col, val = iso_csr(oracle, s, f)
+        _check(g, oracle.trace_sampling(rp, col, val, zk, DT, t_end, m, 1e-6))

@@ -97,4 +97,5 @@ def test_selected_blocks_and_their_seeded_vectors():
     for (i, w, b, Zb, seed), z in zip(sel, zks):
         assert seed == (int(seeds[i - 1, 0]), int(seeds[i - 1, 1]))
         assert np.array_equal(z, seeded_samples(seed, Zb, 3))
-    assert S._chunks([5, 5, 5, 20, 1], 10) == [[0, 1], [2], [3], [4]]
+    from spin_dynamics_gb300.dynamics import batch_groups
+    assert batch_groups([5, 5, 5, 20, 1], 10) == [[0, 1], [2], [3], [4]]
