@@ -51,15 +51,16 @@ SPMM_TRAFFIC_PER_COLUMN = (180.1e6 - 33.2e6) / 64
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--steps", type=int, default=2)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--window-ns", type=float, default=100.0)
+    p.add_argument("--window-ns", type=float, default=2000.0)
     p.add_argument("--samples", type=int, default=512)
     p.add_argument("--krylov", type=int, default=30)
     p.add_argument("--method", default="auto", choices=["auto", "mgs", "lanczos"],
                    help="Krylov orthogonalisation: auto = Lanczos with MGS fallback when kS == kT")
-    p.add_argument("--cpu-samples", type=int, default=0, help="CPU sample size (0 = 12 x cores)")
+    p.add_argument("--cpu-samples", type=int, default=0,
+                   help="CPU sample size (0 = cores x max(1, 1200 / dt steps): one vector per core at 2 us)")
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-batch", action="store_true", help="skip the batched uneven-set leg")
@@ -113,23 +114,28 @@ def cpu_model() -> str:
     return "unknown"
 
 
-def cpu_leg(args, sysp, B, sim, threads):
-    """Time the oracle (fast build) on a bounded sample of the same workload."""
+def oracle_csr(sysp, B):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
     pyoracle.build()
     e1, e2 = sysp.e1, sysp.e2
-    rp, col, val = pyoracle.build_h_general(e1.g_I, e1.A, e1.gammas, e2.g_I, e2.A, e2.gammas, B,
-                                            sysp.J, sysp.D, sysp.kS, sysp.kT)
-    ns = args.cpu_samples or 12 * threads
+    return pyoracle, pyoracle.build_h_general(e1.g_I, e1.A, e1.gammas, e2.g_I, e2.A, e2.gammas, B,
+                                              sysp.J, sysp.D, sysp.kS, sysp.kT)
+
+
+def cpu_leg(args, sysp, B, sim, threads):
+    """Time the oracle (fast build) on a bounded sample of the same workload:
+    the whole window on fewer vectors (one per core at 2 us)."""
+    pyoracle, (rp, col, val) = oracle_csr(sysp, B)
+    steps = int(round(sim.t_end / sim.dt))
+    ns = args.cpu_samples or threads * max(1, round(1200 / steps))
     zk = W.random_phase_samples(sysp.Z, ns)
     t0 = time.perf_counter()
     r = pyoracle.trace_sampling(rp, col, val, zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol,
                                 fast=True, threads=threads)
     el = time.perf_counter() - t0
-    steps = int(round(sim.t_end / sim.dt))
-    cpu_leg.last = (zk, r)  # the vectors and oracle populations, for the accuracy check
+    cpu_leg.last = (sim, zk, r)  # the window, vectors and oracle populations, for the accuracy check
     return {"value": ns * steps / el, "unit": "sample-steps/s", "cores": threads, "kind": "port",
             "sample": f"{ns} samples x {steps} dt steps of the same system (Krylov builds "
                       f"{int(r['n_builds'].sum())}), oracle -O3 native OpenMP, {el:.2f} s, "
@@ -138,7 +144,7 @@ def cpu_leg(args, sysp, B, sim, threads):
 
 def accuracy_check(sysp, B, sim, zk, ref):
     """|Delta Phi_S| and max |Delta P_S| between the GPU path and the oracle on
-    the CPU leg's vectors (same system, window, m, tol)."""
+    the same vectors (same system, window, m, tol)."""
     from spin_dynamics_gb300.dynamics import TraceSampler
     from spin_dynamics_gb300.observables import Observables
 
@@ -150,7 +156,8 @@ def accuracy_check(sysp, B, sim, zk, ref):
     cpu.get_kinetics(sim.dt, sysp.kS, sysp.kT)
     return {"max_abs_dPhi_S": float(np.max(np.abs(got.Phi_S - cpu.Phi_S))),
             "max_abs_dP_S": float(np.max(np.abs(got.P_S - cpu.P_S))), "Phi_S": float(got.Phi_S[-1]),
-            "samples": int(zk.shape[0]), "bound": 1e-10,
+            "samples": int(zk.shape[0]), "window_ns": round(sim.t_end / sim.dt),
+            "bound": 1e-10,
             "reference": "oracle (C++ restatement of the Fortran path) on the same vectors"}
 
 
@@ -670,7 +677,7 @@ def main():
     accuracy = None
     if not args.no_cpu:
         cpu = cpu_leg(args, r["sysp"], r["B"], r["sim"], host_cores())
-        accuracy = accuracy_check(r["sysp"], r["B"], r["sim"], *cpu_leg.last)
+        accuracy = accuracy_check(r["sysp"], r["B"], *cpu_leg.last)
     share = {k: round(v[0] / max(1e-9, sum(x[0] for x in prof.values())), 4) for k, v in prof.items()}
     line = dict(base, value=r["value"], ms_per_step=r["ms"], scaling="weak",
                 config={"workload": workload_name(args, r["M"], r["sim"].N_krylov, r["sim"].tol),
