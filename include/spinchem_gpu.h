@@ -291,6 +291,15 @@ int spc_set_krylov(spc_handle* h, int method);
  * that do not fit one call). */
 int spc_mem_info(int device, int64_t* free_bytes, int64_t* total_bytes);
 
+/* Cap on the device memory one propagation call on this handle may hold
+ * (0, the default: the device's free memory, less a reserve). A call whose
+ * Krylov bases for every sample at once exceed it propagates its samples in
+ * consecutive chunks of 32-sample tiles within each build round; results
+ * agree with the unchunked call to rounding (per-sample reductions are
+ * grouped differently). SPC_ERR_ALLOC when one tile of the largest job does
+ * not fit. */
+int spc_set_memory_limit(spc_handle* h, int64_t bytes);
+
 /* Replay each build round of a propagation as a CUDA graph (1, the
  * default) or launch its kernels one by one (0). The launches of a round are
  * captured when a work-plan shape occurs for the second time within a call

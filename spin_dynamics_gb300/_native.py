@@ -88,6 +88,7 @@ SIGNATURES = {
     "spc_yield_gradient_batch": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _I, _I, _I, _D, _D, _I, _P, _P]),
     "spc_autotune_krylov": (_I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _D, _P, _I, _P, _P]),
     "spc_set_graphs": (_I, [_P, _I]),
+    "spc_set_memory_limit": (_I, [_P, C.c_int64]),
     "spc_mem_info": (_I, [_I, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "spc_set_profiling": (_I, [_P, _I]),
     "spc_get_profile": (_I, [_P, _I, C.POINTER(_D), C.POINTER(C.c_int64), C.POINTER(_D),

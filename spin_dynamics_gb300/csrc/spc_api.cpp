@@ -429,6 +429,13 @@ int spc_set_graphs(spc_handle* h, int enable) {
   return SPC_OK;
 }
 
+int spc_set_memory_limit(spc_handle* h, int64_t bytes) {
+  if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
+  if (bytes < 0) return spc::set_error(SPC_ERR_ARG, "negative memory limit %lld", (long long)bytes);
+  h->h.mem_limit = (size_t)bytes;
+  return SPC_OK;
+}
+
 int spc_set_profiling(spc_handle* h, int enable) {
   if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
   h->h.prof.on = enable != 0;

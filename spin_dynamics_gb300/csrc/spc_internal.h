@@ -129,6 +129,9 @@ struct Handle {
   int krylov_method = 0;
   // replay each build round's launches as a captured CUDA graph
   bool use_graphs = true;
+  // cap on the device bytes one propagation call may hold (0: the device's
+  // free memory decides)
+  size_t mem_limit = 0;
   // H_eff = (Hermitian) - i*kappa*1 for the current Hamiltonian: Lanczos applies
   bool herm_shift = false;
   bool lanczos_active() const {

@@ -1097,24 +1097,65 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     Zmax = std::max<int64_t>(Zmax, jobs[k].n / 4);
   }
   const int nsplit_max = (int)std::max<int64_t>(1, std::min<int64_t>(16, (Zmax + 63) / 64));
+  int nmax = 1;
+  for (const JobSpec& j : jobs) nmax = std::max(nmax, j.n);
+
+  // Samples in flight per build round. All of them when their Krylov bases
+  // and per-sample matrices fit the device (or the handle's memory limit);
+  // otherwise every round runs over consecutive chunks of whole 32-sample
+  // tiles, the capacities scaled down by one factor. States, populations and
+  // clocks stay resident for every sample either way.
+  const double slot_fixed = 16.0 * (6.0 * mm + m + 1 + (double)nsplit_max * ncombo) + 8.0 + 4.0 + 8.0;
+  const double need_fl = 16.0 * (double)(qcap + pcap) + slot_fixed * slots_cap +
+                         (double)(sizeof(TileInfo) + sizeof(unsigned)) * tiles_cap;
+  const double need_global = 16.0 * (double)psi_total + 8.0 * 4.0 * (double)T * G + 16.0 * G;
+  double budget;
+  {
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    double held = 0.0;
+    for (const Handle::Buf* b : {&h->Q, &h->P, &h->coef, &h->rbeta, &h->Ahess, &h->Aexp, &h->proj,
+                                 &h->projpart, &h->cvec, &h->flag, &h->plan, &h->counters, &h->psi,
+                                 &h->obs, &h->tt, &h->kk, &h->done})
+      held += (double)b->bytes;
+    budget = (double)free_b + held - need_global - (512.0 * (1 << 20) + 0.02 * (double)total_b);
+    if (h->mem_limit) budget = std::min(budget, (double)h->mem_limit - need_global);
+  }
+  int64_t qfl = qcap, pfl = pcap;
+  int slots_fl = slots_cap, tiles_fl = tiles_cap;
+  const bool chunked = need_fl > budget;
+  if (chunked) {
+    const double f = std::max(0.0, budget) / need_fl;
+    qfl = std::max<int64_t>((int64_t)(f * (double)qcap), (int64_t)m * nmax * SPC_LANES);
+    pfl = std::max<int64_t>((int64_t)(f * (double)pcap), (int64_t)nmax * SPC_LANES);
+    tiles_fl = std::max(1, (int)(f * tiles_cap));
+    slots_fl = tiles_fl * SPC_LANES;
+    const double fl = 16.0 * (double)(qfl + pfl) + slot_fixed * slots_fl +
+                      (double)(sizeof(TileInfo) + sizeof(unsigned)) * tiles_fl;
+    if (fl > budget)
+      return set_error(SPC_ERR_ALLOC,
+                       "one 32-sample tile of dimension %d at Krylov dimension %d needs %.3g bytes; "
+                       "%.3g are available",
+                       nmax, m, fl, std::max(0.0, budget));
+  }
   // upper bound on work items per round: one wave of the most resident kernel plus one per tile
-  const int items_cap = h->sm_count * 32 + tiles_cap;
-  if (h->ensure(h->psi, sizeof(double2) * psi_total) || h->ensure(h->Q, sizeof(double2) * qcap) ||
-      h->ensure(h->P, sizeof(double2) * pcap) ||
+  const int items_cap = h->sm_count * 32 + tiles_fl;
+  if (h->ensure(h->psi, sizeof(double2) * psi_total) || h->ensure(h->Q, sizeof(double2) * qfl) ||
+      h->ensure(h->P, sizeof(double2) * pfl) ||
       h->ensure(h->partial, sizeof(double2) * (size_t)items_cap * SPC_LANES) ||
-      h->ensure(h->counters, sizeof(unsigned) * tiles_cap) ||
-      h->ensure(h->coef, sizeof(double2) * slots_cap) || h->ensure(h->rbeta, sizeof(double) * slots_cap) ||
-      h->ensure(h->Ahess, sizeof(double2) * mm * slots_cap) ||
-      h->ensure(h->Aexp, sizeof(double2) * mm * slots_cap) ||
-      h->ensure(h->proj, sizeof(double2) * 4 * mm * slots_cap) ||
-      h->ensure(h->projpart, sizeof(double2) * (size_t)nsplit_max * slots_cap * ncombo +
+      h->ensure(h->counters, sizeof(unsigned) * tiles_fl) ||
+      h->ensure(h->coef, sizeof(double2) * slots_fl) || h->ensure(h->rbeta, sizeof(double) * slots_fl) ||
+      h->ensure(h->Ahess, sizeof(double2) * mm * slots_fl) ||
+      h->ensure(h->Aexp, sizeof(double2) * mm * slots_fl) ||
+      h->ensure(h->proj, sizeof(double2) * 4 * mm * slots_fl) ||
+      h->ensure(h->projpart, sizeof(double2) * (size_t)nsplit_max * slots_fl * ncombo +
                                  sizeof(unsigned) * ncombo) ||
-      h->ensure(h->cvec, sizeof(double2) * m * slots_cap) || h->ensure(h->tt, sizeof(double) * G) ||
+      h->ensure(h->cvec, sizeof(double2) * m * slots_fl) || h->ensure(h->tt, sizeof(double) * G) ||
       h->ensure(h->kk, sizeof(int) * G) || h->ensure(h->done, sizeof(int) * G) ||
       h->ensure(h->obs, sizeof(double) * 4 * (size_t)T * G) || h->ensure(h->err, 16) ||
-      h->ensure(h->flag, sizeof(int) * slots_cap) ||
-      h->ensure(h->plan, sizeof(TileInfo) * tiles_cap + sizeof(int2) * 2 * items_cap +
-                             sizeof(int) * 2 * slots_cap + 256) ||
+      h->ensure(h->flag, sizeof(int) * slots_fl) ||
+      h->ensure(h->plan, sizeof(TileInfo) * tiles_fl + sizeof(int2) * 2 * items_cap +
+                             sizeof(int) * 2 * slots_fl + 256) ||
       h->ensure(h->jobtab, (sizeof(JobInit) + sizeof(JobOut)) * nj + 64))
     return SPC_ERR_ALLOC;
   double2* d_psi = (double2*)h->psi.p;
@@ -1129,7 +1170,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   double2* d_proj = (double2*)h->proj.p;
   double2* d_ppart = (double2*)h->projpart.p;
   unsigned* d_combos =
-      (unsigned*)((char*)h->projpart.p + sizeof(double2) * (size_t)nsplit_max * slots_cap * ncombo);
+      (unsigned*)((char*)h->projpart.p + sizeof(double2) * (size_t)nsplit_max * slots_fl * ncombo);
   double2* d_c = (double2*)h->cvec.p;
   double* d_t = (double*)h->tt.p;
   int* d_k = (int*)h->kk.p;
@@ -1141,18 +1182,18 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   // per-round plan: tiles | pass items | SpMM items | map | scol
   char* plan = (char*)h->plan.p;
   TileInfo* d_tiles = (TileInfo*)plan;
-  int2* d_items_p = (int2*)(plan + sizeof(TileInfo) * tiles_cap);
+  int2* d_items_p = (int2*)(plan + sizeof(TileInfo) * tiles_fl);
   int2* d_items_s = d_items_p + items_cap;
   int* d_map = (int*)(d_items_s + items_cap);
-  int* d_scol = d_map + slots_cap;
+  int* d_scol = d_map + slots_fl;
   JobInit* d_jinit = (JobInit*)h->jobtab.p;
   JobOut* d_jout = (JobOut*)((char*)h->jobtab.p + sizeof(JobInit) * nj);
 
   int64_t launches0 = h->launches;
-  CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * tiles_cap, st));
+  CK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * tiles_fl, st));
   CK(cudaMemsetAsync(h->err.p, 0, 16, st));
   CK(cudaMemsetAsync(d_obs, 0, sizeof(double) * 4 * (size_t)T * G, st));
-  CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * slots_cap, st));
+  CK(cudaMemsetAsync(d_flag, 0, sizeof(int) * slots_fl, st));
   CK(cudaMemsetAsync(d_psi, 0, sizeof(double2) * psi_total, st));
   {
     std::vector<unsigned> combos(ncombo);
@@ -1238,7 +1279,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   std::vector<int> job_of(G);
   for (int k = 0; k < nj; ++k)
     for (int s = 0; s < jobs[k].M; ++s) job_of[base[k] + s] = k;
-  std::vector<int> done_h(G, 0), flag_h(slots_cap, 0);
+  std::vector<int> done_h(G, 0), flag_h(slots_fl, 0);
   int64_t builds = 0, rounds = 0, fallbacks = 0;
   const dim3 blk(SPC_LANES, SPC_WARPS);
   bool lanczos_ok = h->krylov_method == 1 || h->krylov_method == 2;
@@ -1312,13 +1353,13 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
       tiles[t].nis = cs[t];
     }
     const int nip = (int)items_p.size(), nis = (int)items_s.size();
-    if (nip > items_cap || nis > items_cap || ntiles > tiles_cap)
+    if (nip > items_cap || nis > items_cap || ntiles > tiles_fl || qo > qfl || po > pfl)
       return set_error(SPC_ERR_ARG, "internal: work plan exceeds its buffer");
     // one host->device copy of the plan
-    const size_t off_items_p = sizeof(TileInfo) * tiles_cap;
+    const size_t off_items_p = sizeof(TileInfo) * tiles_fl;
     const size_t off_items_s = off_items_p + sizeof(int2) * items_cap;
     const size_t off_map = off_items_s + sizeof(int2) * items_cap;
-    const size_t off_scol = off_map + sizeof(int) * slots_cap;
+    const size_t off_scol = off_map + sizeof(int) * slots_fl;
     const size_t plan_bytes = off_scol + sizeof(int) * nslots;
     hplan.resize(plan_bytes);
     std::memcpy(hplan.data(), tiles.data(), sizeof(TileInfo) * ntiles);
@@ -1525,16 +1566,43 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     return SPC_OK;
   };
 
-  std::vector<int> failed, failed2;
+  // end of the chunk of `list` starting at a: whole tiles (a job's run of
+  // samples in groups of 32, as the round forms them) while the Krylov
+  // bases, work vectors and tiles stay within the in-flight capacities
+  auto chunk_end = [&](const std::vector<int>& list, size_t a) -> size_t {
+    if (!chunked) return list.size();
+    int64_t q = 0, p = 0;
+    int nt = 0;
+    size_t c = a;
+    while (c < list.size()) {
+      const int k = job_of[list[c]];
+      size_t e = c;
+      while (e < list.size() && job_of[list[e]] == k && e - c < (size_t)SPC_LANES) ++e;
+      const int64_t dq = (int64_t)m * jobs[k].n * SPC_LANES, dp = (int64_t)jobs[k].n * SPC_LANES;
+      if (nt > 0 && (q + dq > qfl || p + dp > pfl || nt + 1 > tiles_fl)) break;
+      q += dq;
+      p += dp;
+      ++nt;
+      c = e;
+    }
+    return c;
+  };
+
+  std::vector<int> failed, failed2, chunk;
   while (!active.empty()) {
-    int rc = round(active, lanczos_ok, failed);
-    if (rc) return rc;
-    builds += (int64_t)active.size() - (int64_t)failed.size();
-    if (!failed.empty()) {
-      fallbacks += (int64_t)failed.size();
-      rc = round(failed, false, failed2);
+    for (size_t a = 0; a < active.size();) {
+      const size_t b = chunk_end(active, a);
+      chunk.assign(active.begin() + a, active.begin() + b);
+      a = b;
+      int rc = round(chunk, lanczos_ok, failed);
       if (rc) return rc;
-      builds += (int64_t)failed.size();
+      builds += (int64_t)chunk.size() - (int64_t)failed.size();
+      if (!failed.empty()) {
+        fallbacks += (int64_t)failed.size();
+        rc = round(failed, false, failed2);
+        if (rc) return rc;
+        builds += (int64_t)failed.size();
+      }
     }
     CK(cudaMemcpyAsync(done_h.data(), d_done, sizeof(int) * G, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

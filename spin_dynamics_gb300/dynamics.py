@@ -229,6 +229,12 @@ class TraceSampler:
         launch its kernels one by one; results are identical."""
         nat.check(nat.lib().spc_set_graphs(self._h, 1 if enable else 0))
 
+    def set_memory_limit(self, nbytes: int) -> None:
+        """Cap the device memory of one propagation call (0: the device's
+        free memory). Samples beyond it run in chunks of 32-sample tiles
+        within each build round."""
+        nat.check(nat.lib().spc_set_memory_limit(self._h, int(nbytes)))
+
     def set_krylov(self, method: str) -> None:
         """'mgs' (full modified Gram-Schmidt, the reference's get_krylov),
         'lanczos' (kS == kT only) or 'auto' (Lanczos when it applies)."""

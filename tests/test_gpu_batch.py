@@ -176,3 +176,37 @@ def test_job_runner_splits_by_device_memory(sampler, oracle, monkeypatch):
     for s, f, zk, g in zip(systems, fields, zks, got):
         rp, col, val = iso_csr(oracle, s, f)
         _check(g, oracle.trace_sampling(rp, col, val, zk, DT, t_end, m, 1e-6))
+
+
+def test_samples_beyond_the_memory_limit_run_in_chunks(sampler, oracle):
+    """A call whose Krylov bases exceed the handle's memory limit runs each
+    build round over chunks of 32-sample tiles: same results as the
+    unchunked call to rounding, the oracle within 1e-10; a limit below one
+    tile is refused."""
+    from spin_dynamics_gb300._native import SpcError
+
+    s = W.small_pair()
+    zk = W.random_phase_samples(s.Z, 200, seed=4)  # 7 tiles
+    t_end, m = 40 * DT, 20
+    sampler.build_h(s, 0.05, "reference")
+    whole = sampler.trace_sampling(zk, DT, t_end, m, 1e-6)
+    n_whole = sampler.stats()["kernel_launches"]
+    # about 2.9 tiles of bases and per-sample matrices (5.2 MB per tile at
+    # dim 288, m = 20) beside the states and populations
+    sampler.set_memory_limit(16 << 20)
+    try:
+        part = sampler.trace_sampling(zk, DT, t_end, m, 1e-6)
+        n_part = sampler.stats()["kernel_launches"]
+        sampler.set_memory_limit(4 << 20)
+        with pytest.raises(SpcError, match="32-sample tile"):
+            sampler.trace_sampling(zk, DT, t_end, m, 1e-6)
+    finally:
+        sampler.set_memory_limit(0)
+    assert n_part > n_whole
+    for k in ("P_S", "P_T0", "P_Tp", "P_Tm"):
+        assert np.max(np.abs(getattr(part, k) - getattr(whole, k))) < 1e-13, k
+    rp, col, val = iso_csr(oracle, s, 0.05)
+    _check(part, oracle.trace_sampling(rp, col, val, zk, DT, t_end, m, 1e-6))
+    # the handle is usable after the refusal
+    again = sampler.trace_sampling(zk[:40], DT, t_end, m, 1e-6)
+    _check(again, oracle.trace_sampling(rp, col, val, zk[:40], DT, t_end, m, 1e-6))
