@@ -264,6 +264,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
           x.split = (const int*)HB.split.p + HB.rp_off[sy];
           x.col = (const int*)HB.col.p + HB.nz_off[sy];
           x.val = (const double2*)HB.val.p + HB.nz_off[sy];
+          x.kappa = HB.herm[sy] ? &((const HMeta*)HB.meta.p)[sy].kappa : nullptr;
         }
         for (int l = 0; l < SPC_LANES; ++l) {
           const int s = c * SPC_LANES + l;
@@ -422,13 +423,20 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
   plan_items(tile_n, resident((const void*)k_spmm), fs, csn, items_s);
   const int nip = (int)items_p.size(), nis = (int)items_s.size();
   if (nip > items_cap || nis > items_cap) return set_error(SPC_ERR_ARG, "internal: work plan exceeds its buffer");
+  // SpMM work per sample column: all entries (bytes); FLOPs 8 per complex
+  // entry, 4 per real one (forward and adjoint Hamiltonians of a job share the
+  // pattern), plus 4 per row for the -i*kappa shift outside Lanczos
   int64_t nnz_tiles = 0;
+  double spmm_flops = 0.0, herm_rows = 0.0;
   for (int t = 0; t < ntiles; ++t) {
     tf[t].ip0 = tb[t].ip0 = fp[t];
     tf[t].nip = tb[t].nip = cp[t];
     tf[t].is0 = tb[t].is0 = fs[t];
     tf[t].nis = tb[t].nis = csn[t];
-    nnz_tiles += HB.nnz[jobs[tile_job[t]].sys];
+    const int sy = jobs[tile_job[t]].sys;
+    nnz_tiles += HB.nnz[sy];
+    spmm_flops += 8.0 * (double)HB.nnz_cplx[sy] + 4.0 * (double)(HB.nnz[sy] - HB.nnz_cplx[sy]);
+    if (HB.herm[sy]) herm_rows += tile_n[t];
   }
   CK(cudaMemcpyAsync(d_tf, tf.data(), sizeof(TileInfo) * ntiles, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d_tb, tb.data(), sizeof(TileInfo) * ntiles, cudaMemcpyHostToDevice, st));
@@ -498,8 +506,9 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
     h->count_launch(2);
     for (int i = 0; i < m; ++i) {
       pe = h->prof.begin(st);
-      k_spmm<<<nis, blk, 0, st>>>(tiles, d_items_s, d_map, i, d_Q, d_P);
-      h->prof.end(st, pe, PK_SPMM, 8.0 * (double)nnz_tiles * SPC_LANES, 20.0 * (double)nnz_tiles + 32.0 * elems);
+      k_spmm<<<nis, blk, 0, st>>>(tiles, d_items_s, d_map, i, d_Q, d_P, lanczos ? 0 : 1);
+      h->prof.end(st, pe, PK_SPMM, (spmm_flops + (lanczos ? 0.0 : 4.0 * herm_rows)) * SPC_LANES,
+                  20.0 * (double)nnz_tiles + 32.0 * elems);
       h->count_launch();
       pa.col_i = i;
       int j0 = 0;
@@ -509,8 +518,11 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
         pa.row_j = 0;
         pa.jx = 0;
         pe = h->prof.begin(st);
-        k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
-        h->prof.end(st, pe, PK_DOT, 8.0 * elems, 32.0 * elems);
+        if (lanczos)
+          k_rowpass<PASS_DOT, true><<<nip, blk, 0, st>>>(pa);
+        else
+          k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
+        h->prof.end(st, pe, PK_DOT, (lanczos ? 4.0 : 8.0) * elems, 32.0 * elems);
         h->count_launch();
       }
       for (int j = j0; j < i; ++j) {
@@ -518,16 +530,22 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
         pa.jn = j + 1;
         pa.row_j = j + 1;
         pe = h->prof.begin(st);
-        k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
-        h->prof.end(st, pe, PK_AXPY_DOT, 16.0 * elems, 64.0 * elems);
+        if (lanczos)
+          k_rowpass<PASS_AXPY_DOT, true><<<nip, blk, 0, st>>>(pa);
+        else
+          k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
+        h->prof.end(st, pe, PK_AXPY_DOT, (lanczos ? 8.0 : 16.0) * elems, 64.0 * elems);
         h->count_launch();
       }
       if (i < m - 1) {
         pa.jx = i;
         pa.row_j = i + 1;
         pe = h->prof.begin(st);
-        k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
-        h->prof.end(st, pe, PK_AXPY_NORM, 12.0 * elems, 48.0 * elems);
+        if (lanczos)
+          k_rowpass<PASS_AXPY_NORM, true><<<nip, blk, 0, st>>>(pa);
+        else
+          k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
+        h->prof.end(st, pe, PK_AXPY_NORM, (lanczos ? 8.0 : 12.0) * elems, 48.0 * elems);
         pe = h->prof.begin(st);
         k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 0, i + 1, pa.rbeta, d_Q);
         h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);

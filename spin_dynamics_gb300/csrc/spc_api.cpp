@@ -284,6 +284,8 @@ static int batch_jobs(spc_handle* h, int n_jobs, const int* job_sys, const int* 
     j.zk = zk_dev + zoff;
     j.out = out_dev + (size_t)k * 4 * T;
     j.herm_shift = B.herm[s] != 0;
+    j.kappa = j.herm_shift ? &((const spc::HMeta*)B.meta.p)[s].kappa : nullptr;
+    j.nnz_cplx = B.nnz_cplx[s];
     zoff += (int64_t)M[k] * (j.n / 4);
   }
   return SPC_OK;

@@ -348,6 +348,8 @@ struct BuildSlice {
   double2* xval;
   int* split;           // N
   long long* total;     // 1
+  bool herm;            // H = A - i*kappa*1: the execution copy holds A
+  HMeta* meta;          // kappa and complex-entry count of the copy (zeroed)
 };
 
 static int build_slices(Handle* h, std::vector<BuildSlice>& sl, const std::vector<int64_t>& predicted,
@@ -385,7 +387,7 @@ static int build_slices(Handle* h, std::vector<BuildSlice>& sl, const std::vecto
       k_ref_fill<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->ref, b.rowptr, b.col, b.val);
     else
       k_gen_fill_tab<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->gen, b.tab, b.rowptr, b.col, b.val);
-    enqueue_split_rows(N, b.rowptr, b.col, b.val, b.xcol, b.xval, b.split, st);
+    enqueue_split_rows(N, b.rowptr, b.col, b.val, b.xcol, b.xval, b.split, b.herm, b.meta, st);
     h->count_launch(2);
   }
   if (cudaStreamSynchronize(st) != cudaSuccess)
@@ -434,16 +436,24 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode) {
   if (rc) return rc;
   if (h->ensure_rowptr(N + 1) || h->ensure_h_entries(nnz) || h->ensure(h->bcnt, sizeof(int) * N) ||
       h->ensure(h->btot, sizeof(long long)) || h->ensure(h->xcol, sizeof(int) * std::max<int64_t>(nnz, 1)) ||
-      h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nnz, 1)) || h->ensure(h->xsplit, sizeof(int) * N))
+      h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nnz, 1)) || h->ensure(h->xsplit, sizeof(int) * N) ||
+      h->ensure(h->hmeta, sizeof(HMeta)))
     return SPC_ERR_ALLOC;
+  if (cudaMemsetAsync(h->hmeta.p, 0, sizeof(HMeta), h->stream) != cudaSuccess)
+    return set_error(SPC_ERR_CUDA, "Hamiltonian build failed");
   std::vector<BuildSlice> sl(1);
   sl[0] = BuildSlice{&hs, (const NucInfo*)h->bnuc.p, (const double2*)h->btab.p, (int*)h->bcnt.p, h->d_rowptr,
                      h->d_col, h->d_val,
-                     (int*)h->xcol.p, (double2*)h->xval.p, (int*)h->xsplit.p, (long long*)h->btot.p};
+                     (int*)h->xcol.p, (double2*)h->xval.p, (int*)h->xsplit.p, (long long*)h->btot.p,
+                     hs.herm_shift, (HMeta*)h->hmeta.p};
   rc = build_slices(h, sl, {nnz}, mode);
   if (rc) return rc;
+  HMeta meta{};
+  if (cudaMemcpy(&meta, h->hmeta.p, sizeof(HMeta), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return set_error(SPC_ERR_CUDA, "Hamiltonian build failed");
   h->n = (int)N;
   h->nnz = nnz;
+  h->nnz_cplx = (int64_t)meta.ncplx;
   h->herm_shift = hs.herm_shift;
   return SPC_OK;
 }
@@ -481,8 +491,11 @@ int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode)
       h->ensure(B.val, sizeof(double2) * std::max<int64_t>(nz_tot, 1)) ||
       h->ensure(h->xcol, sizeof(int) * std::max<int64_t>(nz_tot, 1)) ||
       h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nz_tot, 1)) ||
-      h->ensure(h->bcnt, sizeof(int) * std::max<int64_t>(n_tot, 1)) || h->ensure(h->btot, sizeof(long long) * ns))
+      h->ensure(h->bcnt, sizeof(int) * std::max<int64_t>(n_tot, 1)) || h->ensure(h->btot, sizeof(long long) * ns) ||
+      h->ensure(B.meta, sizeof(HMeta) * std::max<size_t>(ns, 1)))
     return SPC_ERR_ALLOC;
+  if (cudaMemsetAsync(B.meta.p, 0, sizeof(HMeta) * ns, h->stream) != cudaSuccess)
+    return set_error(SPC_ERR_CUDA, "Hamiltonian build failed");
   std::vector<BuildSlice> sl(ns);
   int64_t coff = 0;
   for (size_t k = 0; k < ns; ++k) {
@@ -490,10 +503,17 @@ int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode)
                        (int*)B.rowptr.p + B.rp_off[k], (int*)h->xcol.p + B.nz_off[k],
                        (double2*)h->xval.p + B.nz_off[k], (int*)B.col.p + B.nz_off[k],
                        (double2*)B.val.p + B.nz_off[k], (int*)B.split.p + B.rp_off[k],
-                       (long long*)h->btot.p + k};
+                       (long long*)h->btot.p + k, hs[k].herm_shift, (HMeta*)B.meta.p + k};
     coff += hs[k].N;
   }
   rc = build_slices(h, sl, B.nnz, mode);
+  B.nnz_cplx.assign(ns, 0);
+  if (!rc && ns) {
+    std::vector<HMeta> meta(ns);
+    if (cudaMemcpy(meta.data(), B.meta.p, sizeof(HMeta) * ns, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = set_error(SPC_ERR_CUDA, "Hamiltonian build failed");
+    for (size_t k = 0; k < ns; ++k) B.nnz_cplx[k] = (int64_t)meta[k].ncplx;
+  }
   // the single-Hamiltonian execution copy (xcol/xval) served as scratch
   h->n = 0;
   h->nnz = 0;

@@ -67,7 +67,7 @@ int Handle::ensure_h_entries(size_t count) {
 Handle::~Handle() {
   Buf* all[] = {&psi, &Q,  &P,    &partial, &counters, &coef, &rbeta, &Ahess, &Aexp, &proj, &projpart,
                 &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag, &xcol, &xval, &xsplit, &plan, &jobtab,
-                &hb.rowptr, &hb.split, &hb.col, &hb.val, &gck, &gseg, &gnu, &gmu, &glam, &cvec2,
+                &hmeta, &hb.rowptr, &hb.split, &hb.col, &hb.val, &hb.meta, &gck, &gseg, &gnu, &gmu, &glam, &cvec2,
                 &gslots, &gracc, &gfacc, &bcnt, &bnuc, &btot, &btab, &tune_out, &tune_zk};
   for (Buf* b : all)
     if (b->p) cudaFree(b->p);

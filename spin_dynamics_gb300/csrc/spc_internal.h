@@ -92,6 +92,13 @@ struct Prof {
   ~Prof();
 };
 
+// Per-system facts of a Hamiltonian's execution copy, written on the device
+// by the row split.
+struct HMeta {
+  double kappa;              // H_eff = A - i*kappa*1 (systems with herm_shift)
+  unsigned long long ncplx;  // entries with a nonzero imaginary part
+};
+
 struct Handle {
   Prof prof;
   int device = 0;
@@ -104,13 +111,15 @@ struct Handle {
   int* d_col = nullptr;
   double2* d_val = nullptr;
   size_t cap_rowptr = 0, cap_h = 0;
+  // execution copy of the Hamiltonian: kappa and complex-entry count (HMeta)
+  int64_t nnz_cplx = 0;
   // propagation workspace (grow-only)
   struct Buf {
     void* p = nullptr;
     size_t bytes = 0;
   };
   Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
-      map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit, plan, jobtab;
+      map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit, plan, jobtab, hmeta;
   // Hamiltonian build scratch: row counts, nucleus tables, nonzero totals
   Buf bcnt, bnuc, btot, btab;
   // autotuner outputs and sample subsets
@@ -123,7 +132,8 @@ struct Handle {
     std::vector<int> n;
     std::vector<int64_t> nnz, rp_off, nz_off;
     std::vector<char> herm;
-    Buf rowptr, split, col, val;
+    std::vector<int64_t> nnz_cplx;
+    Buf rowptr, split, col, val, meta;  // meta: one HMeta per system
   } hb;
   // Krylov method: 0 full MGS (the reference's get_krylov), 1 Lanczos, 2 auto
   int krylov_method = 0;
@@ -163,6 +173,10 @@ struct JobSpec {
   const double2* zk = nullptr;  // device, M x n/4 complex, sample-major
   double* out = nullptr;        // device, 4*T
   bool herm_shift = false;
+  // herm_shift: the execution copy holds the Hermitian part (real diagonal)
+  // and kappa (device) the shift, H_eff = A - i*kappa*1
+  const double* kappa = nullptr;
+  int64_t nnz_cplx = 0;  // entries of the execution copy with a nonzero imaginary part
 };
 
 // One reduced-matrix slot of the yield gradient: the electron pair (G = 4,
@@ -193,8 +207,11 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode);
 // the handle's single Hamiltonian is left unset.
 int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode);
 // Row split of a CSR for k_spmm (complex entries first), enqueued on st.
+// herm: H = A - i*kappa*1 with A Hermitian; the copy then holds A (diagonal
+// entries real) and meta->kappa the shift. meta->ncplx (zeroed by the caller)
+// receives the copy's count of entries with a nonzero imaginary part.
 void enqueue_split_rows(int64_t N, const int* rowptr, const int* col, const double2* val, int* xcol,
-                        double2* xval, int* split, cudaStream_t st);
+                        double2* xval, int* split, bool herm, HMeta* meta, cudaStream_t st);
 int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev,
               int M, double dt, double t_end, int m, double tol, double* out_dev, int T);
 int propagate_batch(Handle* h, const double* theta, const double* init_pop,

@@ -57,6 +57,9 @@ struct TileInfo {
   const int* split;
   const int* col;
   const double2* val;
+  // non-null: the execution copy holds the Hermitian part A of
+  // H_eff = A - i*kappa*1 (real diagonal) and *kappa the shift
+  const double* kappa;
 };
 
 enum PassKind { PASS_NORM_GATHER = 0, PASS_DOT = 1, PASS_AXPY_DOT = 2, PASS_AXPY_NORM = 3 };
@@ -80,8 +83,11 @@ struct PassArgs {
   unsigned* counters; // per tile
 };
 
-template <int KIND>
-__device__ __forceinline__ void pass_finalize(const PassArgs& a, int w, double2 tot) {
+// REAL: the Hermitian Lanczos recurrence on A of H_eff = A - i*kappa*1
+// (tile's kappa non-null): every coefficient is real, the dots keep their real
+// part, and the tridiagonal's diagonal gets the shift: alpha - i*kappa.
+template <int KIND, bool REAL>
+__device__ __forceinline__ void pass_finalize(const PassArgs& a, int w, double2 tot, const double* kappa) {
   const size_t mm = (size_t)a.m * a.m;
   if (KIND == PASS_NORM_GATHER) {
     double b = sqrt(tot.x);
@@ -90,8 +96,13 @@ __device__ __forceinline__ void pass_finalize(const PassArgs& a, int w, double2 
     for (int j = 1; j < a.m; ++j) c[j] = cz();
     a.rbeta[w] = b > 0.0 ? 1.0 / b : 0.0;
   } else if (KIND == PASS_DOT || KIND == PASS_AXPY_DOT) {
-    a.coef[w] = tot;
-    a.Ahess[(size_t)w * mm + a.row_j + (size_t)a.col_i * a.m] = tot;
+    if (REAL) {
+      a.coef[w] = make_double2(tot.x, 0.0);
+      a.Ahess[(size_t)w * mm + a.row_j + (size_t)a.col_i * a.m] = make_double2(tot.x, -*kappa);
+    } else {
+      a.coef[w] = tot;
+      a.Ahess[(size_t)w * mm + a.row_j + (size_t)a.col_i * a.m] = tot;
+    }
   } else {  // PASS_AXPY_NORM: A(i+1, i) = ||p||, and 1/||p|| for the scale
     double b = sqrt(tot.x);
     a.Ahess[(size_t)w * mm + a.row_j + (size_t)a.col_i * a.m] = make_double2(b, 0.0);
@@ -107,8 +118,9 @@ __device__ __forceinline__ void pass_finalize(const PassArgs& a, int w, double2 
 }
 
 // One pass over the rows of a work item: element update + per-slot
-// reduction. Grid = pass items, block (32, SPC_WARPS).
-template <int KIND>
+// reduction. Grid = pass items, block (32, SPC_WARPS). REAL (Lanczos on the
+// Hermitian part): real coefficients (2 DFMA per axpy) and real dots.
+template <int KIND, bool REAL = false>
 __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
   __shared__ double2 red[SPC_WARPS][SPC_LANES];
   __shared__ bool am_last;
@@ -137,7 +149,13 @@ __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
       const double2* P = a.P + T.p_off + tx;
       for (int r = it.y * SPC_WARPS + ty; r < n; r += stride) {
         const size_t o = (size_t)r * SPC_LANES;
-        acc = cjfma(X[o], P[o], acc);
+        if (REAL) {
+          const double2 x = X[o], p = P[o];
+          acc.x = fma(x.x, p.x, acc.x);
+          acc.x = fma(x.y, p.y, acc.x);
+        } else {
+          acc = cjfma(X[o], P[o], acc);
+        }
       }
     } else {
       const double2 cf = a.coef[w];
@@ -146,10 +164,23 @@ __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
       double2* P = a.P + T.p_off + tx;
       for (int r = it.y * SPC_WARPS + ty; r < n; r += stride) {
         const size_t o = (size_t)r * SPC_LANES;
-        double2 p = cfms(cf, Qj[o], P[o]);
+        double2 p;
+        if (REAL) {
+          const double2 q = Qj[o], p0 = P[o];
+          p.x = fma(-cf.x, q.x, p0.x);
+          p.y = fma(-cf.x, q.y, p0.y);
+        } else {
+          p = cfms(cf, Qj[o], P[o]);
+        }
         P[o] = p;
         if (KIND == PASS_AXPY_DOT) {
-          acc = cjfma(Qn[o], p, acc);
+          if (REAL) {
+            const double2 q = Qn[o];
+            acc.x = fma(q.x, p.x, acc.x);
+            acc.x = fma(q.y, p.y, acc.x);
+          } else {
+            acc = cjfma(Qn[o], p, acc);
+          }
         } else {
           acc.x = fma(p.x, p.x, acc.x);
           acc.x = fma(p.y, p.y, acc.x);
@@ -183,7 +214,7 @@ __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
     double2 tot = red[0][tx];
 #pragma unroll
     for (int y = 1; y < SPC_WARPS; ++y) tot = cadd(tot, red[y][tx]);
-    if (act) pass_finalize<KIND>(a, w, tot);
+    if (act) pass_finalize<KIND, REAL>(a, w, tot, T.kappa);
     if (tx == 0) a.counters[it.x] = 0u;
   }
 }
@@ -223,14 +254,19 @@ __global__ void __launch_bounds__(256)
 // P_t = H Q_t[i] for the tile of a SpMM item; one warp per row at a time, the
 // row's (col, val) entries broadcast to all lanes. Rows are stored in the
 // execution order of k_split_rows: entries with a nonzero imaginary part
-// first (4 DFMA each), then real ones from split[r] on (2 DFMA each).
+// first (4 DFMA each), then real ones from split[r] on (2 DFMA each). A tile
+// whose copy holds the Hermitian part A of A - i*kappa*1 gets A x, plus
+// -i*kappa x when `shift` is set (full H_eff for MGS rounds; Lanczos rounds
+// run on A).
 __global__ void __launch_bounds__(256)
     k_spmm(const TileInfo* __restrict__ tiles, const int2* __restrict__ items,
            const int* __restrict__ map, int i, const double2* __restrict__ Q,
-           double2* __restrict__ Pout) {
+           double2* __restrict__ Pout, int shift) {
   const int2 it = items[blockIdx.x];
   const TileInfo& T = tiles[it.x];
   if (i >= T.m) return;
+  const bool sh = shift && T.kappa != nullptr;
+  const double kp = sh ? __ldg(T.kappa) : 0.0;
   const int tx = threadIdx.x;
   const bool act = map[it.x * SPC_LANES + tx] >= 0;
   const int n = T.n;
@@ -282,51 +318,80 @@ __global__ void __launch_bounds__(256)
         a0.y = fma(v0, x0.y, a0.y);
       }
     }
-    if (act) Y[(size_t)r * SPC_LANES] = cadd(a0, a1);
+    if (act) {
+      double2 y = cadd(a0, a1);
+      if (sh) {  // -i*kappa*x_r
+        const double2 xr = X[(size_t)r * SPC_LANES];
+        y.x = fma(kp, xr.y, y.x);
+        y.y = fma(-kp, xr.x, y.y);
+      }
+      Y[(size_t)r * SPC_LANES] = y;
+    }
   }
 }
 
 // Execution copy of a CSR for k_spmm: each row's entries reordered so that
 // those with a nonzero imaginary part come first (original order kept within
-// each class); split[r] is the index of the row's first real entry.
+// each class); split[r] is the index of the row's first real entry. herm
+// (H = A - i*kappa*1, A Hermitian): diagonal entries are stored with their
+// imaginary part removed (real class) and row 0's removed sum is kappa.
+// meta->ncplx counts the copy's complex entries.
 __global__ void k_split_rows(int64_t N, const int* __restrict__ rowptr, const int* __restrict__ col,
                              const double2* __restrict__ val, int* __restrict__ xcol,
-                             double2* __restrict__ xval, int* __restrict__ split) {
+                             double2* __restrict__ xval, int* __restrict__ split, int herm,
+                             HMeta* __restrict__ meta) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= N) return;
-  const int k0 = rowptr[r], k1 = rowptr[r + 1];
-  int o = k0;
-  for (int k = k0; k < k1; ++k)
-    if (val[k].y != 0.0) {
-      xcol[o] = col[k];
-      xval[o] = val[k];
-      o++;
-    }
-  split[r] = o;
-  for (int k = k0; k < k1; ++k)
-    if (val[k].y == 0.0) {
-      xcol[o] = col[k];
-      xval[o] = val[k];
-      o++;
-    }
+  unsigned long long nc = 0;
+  if (r < N) {
+    const int k0 = rowptr[r], k1 = rowptr[r + 1];
+    auto cplx = [&](int k) { return val[k].y != 0.0 && !(herm && col[k] == r); };
+    int o = k0;
+    for (int k = k0; k < k1; ++k)
+      if (cplx(k)) {
+        xcol[o] = col[k];
+        xval[o] = val[k];
+        o++;
+      }
+    split[r] = o;
+    nc = (unsigned long long)(o - k0);
+    double shift = 0.0;
+    for (int k = k0; k < k1; ++k)
+      if (!cplx(k)) {
+        xcol[o] = col[k];
+        xval[o] = herm ? make_double2(val[k].x, 0.0) : val[k];
+        if (herm && col[k] == r) shift += val[k].y;
+        o++;
+      }
+    if (herm && r == 0) meta->kappa = -shift;
+  }
+  for (int d = 16; d > 0; d >>= 1) nc += __shfl_down_sync(0xffffffffu, nc, d);
+  if ((threadIdx.x & 31) == 0 && nc) atomicAdd(&meta->ncplx, nc);
 }
 
 void enqueue_split_rows(int64_t N, const int* rowptr, const int* col, const double2* val, int* xcol,
-                        double2* xval, int* split, cudaStream_t st) {
-  if (N > 0) k_split_rows<<<(int)((N + 255) / 256), 256, 0, st>>>(N, rowptr, col, val, xcol, xval, split);
+                        double2* xval, int* split, bool herm, HMeta* meta, cudaStream_t st) {
+  if (N > 0)
+    k_split_rows<<<(int)((N + 255) / 256), 256, 0, st>>>(N, rowptr, col, val, xcol, xval, split,
+                                                          herm ? 1 : 0, meta);
 }
 
 int prepare_spmm_rows(Handle* h) {
   const int64_t N = h->n, nnz = h->nnz;
   if (h->ensure(h->xcol, sizeof(int) * (nnz > 0 ? nnz : 1)) ||
-      h->ensure(h->xval, sizeof(double2) * (nnz > 0 ? nnz : 1)) || h->ensure(h->xsplit, sizeof(int) * N))
+      h->ensure(h->xval, sizeof(double2) * (nnz > 0 ? nnz : 1)) || h->ensure(h->xsplit, sizeof(int) * N) ||
+      h->ensure(h->hmeta, sizeof(HMeta)))
     return SPC_ERR_ALLOC;
-  k_split_rows<<<(int)((N + 255) / 256), 256, 0, h->stream>>>(
-      N, h->d_rowptr, h->d_col, h->d_val, (int*)h->xcol.p, (double2*)h->xval.p, (int*)h->xsplit.p);
+  HMeta meta{};
+  if (cudaMemsetAsync(h->hmeta.p, 0, sizeof(HMeta), h->stream) != cudaSuccess)
+    return set_error(SPC_ERR_CUDA, "row split of the Hamiltonian failed");
+  enqueue_split_rows(N, h->d_rowptr, h->d_col, h->d_val, (int*)h->xcol.p, (double2*)h->xval.p,
+                     (int*)h->xsplit.p, h->herm_shift, (HMeta*)h->hmeta.p, h->stream);
   h->count_launch();
-  cudaError_t e = cudaStreamSynchronize(h->stream);
+  cudaError_t e = cudaMemcpyAsync(&meta, h->hmeta.p, sizeof(HMeta), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess)
     return set_error(SPC_ERR_CUDA, "row split of the Hamiltonian failed: %s", cudaGetErrorString(e));
+  h->nnz_cplx = (int64_t)meta.ncplx;
   return SPC_OK;
 }
 
@@ -1322,6 +1387,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
         ti.split = jobs[k].split;
         ti.col = jobs[k].col;
         ti.val = jobs[k].val;
+        ti.kappa = jobs[k].herm_shift ? jobs[k].kappa : nullptr;
         ti.m = std::min(m, ti.n);
         qo += (int64_t)m * ti.n * SPC_LANES;
         po += (int64_t)ti.n * SPC_LANES;
@@ -1420,8 +1486,16 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
       pa.partial = d_part;
       pa.counters = d_cnt;
       pa.lanczos = lanczos ? 1 : 0;
+      // SpMM work of the round: all entries (bytes) and FLOPs (8 per complex
+      // entry, 4 per real one, 4 per row for the -i*kappa shift of MGS rounds)
       int64_t nnz_work = 0;
-      for (const TileInfo& ti : tiles) nnz_work += (int64_t)(jobs[ti.job].nnz);
+      double spmm_flops = 0.0;
+      for (const TileInfo& ti : tiles) {
+        const JobSpec& J = jobs[ti.job];
+        nnz_work += J.nnz;
+        spmm_flops += 8.0 * (double)J.nnz_cplx + 4.0 * (double)(J.nnz - J.nnz_cplx) +
+                      (!lanczos && ti.kappa ? 4.0 * ti.n : 0.0);
+      }
       int pe = h->prof.begin(st);
       k_rowpass<PASS_NORM_GATHER><<<nip, blk, 0, st>>>(pa);
       h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
@@ -1431,10 +1505,9 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
       h->count_launch(2);
       for (int i = 0; i < m; ++i) {
         pe = h->prof.begin(st);
-        k_spmm<<<nis, blk, 0, st>>>(d_tiles, d_items_s, d_map, i, d_Q, d_P);
+        k_spmm<<<nis, blk, 0, st>>>(d_tiles, d_items_s, d_map, i, d_Q, d_P, lanczos ? 0 : 1);
         // algorithmic traffic: H once per tile, X once, Y once
-        h->prof.end(st, pe, PK_SPMM, 8.0 * (double)nnz_work * SPC_LANES,
-                    20.0 * (double)nnz_work + 32.0 * elems);
+        h->prof.end(st, pe, PK_SPMM, spmm_flops * SPC_LANES, 20.0 * (double)nnz_work + 32.0 * elems);
         h->count_launch();
         pa.col_i = i;
         // MGS (get_krylov :453-456) projects p on Q_0..Q_i in order. Lanczos
@@ -1447,8 +1520,11 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
           pa.row_j = 0;
           pa.jx = 0;
           pe = h->prof.begin(st);
-          k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
-          h->prof.end(st, pe, PK_DOT, 8.0 * elems, 32.0 * elems);
+          if (lanczos)
+            k_rowpass<PASS_DOT, true><<<nip, blk, 0, st>>>(pa);
+          else
+            k_rowpass<PASS_DOT><<<nip, blk, 0, st>>>(pa);
+          h->prof.end(st, pe, PK_DOT, (lanczos ? 4.0 : 8.0) * elems, 32.0 * elems);
           h->count_launch();
         }
         for (int j = j0; j < i; ++j) {
@@ -1456,16 +1532,22 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
           pa.jn = j + 1;
           pa.row_j = j + 1;
           pe = h->prof.begin(st);
-          k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
-          h->prof.end(st, pe, PK_AXPY_DOT, 16.0 * elems, 64.0 * elems);
+          if (lanczos)
+            k_rowpass<PASS_AXPY_DOT, true><<<nip, blk, 0, st>>>(pa);
+          else
+            k_rowpass<PASS_AXPY_DOT><<<nip, blk, 0, st>>>(pa);
+          h->prof.end(st, pe, PK_AXPY_DOT, (lanczos ? 8.0 : 16.0) * elems, 64.0 * elems);
           h->count_launch();
         }
         if (i < m - 1) {
           pa.jx = i;
           pa.row_j = i + 1;
           pe = h->prof.begin(st);
-          k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
-          h->prof.end(st, pe, PK_AXPY_NORM, 12.0 * elems, 48.0 * elems);
+          if (lanczos)
+            k_rowpass<PASS_AXPY_NORM, true><<<nip, blk, 0, st>>>(pa);
+          else
+            k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
+          h->prof.end(st, pe, PK_AXPY_NORM, (lanczos ? 8.0 : 12.0) * elems, 48.0 * elems);
           pe = h->prof.begin(st);
           k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 0, i + 1, d_rb,
                                        d_Q);
@@ -1650,6 +1732,8 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   j.split = (const int*)h->xsplit.p;
   j.col = (const int*)h->xcol.p;
   j.val = (const double2*)h->xval.p;
+  j.kappa = h->herm_shift ? &((const HMeta*)h->hmeta.p)->kappa : nullptr;
+  j.nnz_cplx = h->nnz_cplx;
   j.zk = (const double2*)zk_dev;
   j.out = out_dev;
   j.herm_shift = h->herm_shift;

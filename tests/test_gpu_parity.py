@@ -146,6 +146,33 @@ def test_large_pair_anisotropic(sampler, oracle):
     _compare(got, ref, sim.dt, sysp.kS, sysp.kT, oracle)
 
 
+@pytest.mark.parametrize("m", [47, 48])
+@pytest.mark.parametrize("method", ["mgs", "lanczos"])
+def test_largest_krylov_dimensions(sampler, oracle, m, method):
+    """The largest accepted Krylov dimensions (the largest expm and projector
+    shared-memory footprints, an odd size) at dim 55296 with anisotropic
+    couplings and at dim 288, both orthogonalisations."""
+    sampler.set_krylov(method)
+    try:
+        sysp, B = W.large_pair()
+        rp, col, val = general_csr(oracle, sysp, B)
+        zk = W.random_phase_samples(sysp.Z, 3, seed=m)
+        dt, t_end = 0.17608596, 60 * 0.17608596
+        ref = oracle.trace_sampling(rp, col, val, zk, dt, t_end, m, 1e-7)
+        sampler.build_h(sysp, B, "general")
+        got = sampler.trace_sampling(zk, dt, t_end, m, 1e-7)
+        _compare(got, ref, dt, sysp.kS, sysp.kT, oracle)
+        small = W.small_pair()
+        rp, col, val = iso_csr(oracle, small, 0.05)
+        zk = W.random_phase_samples(small.Z, 40, seed=m + 1)
+        ref = oracle.trace_sampling(rp, col, val, zk, dt, 400 * dt, m, 1e-9)
+        sampler.set_h(rp, col, val)
+        got = sampler.trace_sampling(zk, dt, 400 * dt, m, 1e-9)
+        _compare(got, ref, dt, small.kS, small.kT, oracle)
+    finally:
+        sampler.set_krylov("mgs")
+
+
 @pytest.mark.parametrize("M", [1, 33, 70])
 def test_ragged_sample_counts(sampler, oracle, M):
     sysp, sim = W.small_pair(), W.small_sim(M=M, t_end_ns=300.0)
