@@ -97,3 +97,45 @@ def test_auto_uses_mgs_for_unequal_rates(sampler, oracle):
     finally:
         sampler.set_krylov("mgs")
     assert _max_err(got, ref) <= ABS_TOL
+
+
+@pytest.mark.parametrize("method", ["lanczos", "mgs"])
+def test_split_diagonal_shift_in_a_user_csr(sampler, oracle, method):
+    """A caller's CSR whose rows carry the Haberkorn shift in two duplicate
+    diagonal entries (a quarter and three quarters of -i*kbar/2): it is
+    Hermitian plus a scalar shift once duplicates are summed, so Lanczos
+    runs on the Hermitian part and MGS adds the shift back in the SpMM; both
+    match the oracle on the same CSR."""
+    sysp = W.small_pair()
+    rp, col, val = iso_csr(oracle, sysp, 0.05)
+    n = len(rp) - 1
+    rp2, col2, val2 = [0], [], []
+    for r in range(n):
+        ks = range(rp[r], rp[r + 1])
+        kap = -sum(val[k].imag for k in ks if col[k] == r)
+        first = True
+        for k in ks:
+            v = val[k]
+            col2.append(col[k])
+            if col[k] == r:
+                val2.append(complex(v.real, -0.25 * kap if first else 0.0))
+                first = False
+            else:
+                val2.append(v)
+        col2.append(r)
+        val2.append(complex(0.0, -0.75 * kap))
+        rp2.append(len(col2))
+    rp2, col2, val2 = np.array(rp2, np.int32), np.array(col2, np.int32), np.array(val2)
+    zk = W.random_phase_samples(sysp.Z, 40, seed=9)
+    dt = 0.17608596
+    ref = oracle.trace_sampling(rp2, col2, val2, zk, dt, 150 * dt, 16, 1e-7)
+    sampler.set_krylov(method)
+    try:
+        sampler.set_h(rp2, col2, val2)
+        got = sampler.trace_sampling(zk, dt, 150 * dt, 16, 1e-7)
+        fallbacks = sampler.stats()["lanczos_fallbacks"]
+    finally:
+        sampler.set_krylov("mgs")
+    assert _max_err(got, ref) <= ABS_TOL
+    if method == "lanczos":
+        assert fallbacks == 0
