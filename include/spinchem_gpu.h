@@ -291,6 +291,18 @@ int spc_set_krylov(spc_handle* h, int method);
  * that do not fit one call). */
 int spc_mem_info(int device, int64_t* free_bytes, int64_t* total_bytes);
 
+/* Propagation of small systems with one CTA per sample carrying the
+ * sample's whole run (every Krylov build, expm, projectors, dt loop) in one
+ * launch: SPC_SAMPLE_AUTO (default) when every job has at most 2048 rows,
+ * m <= 32, a build of about 2.5e6 FP64 FMAs or less and the samples fill at
+ * most two waves of CTAs; SPC_SAMPLE_OFF never; SPC_SAMPLE_ON whenever the
+ * call fits it (rows, m, shared and device memory). The tiled path serves
+ * every other call. Results agree with the tiled path to rounding. */
+#define SPC_SAMPLE_AUTO 0
+#define SPC_SAMPLE_OFF 1
+#define SPC_SAMPLE_ON 2
+int spc_set_sample_path(spc_handle* h, int mode);
+
 /* Cap on the device memory one propagation call on this handle may hold
  * (0, the default: the device's free memory, less a reserve). A call whose
  * Krylov bases for every sample at once exceed it propagates its samples in
@@ -346,7 +358,7 @@ int spc_set_profiling(spc_handle* h, int enable);
 /* Accumulated time (ms), launches, and the algorithmic FLOPs and bytes of
  * kernel class `kind` (0 <= kind < SPC_KERNEL_KINDS) since profiling was
  * enabled. */
-#define SPC_KERNEL_KINDS 13
+#define SPC_KERNEL_KINDS 14
 int spc_get_profile(const spc_handle* h, int kind, double* ms, int64_t* launches, double* flops,
                     double* bytes);
 

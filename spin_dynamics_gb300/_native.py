@@ -89,6 +89,7 @@ SIGNATURES = {
     "spc_autotune_krylov": (_I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _D, _P, _I, _P, _P]),
     "spc_set_graphs": (_I, [_P, _I]),
     "spc_set_memory_limit": (_I, [_P, C.c_int64]),
+    "spc_set_sample_path": (_I, [_P, _I]),
     "spc_mem_info": (_I, [_I, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "spc_set_profiling": (_I, [_P, _I]),
     "spc_get_profile": (_I, [_P, _I, C.POINTER(_D), C.POINTER(C.c_int64), C.POINTER(_D),
@@ -96,7 +97,8 @@ SIGNATURES = {
     "spc_kernel_kind_name": (C.c_char_p, [_I]),
     "spc_fp64_peak": (_I, [_I, C.POINTER(_D)]),
 }
-SPC_KERNEL_KINDS = 13
+SPC_KERNEL_KINDS = 14
+SPC_SAMPLE_AUTO, SPC_SAMPLE_OFF, SPC_SAMPLE_ON = 0, 1, 2
 
 _LIB: C.CDLL | None = None
 

@@ -431,6 +431,13 @@ int spc_set_graphs(spc_handle* h, int enable) {
   return SPC_OK;
 }
 
+int spc_set_sample_path(spc_handle* h, int mode) {
+  if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
+  if (mode < SPC_SAMPLE_AUTO || mode > SPC_SAMPLE_ON) return spc::set_error(SPC_ERR_ARG, "unknown sample-path mode %d", mode);
+  h->h.sample_path = mode;
+  return SPC_OK;
+}
+
 int spc_set_memory_limit(spc_handle* h, int64_t bytes) {
   if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
   if (bytes < 0) return spc::set_error(SPC_ERR_ARG, "negative memory limit %lld", (long long)bytes);

@@ -11,7 +11,7 @@ namespace spc {
 static const char* kKindNames[PROF_KINDS] = {"spmm",   "mgs_dot",    "mgs_axpy_dot", "mgs_axpy_norm",
                                              "scale",  "expm",       "projectors",   "proj_reduce",
                                              "dtloop", "psi_update", "setup",        "contract",
-                                             "costate"};
+                                             "costate", "sample_cta"};
 
 const char* prof_kind_name(int k) { return (k >= 0 && k < PROF_KINDS) ? kKindNames[k] : ""; }
 

@@ -67,6 +67,7 @@ enum ProfKind {
   PK_SETUP,
   PK_CONTRACT,
   PK_COSTATE,
+  PK_SAMPLE,  // one CTA per sample (small systems)
   PROF_KINDS
 };
 const char* prof_kind_name(int k);
@@ -142,6 +143,9 @@ struct Handle {
   // cap on the device bytes one propagation call may hold (0: the device's
   // free memory decides)
   size_t mem_limit = 0;
+  // one-CTA-per-sample kernel for small systems: 0 when it pays, 1 never,
+  // 2 whenever the call fits it
+  int sample_path = 0;
   // H_eff = (Hermitian) - i*kappa*1 for the current Hamiltonian: Lanczos applies
   bool herm_shift = false;
   bool lanczos_active() const {

@@ -529,28 +529,40 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
     }
     expm_sync<WARP>();
   }
-  // T = inv(D): column j solves LU x = P e_j
-  for (int j = tid; j < m; j += nt) {
-    double2* x = T + j * m;
-    for (int i = 0; i < m; ++i) x[i] = i == j ? make_double2(1.0, 0.0) : cz();
-    for (int k = 0; k < m; ++k)
-      if (piv[k] != k) {
-        const double2 t0 = x[k];
-        x[k] = x[piv[k]];
-        x[piv[k]] = t0;
-      }
-    for (int i = 0; i < m; ++i) {
-      double2 acc = x[i];
-      for (int k = 0; k < i; ++k) acc = cfms(D[i + k * m], x[k], acc);
-      x[i] = acc;
-    }
-    for (int i = m - 1; i >= 0; --i) {
-      double2 acc = x[i];
-      for (int k = i + 1; k < m; ++k) acc = cfms(D[i + k * m], x[k], acc);
-      x[i] = cdiv(acc, D[i + i * m]);
+  // T = inv(D): the columns of P (the row swaps applied to the identity),
+  // then the unit-lower and the upper triangular solves of all m columns as
+  // rank-1 updates over every (row, column) at once, one sync per step.
+  // Forward, an element gets its updates in the serial substitution's order
+  // (k ascending); backward, k descends from the last column.
+  int* perm = reinterpret_cast<int*>(rowsum);  // the row sums are spent
+  if (tid == 0) {
+    for (int i = 0; i < m; ++i) perm[i] = i;
+    for (int k = 0; k < m; ++k) {
+      const int a = perm[k];
+      perm[k] = perm[piv[k]];
+      perm[piv[k]] = a;
     }
   }
   expm_sync<WARP>();
+  for (int idx = tid; idx < mm; idx += nt) T[idx] = perm[idx % m] == idx / m ? make_double2(1.0, 0.0) : cz();
+  expm_sync<WARP>();
+  for (int k = 0; k + 1 < m; ++k) {
+    const int rem = m - k - 1;
+    for (int idx = tid; idx < rem * m; idx += nt) {
+      const int i = k + 1 + idx % rem, j = idx / rem;
+      T[i + j * m] = cfms(D[i + k * m], T[k + j * m], T[i + j * m]);
+    }
+    expm_sync<WARP>();
+  }
+  for (int k = m - 1; k >= 0; --k) {
+    for (int j = tid; j < m; j += nt) T[k + j * m] = cdiv(T[k + j * m], D[k + k * m]);
+    expm_sync<WARP>();
+    for (int idx = tid; idx < k * m; idx += nt) {
+      const int i = idx % k, j = idx / k;
+      T[i + j * m] = cfms(D[i + k * m], T[k + j * m], T[i + j * m]);
+    }
+    expm_sync<WARP>();
+  }
   // E = inv(D) E, then s squarings
   smem_matmul(m, T, E, X, tid, nt);
   expm_sync<WARP>();
@@ -1135,9 +1147,16 @@ static void plan_items(const std::vector<int>& tile_n, int resident, std::vector
   }
 }
 
+#include "spc_small.cuh"
+
 int propagate_batch(Handle* h, const double* theta, const double* init_pop,
                     const std::vector<JobSpec>& jobs, double dt, double t_end, int m, double tol,
                     int T) {
+  if (h->sample_path != SPC_SAMPLE_OFF) {
+    size_t smem = 0;
+    if (small_path_fits(h, jobs, m, T, smem))
+      return propagate_small(h, theta, init_pop, jobs, dt, t_end, m, tol, T, smem);
+  }
   auto t_start = std::chrono::steady_clock::now();
   cudaStream_t st = h->stream;
   const int nj = (int)jobs.size();

@@ -1,0 +1,572 @@
+// Small systems: one CTA carries one sample's whole propagation -- every
+// Krylov build, expm, projector Gram, dt loop and psi update until t_end --
+// in a single launch (trace_sampling_para's per-sample loop,
+// src/qm_dynamics.f90:322-378, with the CTA's threads over rows).
+//
+// Why: a system of a few hundred rows gives the tiled path (32 samples per
+// tile, one launch per phase) kernels of microseconds, so a build round of
+// ~90 launches is bound by launch and synchronisation latency, not by the
+// FP64 pipe. Here a sample's build is ~1e6 DFMA on its own SM with
+// block-level barriers only. Used when every job has at most SMALL_NMAX rows,
+// m <= 32 and the samples fill at most a few waves (propagate_batch).
+//
+// Per sample the arithmetic is the tiled path's: the SpMM row loop of k_spmm,
+// real-coefficient Lanczos on the Hermitian part (orthonormality checked from
+// the projector Grams, MGS rebuild when it fails) or MGS, expm_one, the four
+// Hermitian projector Grams, the reference's dt-loop semantics. Reductions
+// are two-level and in a fixed order (warp tree, then the warps in order), so
+// results repeat bit for bit; they differ from the tiled path's by rounding.
+// Control flow is uniform across the CTA: every barrier is reached by all
+// threads, and a sample leaves the loop only when the whole CTA does.
+#define SMALL_THREADS 256
+#define SMALL_WARPS (SMALL_THREADS / 32)
+#define SMALL_NC 16      // projector staging: rows per chunk
+#define SMALL_MAXC 9     // projector combinations per thread: 4 * 32 * 33 / 2 <= 9 * 256
+#define SMALL_MAX_M 32
+#define SMALL_NMAX 2048
+
+struct SmallJob {
+  int n, Z, me;            // rows, nuclear rows, Krylov dimension min(m, n)
+  const int* rowptr;       // execution-order CSR (k_split_rows)
+  const int* split;
+  const int* col;
+  const double2* val;
+  const double* kappa;     // non-null: the copy holds A of A - i*kappa*1
+  const double2* zk;       // M x Z sample vectors of the job
+};
+
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+
+// Sum over the CTA: warp trees, then the warps in order; every thread gets
+// the total. Called by all threads.
+__device__ __forceinline__ double2 block_sum2(double2 v, double2* red) {
+  v = warp_sum2(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double2 s = red[0];
+#pragma unroll
+  for (int w = 1; w < SMALL_WARPS; ++w) s = cadd(s, red[w]);
+  __syncthreads();
+  return s;
+}
+
+// y = H x for the rows r = tid, tid + nt, ... (k_spmm's per-row order);
+// shift adds -i*kappa*x_r.
+__device__ __forceinline__ void small_spmm(const SmallJob& J, const double2* __restrict__ x, double2* __restrict__ y,
+                                           bool shift, double kap) {
+  for (int r = threadIdx.x; r < J.n; r += SMALL_THREADS) {
+    const int k0 = __ldg(J.rowptr + r), ks = __ldg(J.split + r), k1 = __ldg(J.rowptr + r + 1);
+    double2 a0 = cz(), a1 = cz();
+    int k = k0;
+    for (; k + 1 < ks; k += 2) {
+      a0 = cfma(__ldg(J.val + k), x[__ldg(J.col + k)], a0);
+      a1 = cfma(__ldg(J.val + k + 1), x[__ldg(J.col + k + 1)], a1);
+    }
+    if (k < ks) {
+      a0 = cfma(__ldg(J.val + k), x[__ldg(J.col + k)], a0);
+      k++;
+    }
+    for (; k + 1 < k1; k += 2) {
+      const double v0 = __ldg(&J.val[k].x), v1 = __ldg(&J.val[k + 1].x);
+      const double2 x0 = x[__ldg(J.col + k)], x1 = x[__ldg(J.col + k + 1)];
+      a0.x = fma(v0, x0.x, a0.x);
+      a0.y = fma(v0, x0.y, a0.y);
+      a1.x = fma(v1, x1.x, a1.x);
+      a1.y = fma(v1, x1.y, a1.y);
+    }
+    if (k < k1) {
+      const double v0 = __ldg(&J.val[k].x);
+      const double2 x0 = x[__ldg(J.col + k)];
+      a0.x = fma(v0, x0.x, a0.x);
+      a0.y = fma(v0, x0.y, a0.y);
+    }
+    double2 yv = cadd(a0, a1);
+    if (shift) {
+      const double2 xr = x[r];
+      yv.x = fma(kap, xr.y, yv.x);
+      yv.y = fma(-kap, xr.x, yv.y);
+    }
+    y[r] = yv;
+  }
+}
+
+// The four projector Grams (k_proj + k_proj_reduce): P_t = V_t^H V_t over
+// the Z nuclear rows, V_0 = Q_|aa>, V_1 = Q_|ab> - Q_|ba> (S, halved),
+// V_2 = Q_|ab> + Q_|ba> (T0, halved), V_3 = Q_|bb>; staged SMALL_NC rows at
+// a time in V (4 m SMALL_NC complex). Ends with a barrier.
+__device__ void small_projectors(int m, int me, int n, int Z, const double2* __restrict__ Q, double2* P, double2* V) {
+  const int tid = threadIdx.x;
+  const size_t mm = (size_t)m * m;
+  const int nc4 = me * (me + 1) / 2, ncombo = 4 * nc4;
+  double2 acc[SMALL_MAXC];
+  int oi[SMALL_MAXC], oj[SMALL_MAXC], tq[SMALL_MAXC], iq[SMALL_MAXC], jq[SMALL_MAXC];
+#pragma unroll
+  for (int q = 0; q < SMALL_MAXC; ++q) {
+    acc[q] = cz();
+    oi[q] = oj[q] = tq[q] = iq[q] = jq[q] = 0;
+    const int cid = tid + q * SMALL_THREADS;
+    if (cid < ncombo) {
+      const int t = cid / nc4;
+      int rem = cid % nc4, i = 0;
+      while (rem >= me - i) {  // (i, j >= i) in row order
+        rem -= me - i;
+        ++i;
+      }
+      const int j = i + rem;
+      tq[q] = t;
+      iq[q] = i;
+      jq[q] = j;
+      oi[q] = (t * m + i) * SMALL_NC;
+      oj[q] = (t * m + j) * SMALL_NC;
+    }
+  }
+  for (int c0 = 0; c0 < Z; c0 += SMALL_NC) {
+    const int len = min(SMALL_NC, Z - c0);
+    for (int idx = tid; idx < me * SMALL_NC; idx += SMALL_THREADS) {
+      const int j = idx / SMALL_NC, nn = idx % SMALL_NC;
+      double2 q1 = cz(), q2 = cz(), q3 = cz(), q4 = cz();
+      if (nn < len) {
+        const double2* base = Q + (size_t)j * n + c0 + nn;
+        q1 = base[0];
+        q2 = base[Z];
+        q3 = base[2 * Z];
+        q4 = base[3 * Z];
+      }
+      V[(0 * m + j) * SMALL_NC + nn] = q1;
+      V[(1 * m + j) * SMALL_NC + nn] = csub(q2, q3);
+      V[(2 * m + j) * SMALL_NC + nn] = cadd(q2, q3);
+      V[(3 * m + j) * SMALL_NC + nn] = q4;
+    }
+    __syncthreads();
+    for (int nn = 0; nn < len; ++nn) {
+#pragma unroll
+      for (int q = 0; q < SMALL_MAXC; ++q)
+        if (tid + q * SMALL_THREADS < ncombo) acc[q] = cjfma(V[oi[q] + nn], V[oj[q] + nn], acc[q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < SMALL_MAXC; ++q) {
+    if (tid + q * SMALL_THREADS < ncombo) {
+      const int t = tq[q], i = iq[q], j = jq[q];
+      double2 s = acc[q];
+      if (t == 1 || t == 2) s = make_double2(0.5 * s.x, 0.5 * s.y);
+      double2* Pt = P + t * mm;
+      Pt[i + j * m] = s;
+      if (i != j) Pt[j + i * m] = make_double2(s.x, -s.y);
+    }
+  }
+  __syncthreads();
+}
+
+// Grid: one CTA of SMALL_THREADS per sample (global sample s = blockIdx.x).
+// work + soff[s]: the sample's basis (m x n), work vector (n) and state (n).
+// Dynamic shared memory: A, E (m^2 each), P (4 m^2), c and c' (m each), and
+// max(5 m^2, 4 m SMALL_NC) of expm / projector scratch, all complex.
+__global__ void __launch_bounds__(SMALL_THREADS, 2)
+    k_small_prop(const SmallJob* __restrict__ jobs, const int* __restrict__ sjob, const int* __restrict__ scol,
+                 const int64_t* __restrict__ soff, double2* __restrict__ work, Theta th, int m, int T, double dt,
+                 double t_end, double tol, int lanczos, double* __restrict__ obs,
+                 long long* __restrict__ nsteps, unsigned long long* __restrict__ counts, int* __restrict__ err) {
+  extern __shared__ double2 smem[];
+  __shared__ double rowsum[SPC_MAX_M];
+  __shared__ int piv[SPC_MAX_M];
+  __shared__ int s_sh, p_sh;
+  __shared__ double2 red[SMALL_WARPS];
+  __shared__ double2 part[SMALL_WARPS][32];
+  __shared__ double terms[SMALL_WARPS];
+  __shared__ double cstat[2];
+
+  const int s = blockIdx.x;
+  const SmallJob J = jobs[sjob[s]];
+  const int n = J.n, Z = J.Z, me = J.me;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const size_t mm = (size_t)m * m;
+  double2* A = smem;
+  double2* E = A + mm;
+  double2* P = E + mm;
+  double2* cA = P + 4 * mm;
+  double2* cB = cA + m;
+  double2* X = cB + m;
+  double2* Q = work + soff[s];
+  double2* p = Q + (size_t)m * n;
+  double2* psi = p + n;
+  const bool herm = J.kappa != nullptr;
+  const double kap = herm ? *J.kappa : 0.0;
+  const double2* zk = J.zk + (size_t)scol[s] * Z;
+  double* o = obs + (size_t)s * 4 * T;
+
+  // psi_0 = theta (x) z (kron_vector)
+  for (int r = tid; r < n; r += SMALL_THREADS) psi[r] = cmul(th.v[r / Z], zk[r % Z]);
+  __syncthreads();
+  double t = 0.0;
+  int k = 1;  // outputs 0 hold the initial populations (k_obs_init)
+  long long steps = 0;
+  unsigned long long nb = 0, nf = 0;
+  bool done = !(0.0 < t_end);
+  while (!done) {
+    bool lz = lanczos != 0 && herm;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+      for (int i = tid; i < (int)mm; i += SMALL_THREADS) A[i] = cz();
+      // c = ||psi|| e_1, Q_0 = psi / ||psi|| (get_krylov :440-447)
+      double2 acc = cz();
+      for (int r = tid; r < n; r += SMALL_THREADS) {
+        const double2 x = psi[r];
+        acc.x = fma(x.x, x.x, acc.x);
+        acc.x = fma(x.y, x.y, acc.x);
+      }
+      const double b0 = sqrt(block_sum2(acc, red).x);
+      const double rb0 = b0 > 0.0 ? 1.0 / b0 : 0.0;
+      for (int r = tid; r < n; r += SMALL_THREADS) {
+        const double2 x = psi[r];
+        Q[r] = make_double2(x.x * rb0, x.y * rb0);
+      }
+      if (tid < m) cA[tid] = tid == 0 ? make_double2(b0, 0.0) : cz();
+      __syncthreads();
+      double beta = 0.0;
+      for (int i = 0; i < me; ++i) {
+        const double2* qi = Q + (size_t)i * n;
+        small_spmm(J, qi, p, !lz && herm, kap);
+        __syncthreads();
+        if (lz) {
+          // p -= beta_{i-1} Q_{i-1}; alpha_i = Re <Q_i, p>
+          double2 a2 = cz();
+          for (int r = tid; r < n; r += SMALL_THREADS) {
+            double2 pv = p[r];
+            if (i > 0) {
+              const double2 q = qi[r - n];
+              pv.x = fma(-beta, q.x, pv.x);
+              pv.y = fma(-beta, q.y, pv.y);
+              p[r] = pv;
+            }
+            const double2 x = qi[r];
+            a2.x = fma(x.x, pv.x, a2.x);
+            a2.x = fma(x.y, pv.y, a2.x);
+          }
+          const double alpha = block_sum2(a2, red).x;
+          if (tid == 0) A[i + i * m] = make_double2(alpha, -kap);
+          if (i < me - 1) {
+            double2 nr = cz();
+            for (int r = tid; r < n; r += SMALL_THREADS) {
+              const double2 q = qi[r];
+              double2 pv = p[r];
+              pv.x = fma(-alpha, q.x, pv.x);
+              pv.y = fma(-alpha, q.y, pv.y);
+              p[r] = pv;
+              nr.x = fma(pv.x, pv.x, nr.x);
+              nr.x = fma(pv.y, pv.y, nr.x);
+            }
+            beta = sqrt(block_sum2(nr, red).x);
+            if (tid == 0) {
+              A[(i + 1) + i * m] = make_double2(beta, 0.0);
+              A[i + (i + 1) * m] = make_double2(beta, 0.0);
+            }
+            const double rb = beta > 0.0 ? 1.0 / beta : 0.0;
+            double2* qn = Q + (size_t)(i + 1) * n;
+            for (int r = tid; r < n; r += SMALL_THREADS) {
+              const double2 pv = p[r];
+              qn[r] = make_double2(pv.x * rb, pv.y * rb);
+            }
+            __syncthreads();
+          }
+        } else {
+          // MGS (get_krylov :453-456): h_0 = <Q_0, p>; then p -= h_j Q_j
+          // fused with h_{j+1} = <Q_{j+1}, p>
+          double2 a2 = cz();
+          for (int r = tid; r < n; r += SMALL_THREADS) a2 = cjfma(Q[r], p[r], a2);
+          double2 hc = block_sum2(a2, red);
+          if (tid == 0) A[0 + i * m] = hc;
+          for (int j = 0; j < i; ++j) {
+            const double2* qj = Q + (size_t)j * n;
+            a2 = cz();
+            for (int r = tid; r < n; r += SMALL_THREADS) {
+              const double2 pv = cfms(hc, qj[r], p[r]);
+              p[r] = pv;
+              a2 = cjfma(qj[r + n], pv, a2);
+            }
+            hc = block_sum2(a2, red);
+            if (tid == 0) A[(j + 1) + i * m] = hc;
+          }
+          if (i < me - 1) {
+            double2 nr = cz();
+            for (int r = tid; r < n; r += SMALL_THREADS) {
+              const double2 pv = cfms(hc, qi[r], p[r]);
+              p[r] = pv;
+              nr.x = fma(pv.x, pv.x, nr.x);
+              nr.x = fma(pv.y, pv.y, nr.x);
+            }
+            const double b = sqrt(block_sum2(nr, red).x);
+            if (tid == 0) A[(i + 1) + i * m] = make_double2(b, 0.0);
+            const double rb = b > 0.0 ? 1.0 / b : 0.0;
+            double2* qn = Q + (size_t)(i + 1) * n;
+            for (int r = tid; r < n; r += SMALL_THREADS) {
+              const double2 pv = p[r];
+              qn[r] = make_double2(pv.x * rb, pv.y * rb);
+            }
+            __syncthreads();
+          }
+        }
+      }
+      small_projectors(m, me, n, Z, Q, P, X);
+      if (!lz) break;
+      // a Lanczos basis must be orthonormal: max |sum_t P_t - I| <= ORTHO_TOL
+      double mx = 0.0;
+      for (int id = tid; id < me * me; id += SMALL_THREADS) {
+        const int i = id % me, j = id / me;
+        const size_t x = (size_t)i + (size_t)j * m;
+        const double2 g = cadd(cadd(P[x], P[mm + x]), cadd(P[2 * mm + x], P[3 * mm + x]));
+        const double e = fmax(fabs(g.x - (i == j ? 1.0 : 0.0)), fabs(g.y));
+        mx = (e > mx || e != e) ? e : mx;
+      }
+      for (int d = 16; d > 0; d >>= 1) {
+        const double v = __shfl_xor_sync(0xffffffffu, mx, d);
+        mx = (v > mx || v != v) ? v : mx;
+      }
+      if (lane == 0) terms[warp] = mx;
+      __syncthreads();
+      double mall = terms[0];
+      for (int w = 1; w < SMALL_WARPS; ++w) mall = (terms[w] > mall || terms[w] != terms[w]) ? terms[w] : mall;
+      __syncthreads();
+      if (mall <= ORTHO_TOL) break;
+      nf++;
+      lz = false;  // rebuild this basis with full MGS
+    }
+    nb++;
+    expm_one<false>(me, m, A, E, dt, X, rowsum, piv, &s_sh, &p_sh, tid, SMALL_THREADS, err);
+    __syncthreads();
+    // dt loop (:348-364): c <- E c; P_X(t) = Re(c^H P_X c); stop when the
+    // last Krylov coordinate grows past tol or the window ends
+    double2* c = cA;
+    double2* cn = cB;
+    double c2 = 1.0, cm2 = 0.0;
+    while (cm2 <= tol * c2 && t < t_end) {
+      if (k >= T) {  // output full (guard; every thread takes it)
+        if (tid == 0) atomicExch(err, 1);
+        done = true;
+        break;
+      }
+      // c' = E c: warp w sums columns j = w, w + 8, ...; lane = row
+      double2 a = cz();
+      if (lane < me)
+        for (int j = warp; j < me; j += SMALL_WARPS) a = cfma(E[lane + j * m], c[j], a);
+      part[warp][lane] = a;
+      __syncthreads();
+      if (tid < me) {
+        double2 v = part[0][tid];
+        for (int w = 1; w < SMALL_WARPS; ++w) v = cadd(v, part[w][tid]);
+        cn[tid] = v;
+      }
+      __syncthreads();
+      // Re(c'^H P_t c') for the 4 types, two warps each: the Hermitian form as
+      // its diagonal plus twice the real part of the upper triangle, the
+      // (i <= j) pairs dealt round-robin over the type's 64 threads
+      {
+        const int ty = warp >> 1, h2 = ((warp & 1) << 5) | lane;
+        const double2* Pt = P + ty * mm;
+        double acc2 = 0.0;
+        const int npair = me * (me + 1) / 2;
+        int i = 0, rem = h2;
+        while (i < me && rem >= me - i) {
+          rem -= me - i;
+          ++i;
+        }
+        for (int pidx = h2; pidx < npair; pidx += 64) {
+          const int j = i + rem;
+          const double2 ci = cn[i], cj = cn[j];
+          const double2 pij = Pt[i + j * m];
+          // w = P_ij c_j; term = Re(conj(c_i) w)
+          const double wx = fma(pij.x, cj.x, -pij.y * cj.y), wy = fma(pij.x, cj.y, pij.y * cj.x);
+          const double tr = fma(ci.x, wx, ci.y * wy);
+          acc2 += (i == j) ? tr : 2.0 * tr;
+          rem += 64;
+          while (i < me && rem >= me - i) {
+            rem -= me - i;
+            ++i;
+          }
+        }
+        acc2 = warp_sum(acc2);
+        if (lane == 0) terms[warp] = acc2;
+        if (warp == 0) {
+          double nn = 0.0;
+          if (lane < me) nn = fma(cn[lane].x, cn[lane].x, cn[lane].y * cn[lane].y);
+          nn = warp_sum(nn);
+          if (lane == 0) {
+            cstat[0] = nn;
+            const double2 cmv = cn[me - 1];
+            cstat[1] = cmv.x * cmv.x + cmv.y * cmv.y;
+          }
+        }
+      }
+      __syncthreads();
+      if (tid < 4) {
+        const int slot = tid == 0 ? 2 : (tid == 1 ? 0 : (tid == 2 ? 1 : 3));  // proj type -> obs slot
+        o[slot * T + k] = terms[2 * tid] + terms[2 * tid + 1];
+      }
+      c2 = cstat[0];
+      cm2 = cstat[1];
+      double2* tmp = c;
+      c = cn;
+      cn = tmp;
+      t = t + dt;
+      k = k + 1;
+      steps++;
+    }
+    if (!done) done = !(t < t_end);
+    if (!done) {
+      // psi = Q c (:365)
+      for (int r = tid; r < n; r += SMALL_THREADS) {
+        double2 acc3 = cz();
+        for (int j = 0; j < me; ++j) acc3 = cfma(Q[(size_t)j * n + r], c[j], acc3);
+        psi[r] = acc3;
+      }
+    }
+    // c lives in cA or cB; the next build rewrites cA after a barrier
+    __syncthreads();
+  }
+  if (tid == 0) {
+    atomicAdd((unsigned long long*)nsteps, (unsigned long long)steps);
+    atomicAdd(&counts[0], nb);
+    atomicAdd(&counts[1], nf);
+  }
+}
+
+// Dynamic shared memory of k_small_prop for Krylov dimension m (bytes).
+static size_t small_smem_bytes(int m) {
+  const size_t mm = (size_t)m * m;
+  return sizeof(double2) * (6 * mm + 2 * (size_t)m + std::max<size_t>(5 * mm, 4 * (size_t)m * SMALL_NC));
+}
+
+// Whether a call runs on k_small_prop (sets smem). Rows, m, shared memory
+// and device memory must fit; in SPC_SAMPLE_AUTO mode also every job's build
+// must be small (an estimate of its FP64 FMAs: SpMM, passes, projectors,
+// expm) and the samples at most two waves of resident CTAs.
+static bool small_path_fits(Handle* h, const std::vector<JobSpec>& jobs, int m, int T, size_t& smem) {
+  if (m > SMALL_MAX_M || jobs.empty()) return false;
+  int64_t G = 0;
+  double bytes = 0.0, wmax = 0.0;
+  for (const JobSpec& j : jobs) {
+    if (j.n > SMALL_NMAX || j.n < 4 || j.M < 1) return false;
+    G += j.M;
+    bytes += 16.0 * (double)(m + 2) * j.n * j.M;
+    const double me = std::min(m, j.n), n = j.n;
+    wmax = std::max(wmax, 4.0 * me * (double)j.nnz + 16.0 * me * n + 2.0 * n * me * me + 48.0 * me * me * me);
+  }
+  if (G > INT32_MAX) return false;
+  bytes += 32.0 * T * (double)G + 16.0 * (double)G;
+  smem = small_smem_bytes(m);
+  if (smem > h->smem_optin) return false;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
+  double held = 0.0;
+  for (const Handle::Buf* b : {&h->Q, &h->obs, &h->tt, &h->kk, &h->done}) held += (double)b->bytes;
+  double budget = (double)free_b + held - (512.0 * (1 << 20) + 0.02 * (double)total_b);
+  if (h->mem_limit) budget = std::min(budget, (double)h->mem_limit);
+  if (bytes > budget) return false;
+  if (h->sample_path == SPC_SAMPLE_ON) return true;
+  if (cudaFuncSetAttribute(k_small_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return false;
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_small_prop, SMALL_THREADS, smem) != cudaSuccess) return false;
+  return wmax <= 2.5e6 && G <= 2LL * h->sm_count * std::max(1, b);
+}
+
+// propagate_batch on k_small_prop: one launch for every sample of every job,
+// then the per-job average (k_average).
+static int propagate_small(Handle* h, const double* theta, const double* init_pop, const std::vector<JobSpec>& jobs,
+                           double dt, double t_end, int m, double tol, int T, size_t smem) {
+  auto t_start = std::chrono::steady_clock::now();
+  cudaStream_t st = h->stream;
+  const int nj = (int)jobs.size();
+  int G = 0;
+  for (const JobSpec& j : jobs) G += j.M;
+  std::vector<SmallJob> sj(nj);
+  std::vector<JobOut> jo(nj);
+  std::vector<int> sjob(G), scol(G);
+  std::vector<int64_t> soff(G);
+  bool lanczos = h->krylov_method == 1 || h->krylov_method == 2;
+  int64_t wt = 0;
+  for (int k = 0, g = 0; k < nj; ++k) {
+    const JobSpec& j = jobs[k];
+    lanczos = lanczos && j.herm_shift;
+    sj[k] = SmallJob{j.n, j.n / 4, std::min(m, j.n), j.rowptr, j.split, j.col, j.val,
+                     j.herm_shift ? j.kappa : nullptr, j.zk};
+    jo[k] = JobOut{g, j.M, j.out};
+    for (int s = 0; s < j.M; ++s, ++g) {
+      sjob[g] = k;
+      scol[g] = s;
+      soff[g] = wt;
+      wt += (int64_t)(m + 2) * j.n;
+    }
+  }
+  // plan: jobs | sample -> job | sample -> column | sample -> work offset
+  const size_t o_sjob = sizeof(SmallJob) * nj;
+  const size_t o_scol = o_sjob + sizeof(int) * G;
+  const size_t o_soff = (o_scol + sizeof(int) * G + 7) / 8 * 8;
+  const size_t plan_bytes = o_soff + sizeof(int64_t) * G;
+  if (h->ensure(h->Q, sizeof(double2) * wt) || h->ensure(h->obs, sizeof(double) * 4 * (size_t)T * G) ||
+      h->ensure(h->tt, sizeof(double) * G) || h->ensure(h->kk, sizeof(int) * G) ||
+      h->ensure(h->done, sizeof(int) * G) || h->ensure(h->err, 32) || h->ensure(h->plan, plan_bytes) ||
+      h->ensure(h->jobtab, sizeof(JobOut) * nj + 64))
+    return SPC_ERR_ALLOC;
+  std::vector<char> hp(plan_bytes);
+  std::memcpy(hp.data(), sj.data(), sizeof(SmallJob) * nj);
+  std::memcpy(hp.data() + o_sjob, sjob.data(), sizeof(int) * G);
+  std::memcpy(hp.data() + o_scol, scol.data(), sizeof(int) * G);
+  std::memcpy(hp.data() + o_soff, soff.data(), sizeof(int64_t) * G);
+  char* plan = (char*)h->plan.p;
+  int64_t launches0 = h->launches;
+  CK(cudaMemcpyAsync(plan, hp.data(), plan_bytes, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->jobtab.p, jo.data(), sizeof(JobOut) * nj, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(h->err.p, 0, 32, st));
+  double* d_obs = (double*)h->obs.p;
+  // slots past a sample's last step stay zero, as the reference's arrays
+  CK(cudaMemsetAsync(d_obs, 0, sizeof(double) * 4 * (size_t)T * G, st));
+  k_obs_init<<<(G + 127) / 128, 128, 0, st>>>(G, T, init_pop[0], init_pop[1], init_pop[2], init_pop[3], d_obs,
+                                               (double*)h->tt.p, (int*)h->kk.p, (int*)h->done.p);
+  h->count_launch();
+  Theta th;
+  for (int e = 0; e < 4; ++e) th.v[e] = make_double2(theta[2 * e], theta[2 * e + 1]);
+  CK(cudaFuncSetAttribute(k_small_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int* d_err = (int*)h->err.p;
+  long long* d_nsteps = (long long*)((char*)h->err.p + 8);
+  unsigned long long* d_counts = (unsigned long long*)((char*)h->err.p + 16);
+  int pe = h->prof.begin(st);
+  k_small_prop<<<G, SMALL_THREADS, smem, st>>>((const SmallJob*)plan, (const int*)(plan + o_sjob),
+                                               (const int*)(plan + o_scol), (const int64_t*)(plan + o_soff),
+                                               (double2*)h->Q.p, th, m, T, dt, t_end, tol, lanczos ? 1 : 0, d_obs,
+                                               d_nsteps, d_counts, d_err);
+  h->prof.end(st, pe, PK_SAMPLE, 0.0, 0.0);
+  h->count_launch();
+  for (int j0 = 0; j0 < nj; j0 += 65535) {
+    const int cnt = std::min(65535, nj - j0);
+    k_average<<<dim3((4 * T + 255) / 256, cnt), 256, 0, st>>>((const JobOut*)h->jobtab.p, j0, T, d_obs);
+    h->count_launch();
+  }
+  CK(cudaGetLastError());
+  unsigned char eh[32];
+  CK(cudaMemcpyAsync(eh, h->err.p, 32, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  h->prof.collect();
+  int err0 = 0;
+  long long nsteps = 0;
+  unsigned long long counts[2] = {0, 0};
+  std::memcpy(&err0, eh, 4);
+  std::memcpy(&nsteps, eh + 8, 8);
+  std::memcpy(counts, eh + 16, 16);
+  h->stats.krylov_builds = (int64_t)counts[0];
+  h->stats.lanczos_fallbacks = (int64_t)counts[1];
+  h->stats.rounds = 1;
+  h->stats.sample_steps = nsteps;
+  h->stats.kernel_launches = h->launches - launches0;
+  h->stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  if (err0 == 1) return set_error(SPC_ERR_NUMERIC, "time index overflow: the dt loop ran past %d output slots", T);
+  if (err0 == 2) return set_error(SPC_ERR_NUMERIC, "singular Pade denominator in expm");
+  return SPC_OK;
+}

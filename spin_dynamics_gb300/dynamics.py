@@ -229,6 +229,12 @@ class TraceSampler:
         launch its kernels one by one; results are identical."""
         nat.check(nat.lib().spc_set_graphs(self._h, 1 if enable else 0))
 
+    def set_sample_path(self, mode: str) -> None:
+        """Small systems with one CTA per sample ('auto' when it pays, 'off',
+        'on' whenever the call fits it); results agree to rounding."""
+        code = {"auto": nat.SPC_SAMPLE_AUTO, "off": nat.SPC_SAMPLE_OFF, "on": nat.SPC_SAMPLE_ON}[mode]
+        nat.check(nat.lib().spc_set_sample_path(self._h, code))
+
     def set_memory_limit(self, nbytes: int) -> None:
         """Cap the device memory of one propagation call (0: the device's
         free memory). Samples beyond it run in chunks of 32-sample tiles

@@ -188,6 +188,7 @@ def test_samples_beyond_the_memory_limit_run_in_chunks(sampler, oracle):
     s = W.small_pair()
     zk = W.random_phase_samples(s.Z, 200, seed=4)  # 7 tiles
     t_end, m = 40 * DT, 20
+    sampler.set_sample_path("off")  # the tiled path's chunking
     sampler.build_h(s, 0.05, "reference")
     whole = sampler.trace_sampling(zk, DT, t_end, m, 1e-6)
     n_whole = sampler.stats()["kernel_launches"]
@@ -202,6 +203,7 @@ def test_samples_beyond_the_memory_limit_run_in_chunks(sampler, oracle):
             sampler.trace_sampling(zk, DT, t_end, m, 1e-6)
     finally:
         sampler.set_memory_limit(0)
+        sampler.set_sample_path("auto")
     assert n_part > n_whole
     for k in ("P_S", "P_T0", "P_Tp", "P_Tm"):
         assert np.max(np.abs(getattr(part, k) - getattr(whole, k))) < 1e-13, k

@@ -250,7 +250,8 @@ def test_exact_krylov_breakdown_gives_the_exact_answer(sampler, oracle):
 @pytest.mark.parametrize("method", ["mgs", "auto"])
 def test_graph_replay_equals_direct_launches(sampler, method):
     """Rounds replayed as captured CUDA graphs give the same bits as the
-    same launches issued one by one (single job and a batch)."""
+    same launches issued one by one (single job and a batch; the tiled path,
+    which small systems take only when the per-sample path is off)."""
     DT = 1.0 * GAMMA_E / 1000
     s = W.small_pair()
     zk = W.random_phase_samples(s.Z, 40, seed=12)
@@ -259,6 +260,7 @@ def test_graph_replay_equals_direct_launches(sampler, method):
     zb = W.random_phase_samples(nb.Z, 7, seed=13)
     out = {}
     sampler.set_krylov(method)
+    sampler.set_sample_path("off")
     try:
         for graphs in (False, True):
             sampler.set_graphs(graphs)
@@ -270,6 +272,7 @@ def test_graph_replay_equals_direct_launches(sampler, method):
     finally:
         sampler.set_graphs(True)
         sampler.set_krylov("mgs")
+        sampler.set_sample_path("auto")
     (a1, am, _), (b1, bm, rounds) = out[False], out[True]
     assert rounds > 2
     for k in ("P_S", "P_T0", "P_Tp", "P_Tm"):
