@@ -383,13 +383,21 @@ def batched_leg(args, sampler, local_rank):
     work = sum(Ms) * steps
     batched()  # first launches of the leg are the batched call's (allocation, page-in)
     t_single = timed(per_instance)
+    # the same per-instance calls kept on the tiled path (small jobs otherwise
+    # take the one-CTA-per-sample kernel)
+    sampler.set_sample_path("off")
+    try:
+        t_single_tiles = timed(per_instance)
+    finally:
+        sampler.set_sample_path("auto")
     breakdown = profiled(sampler, batched)
     t_batch = timed(batched)
     t_build = timed(lambda: [sampler.build_h_batch([systems[i] for i in grp], [fields[i] for i in grp], "general")
                              for grp in groups])
     dims = [4 * s.Z for s in systems]
     return {"value": work / t_batch, "per_instance_value": work / t_single,
-            "ratio": t_single / t_batch, "unit": "sample-steps/s", "jobs": len(zks),
+            "ratio": t_single / t_batch, "per_instance_tiled_value": work / t_single_tiles,
+            "ratio_vs_tiled_per_instance": t_single_tiles / t_batch, "unit": "sample-steps/s", "jobs": len(zks),
             "pairs": len(pairs), "orientations": len(dirs), "dims": [min(dims), max(dims)],
             "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m, "kernel_breakdown": breakdown,
             "seconds": t_batch, "build_seconds": t_build, "per_instance_seconds": t_single,

@@ -409,13 +409,20 @@ __device__ __forceinline__ void expm_sync() {
     __syncthreads();
 }
 
+// C = A B; each dot in two interleaved partial sums (even and odd k) so that
+// consecutive FMAs of a thread do not wait on each other.
 __device__ void smem_matmul(int m, const double2* A, const double2* B, double2* C, int tid, int nt) {
   const int mm = m * m;
   for (int idx = tid; idx < mm; idx += nt) {
     const int i = idx % m, j = idx / m;
-    double2 acc = cz();
-    for (int k = 0; k < m; ++k) acc = cfma(A[i + k * m], B[k + j * m], acc);
-    C[idx] = acc;
+    double2 a0 = cz(), a1 = cz();
+    int k = 0;
+    for (; k + 1 < m; k += 2) {
+      a0 = cfma(A[i + k * m], B[k + j * m], a0);
+      a1 = cfma(A[i + (k + 1) * m], B[(k + 1) + j * m], a1);
+    }
+    if (k < m) a0 = cfma(A[i + k * m], B[k + j * m], a0);
+    C[idx] = cadd(a0, a1);
   }
 }
 
@@ -456,34 +463,39 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
   expm_sync<WARP>();
   const int s = *s_sh;
   const double sc = ldexp(1.0, -s);  // A/2**s, exact
+  for (int i = tid; i < mm; i += nt) A2[i] = make_double2(A2[i].x * sc, A2[i].y * sc);
+  expm_sync<WARP>();
+  // Pade(6,6) numerator N = sum c_k a^k and denominator D = sum (-1)^k c_k a^k
+  // with the reference's coefficient recurrence (:54-77), evaluated from the
+  // even and odd parts (Paterson-Stockmeyer): a^2, a^4, a^6 and
+  // a (c1 + c3 a^2 + c5 a^4), four products instead of five
+  const int q = 6;
+  double ck[q + 1];
+  ck[0] = 1.0;
+  ck[1] = 0.5;
+  for (int k = 2; k <= q; ++k) ck[k] = ck[k - 1] * (double)(q - k + 1) / (double)(k * (2 * q - k + 1));
+  smem_matmul(m, A2, A2, X, tid, nt);  // a^2
+  expm_sync<WARP>();
+  smem_matmul(m, X, X, T, tid, nt);    // a^4
+  expm_sync<WARP>();
+  smem_matmul(m, T, X, D, tid, nt);    // a^6
+  expm_sync<WARP>();
   for (int i = tid; i < mm; i += nt) {
-    double2 a = make_double2(A2[i].x * sc, A2[i].y * sc);
-    A2[i] = a;
-    X[i] = a;
     const double id = (i % (m + 1) == 0) ? 1.0 : 0.0;
-    E[i] = make_double2(id + 0.5 * a.x, 0.5 * a.y);
-    D[i] = make_double2(id - 0.5 * a.x, -0.5 * a.y);
+    const double2 x2 = X[i], x4 = T[i], x6 = D[i];
+    E[i] = make_double2(id + ck[2] * x2.x + ck[4] * x4.x + ck[6] * x6.x, ck[2] * x2.y + ck[4] * x4.y + ck[6] * x6.y);
+    D[i] = make_double2(id * ck[1] + ck[3] * x2.x + ck[5] * x4.x, ck[3] * x2.y + ck[5] * x4.y);
   }
   expm_sync<WARP>();
-  // Pade(6,6) by the c_k recurrence (:54-77)
-  const int q = 6;
-  double c = 0.5;
-  bool p = true;
-  for (int k = 2; k <= q; ++k) {
-    c = c * (double)(q - k + 1) / (double)(k * (2 * q - k + 1));
-    smem_matmul(m, A2, X, T, tid, nt);
-    expm_sync<WARP>();
-    for (int i = tid; i < mm; i += nt) {
-      const double2 x = T[i];
-      X[i] = x;
-      E[i] = make_double2(E[i].x + c * x.x, E[i].y + c * x.y);
-      D[i] = p ? make_double2(D[i].x + c * x.x, D[i].y + c * x.y)
-               : make_double2(D[i].x - c * x.x, D[i].y - c * x.y);
-    }
-    p = !p;
-    expm_sync<WARP>();
+  smem_matmul(m, A2, D, X, tid, nt);   // odd part
+  expm_sync<WARP>();
+  for (int i = tid; i < mm; i += nt) {
+    const double2 ev = E[i], od = X[i];
+    T[i] = cadd(ev, od);  // N
+    D[i] = csub(ev, od);  // D
   }
-  // inv(D) by LU with partial pivoting (|re|+|im| pivot, as izamax), in place
+  expm_sync<WARP>();
+  // LU of D with partial pivoting (|re|+|im| pivot, as izamax), in place
   for (int k = 0; k < m; ++k) {
     if (tid < 32) {
       double best = -1.0;
@@ -529,11 +541,9 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
     }
     expm_sync<WARP>();
   }
-  // T = inv(D): the columns of P (the row swaps applied to the identity),
-  // then the unit-lower and the upper triangular solves of all m columns as
-  // rank-1 updates over every (row, column) at once, one sync per step.
-  // Forward, an element gets its updates in the serial substitution's order
-  // (k ascending); backward, k descends from the last column.
+  // E = D^-1 N: the rows of N permuted as the LU's row swaps (P N), then the
+  // unit-lower and the upper triangular solves of all m columns as rank-1
+  // updates over every (row, column) at once, one sync per step
   int* perm = reinterpret_cast<int*>(rowsum);  // the row sums are spent
   if (tid == 0) {
     for (int i = 0; i < m; ++i) perm[i] = i;
@@ -544,30 +554,26 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
     }
   }
   expm_sync<WARP>();
-  for (int idx = tid; idx < mm; idx += nt) T[idx] = perm[idx % m] == idx / m ? make_double2(1.0, 0.0) : cz();
+  for (int idx = tid; idx < mm; idx += nt) E[idx] = T[perm[idx % m] + (idx / m) * m];
   expm_sync<WARP>();
   for (int k = 0; k + 1 < m; ++k) {
     const int rem = m - k - 1;
     for (int idx = tid; idx < rem * m; idx += nt) {
       const int i = k + 1 + idx % rem, j = idx / rem;
-      T[i + j * m] = cfms(D[i + k * m], T[k + j * m], T[i + j * m]);
+      E[i + j * m] = cfms(D[i + k * m], E[k + j * m], E[i + j * m]);
     }
     expm_sync<WARP>();
   }
   for (int k = m - 1; k >= 0; --k) {
-    for (int j = tid; j < m; j += nt) T[k + j * m] = cdiv(T[k + j * m], D[k + k * m]);
+    for (int j = tid; j < m; j += nt) E[k + j * m] = cdiv(E[k + j * m], D[k + k * m]);
     expm_sync<WARP>();
     for (int idx = tid; idx < k * m; idx += nt) {
       const int i = idx % k, j = idx / k;
-      T[i + j * m] = cfms(D[i + k * m], T[k + j * m], T[i + j * m]);
+      E[i + j * m] = cfms(D[i + k * m], E[k + j * m], E[i + j * m]);
     }
     expm_sync<WARP>();
   }
-  // E = inv(D) E, then s squarings
-  smem_matmul(m, T, E, X, tid, nt);
-  expm_sync<WARP>();
-  for (int i = tid; i < mm; i += nt) E[i] = X[i];
-  expm_sync<WARP>();
+  // s squarings
   for (int k = 0; k < s; ++k) {
     smem_matmul(m, E, E, X, tid, nt);
     expm_sync<WARP>();

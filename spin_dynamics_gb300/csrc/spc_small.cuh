@@ -21,6 +21,7 @@
 #define SMALL_THREADS 256
 #define SMALL_WARPS (SMALL_THREADS / 32)
 #define SMALL_NC 16      // projector staging: rows per chunk
+#define SMALL_VS 17      // staging row stride (padded: rows of one chunk start in different banks)
 #define SMALL_MAXC 9     // projector combinations per thread: 4 * 32 * 33 / 2 <= 9 * 256
 #define SMALL_MAX_M 32
 #define SMALL_NMAX 2048
@@ -44,17 +45,20 @@ __device__ __forceinline__ double2 warp_sum2(double2 v) {
   return v;
 }
 
-// Sum over the CTA: warp trees, then the warps in order; every thread gets
-// the total. Called by all threads.
+// Sum over the CTA: warp trees, then warp 0 sums the warps' partials with the
+// same tree; every thread gets the total (red holds SMALL_WARPS + 1). Only
+// warp 0 spends FP64 adds on the second level. Called by all threads.
 __device__ __forceinline__ double2 block_sum2(double2 v, double2* red) {
   v = warp_sum2(v);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  double2 s = red[0];
-#pragma unroll
-  for (int w = 1; w < SMALL_WARPS; ++w) s = cadd(s, red[w]);
+  if (threadIdx.x < 32) {
+    double2 x = threadIdx.x < SMALL_WARPS ? red[threadIdx.x] : cz();
+    x = warp_sum2(x);
+    if (threadIdx.x == 0) red[SMALL_WARPS] = x;
+  }
   __syncthreads();
-  return s;
+  return red[SMALL_WARPS];
 }
 
 // y = H x for the rows r = tid, tid + nt, ... (k_spmm's per-row order);
@@ -100,19 +104,26 @@ __device__ __forceinline__ void small_spmm(const SmallJob& J, const double2* __r
 // The four projector Grams (k_proj + k_proj_reduce): P_t = V_t^H V_t over
 // the Z nuclear rows, V_0 = Q_|aa>, V_1 = Q_|ab> - Q_|ba> (S, halved),
 // V_2 = Q_|ab> + Q_|ba> (T0, halved), V_3 = Q_|bb>; staged SMALL_NC rows at
-// a time in V (4 m SMALL_NC complex). Ends with a barrier.
+// a time in V (4 m SMALL_VS complex). MAXC = ceil(combinations / threads)
+// exactly: a combination slot that no thread needs still issues its
+// (predicated-off) DFMAs. Ends with a barrier.
+template <int MAXC>
 __device__ void small_projectors(int m, int me, int n, int Z, const double2* __restrict__ Q, double2* P, double2* V) {
   const int tid = threadIdx.x;
   const size_t mm = (size_t)m * m;
   const int nc4 = me * (me + 1) / 2, ncombo = 4 * nc4;
-  double2 acc[SMALL_MAXC];
-  int oi[SMALL_MAXC], oj[SMALL_MAXC], tq[SMALL_MAXC], iq[SMALL_MAXC], jq[SMALL_MAXC];
+  // ceil(ncombo / MAXC) threads hold the combinations: the warps past them
+  // skip the accumulation instead of issuing predicated-off FMAs
+  const int nth = (ncombo + MAXC - 1) / MAXC;
+  const bool on = tid < nth;
+  double2 acc[MAXC];
+  int oi[MAXC], oj[MAXC], tq[MAXC], iq[MAXC], jq[MAXC];
 #pragma unroll
-  for (int q = 0; q < SMALL_MAXC; ++q) {
+  for (int q = 0; q < MAXC; ++q) {
     acc[q] = cz();
     oi[q] = oj[q] = tq[q] = iq[q] = jq[q] = 0;
-    const int cid = tid + q * SMALL_THREADS;
-    if (cid < ncombo) {
+    const int cid = tid + q * nth;
+    if (on && cid < ncombo) {
       const int t = cid / nc4;
       int rem = cid % nc4, i = 0;
       while (rem >= me - i) {  // (i, j >= i) in row order
@@ -123,8 +134,8 @@ __device__ void small_projectors(int m, int me, int n, int Z, const double2* __r
       tq[q] = t;
       iq[q] = i;
       jq[q] = j;
-      oi[q] = (t * m + i) * SMALL_NC;
-      oj[q] = (t * m + j) * SMALL_NC;
+      oi[q] = (t * m + i) * SMALL_VS;
+      oj[q] = (t * m + j) * SMALL_VS;
     }
   }
   for (int c0 = 0; c0 < Z; c0 += SMALL_NC) {
@@ -139,22 +150,23 @@ __device__ void small_projectors(int m, int me, int n, int Z, const double2* __r
         q3 = base[2 * Z];
         q4 = base[3 * Z];
       }
-      V[(0 * m + j) * SMALL_NC + nn] = q1;
-      V[(1 * m + j) * SMALL_NC + nn] = csub(q2, q3);
-      V[(2 * m + j) * SMALL_NC + nn] = cadd(q2, q3);
-      V[(3 * m + j) * SMALL_NC + nn] = q4;
+      V[(0 * m + j) * SMALL_VS + nn] = q1;
+      V[(1 * m + j) * SMALL_VS + nn] = csub(q2, q3);
+      V[(2 * m + j) * SMALL_VS + nn] = cadd(q2, q3);
+      V[(3 * m + j) * SMALL_VS + nn] = q4;
     }
     __syncthreads();
-    for (int nn = 0; nn < len; ++nn) {
+    if (on)
+      for (int nn = 0; nn < len; ++nn) {
 #pragma unroll
-      for (int q = 0; q < SMALL_MAXC; ++q)
-        if (tid + q * SMALL_THREADS < ncombo) acc[q] = cjfma(V[oi[q] + nn], V[oj[q] + nn], acc[q]);
-    }
+        for (int q = 0; q < MAXC; ++q)
+          if (tid + q * nth < ncombo) acc[q] = cjfma(V[oi[q] + nn], V[oj[q] + nn], acc[q]);
+      }
     __syncthreads();
   }
 #pragma unroll
-  for (int q = 0; q < SMALL_MAXC; ++q) {
-    if (tid + q * SMALL_THREADS < ncombo) {
+  for (int q = 0; q < MAXC; ++q) {
+    if (on && tid + q * nth < ncombo) {
       const int t = tq[q], i = iq[q], j = jq[q];
       double2 s = acc[q];
       if (t == 1 || t == 2) s = make_double2(0.5 * s.x, 0.5 * s.y);
@@ -166,10 +178,25 @@ __device__ void small_projectors(int m, int me, int n, int Z, const double2* __r
   __syncthreads();
 }
 
+__device__ void small_projectors_any(int m, int me, int n, int Z, const double2* Q, double2* P, double2* V) {
+  const int ncombo = 2 * me * (me + 1);
+  switch ((ncombo + SMALL_THREADS - 1) / SMALL_THREADS) {
+    case 1: small_projectors<1>(m, me, n, Z, Q, P, V); break;
+    case 2: small_projectors<2>(m, me, n, Z, Q, P, V); break;
+    case 3: small_projectors<3>(m, me, n, Z, Q, P, V); break;
+    case 4: small_projectors<4>(m, me, n, Z, Q, P, V); break;
+    case 5: small_projectors<5>(m, me, n, Z, Q, P, V); break;
+    case 6: small_projectors<6>(m, me, n, Z, Q, P, V); break;
+    case 7: small_projectors<7>(m, me, n, Z, Q, P, V); break;
+    case 8: small_projectors<8>(m, me, n, Z, Q, P, V); break;
+    default: small_projectors<SMALL_MAXC>(m, me, n, Z, Q, P, V); break;
+  }
+}
+
 // Grid: one CTA of SMALL_THREADS per sample (global sample s = blockIdx.x).
 // work + soff[s]: the sample's basis (m x n), work vector (n) and state (n).
 // Dynamic shared memory: A, E (m^2 each), P (4 m^2), c and c' (m each), and
-// max(5 m^2, 4 m SMALL_NC) of expm / projector scratch, all complex.
+// max(5 m^2, 4 m SMALL_VS) of expm / projector scratch, all complex.
 __global__ void __launch_bounds__(SMALL_THREADS, 2)
     k_small_prop(const SmallJob* __restrict__ jobs, const int* __restrict__ sjob, const int* __restrict__ scol,
                  const int64_t* __restrict__ soff, double2* __restrict__ work, Theta th, int m, int T, double dt,
@@ -179,9 +206,9 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
   __shared__ double rowsum[SPC_MAX_M];
   __shared__ int piv[SPC_MAX_M];
   __shared__ int s_sh, p_sh;
-  __shared__ double2 red[SMALL_WARPS];
+  __shared__ double2 red[SMALL_WARPS + 1];
   __shared__ double2 part[SMALL_WARPS][32];
-  __shared__ double terms[SMALL_WARPS];
+  __shared__ double terms[16];
   __shared__ double cstat[2];
 
   const int s = blockIdx.x;
@@ -314,7 +341,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
           }
         }
       }
-      small_projectors(m, me, n, Z, Q, P, X);
+      small_projectors_any(m, me, n, Z, Q, P, X);
       if (!lz) break;
       // a Lanczos basis must be orthonormal: max |sum_t P_t - I| <= ORTHO_TOL
       double mx = 0.0;
@@ -331,8 +358,16 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
       }
       if (lane == 0) terms[warp] = mx;
       __syncthreads();
-      double mall = terms[0];
-      for (int w = 1; w < SMALL_WARPS; ++w) mall = (terms[w] > mall || terms[w] != terms[w]) ? terms[w] : mall;
+      if (warp == 0) {
+        double v = lane < SMALL_WARPS ? terms[lane] : 0.0;
+        for (int d = 16; d > 0; d >>= 1) {
+          const double u = __shfl_xor_sync(0xffffffffu, v, d);
+          v = (u > v || u != u) ? u : v;
+        }
+        if (lane == 0) cstat[0] = v;
+      }
+      __syncthreads();
+      const double mall = cstat[0];
       __syncthreads();
       if (mall <= ORTHO_TOL) break;
       nf++;
@@ -364,50 +399,59 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
         cn[tid] = v;
       }
       __syncthreads();
-      // Re(c'^H P_t c') for the 4 types, two warps each: the Hermitian form as
-      // its diagonal plus twice the real part of the upper triangle, the
-      // (i <= j) pairs dealt round-robin over the type's 64 threads
-      {
-        const int ty = warp >> 1, h2 = ((warp & 1) << 5) | lane;
-        const double2* Pt = P + ty * mm;
-        double acc2 = 0.0;
+      // Re(c'^H P_t c') for the 4 types on warps 0-3 (one per scheduler):
+      // each Hermitian form is its diagonal plus twice the real part of the
+      // upper triangle, and g_ij = conj(c_i) c_j is shared by the types:
+      // Re(conj(c_i) P_ij c_j) = Re(P_ij) Re(g_ij) - Im(P_ij) Im(g_ij).
+      // Warp 4 takes |c'|^2 and |c'_{m-1}|^2.
+      if (warp < 4) {
+        double f0 = 0.0, f1 = 0.0, f2 = 0.0, f3 = 0.0;
         const int npair = me * (me + 1) / 2;
-        int i = 0, rem = h2;
+        int i = 0, rem = tid;
         while (i < me && rem >= me - i) {
           rem -= me - i;
           ++i;
         }
-        for (int pidx = h2; pidx < npair; pidx += 64) {
+        for (int pidx = tid; pidx < npair; pidx += 128) {
           const int j = i + rem;
           const double2 ci = cn[i], cj = cn[j];
-          const double2 pij = Pt[i + j * m];
-          // w = P_ij c_j; term = Re(conj(c_i) w)
-          const double wx = fma(pij.x, cj.x, -pij.y * cj.y), wy = fma(pij.x, cj.y, pij.y * cj.x);
-          const double tr = fma(ci.x, wx, ci.y * wy);
-          acc2 += (i == j) ? tr : 2.0 * tr;
-          rem += 64;
+          const double sc = (i == j) ? 1.0 : 2.0;
+          const double gx = sc * fma(ci.x, cj.x, ci.y * cj.y), gy = sc * fma(ci.x, cj.y, -ci.y * cj.x);
+          const size_t x = (size_t)i + (size_t)j * m;
+          f0 = fma(P[x].x, gx, fma(-P[x].y, gy, f0));
+          f1 = fma(P[mm + x].x, gx, fma(-P[mm + x].y, gy, f1));
+          f2 = fma(P[2 * mm + x].x, gx, fma(-P[2 * mm + x].y, gy, f2));
+          f3 = fma(P[3 * mm + x].x, gx, fma(-P[3 * mm + x].y, gy, f3));
+          rem += 128;
           while (i < me && rem >= me - i) {
             rem -= me - i;
             ++i;
           }
         }
-        acc2 = warp_sum(acc2);
-        if (lane == 0) terms[warp] = acc2;
-        if (warp == 0) {
-          double nn = 0.0;
-          if (lane < me) nn = fma(cn[lane].x, cn[lane].x, cn[lane].y * cn[lane].y);
-          nn = warp_sum(nn);
-          if (lane == 0) {
-            cstat[0] = nn;
-            const double2 cmv = cn[me - 1];
-            cstat[1] = cmv.x * cmv.x + cmv.y * cmv.y;
-          }
+        f0 = warp_sum(f0);
+        f1 = warp_sum(f1);
+        f2 = warp_sum(f2);
+        f3 = warp_sum(f3);
+        if (lane == 0) {
+          terms[4 * warp + 0] = f0;
+          terms[4 * warp + 1] = f1;
+          terms[4 * warp + 2] = f2;
+          terms[4 * warp + 3] = f3;
+        }
+      } else if (warp == 4) {
+        double nn = 0.0;
+        if (lane < me) nn = fma(cn[lane].x, cn[lane].x, cn[lane].y * cn[lane].y);
+        nn = warp_sum(nn);
+        if (lane == 0) {
+          cstat[0] = nn;
+          const double2 cmv = cn[me - 1];
+          cstat[1] = cmv.x * cmv.x + cmv.y * cmv.y;
         }
       }
       __syncthreads();
       if (tid < 4) {
         const int slot = tid == 0 ? 2 : (tid == 1 ? 0 : (tid == 2 ? 1 : 3));  // proj type -> obs slot
-        o[slot * T + k] = terms[2 * tid] + terms[2 * tid + 1];
+        o[slot * T + k] = ((terms[tid] + terms[4 + tid]) + terms[8 + tid]) + terms[12 + tid];
       }
       c2 = cstat[0];
       cm2 = cstat[1];
@@ -440,7 +484,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
 // Dynamic shared memory of k_small_prop for Krylov dimension m (bytes).
 static size_t small_smem_bytes(int m) {
   const size_t mm = (size_t)m * m;
-  return sizeof(double2) * (6 * mm + 2 * (size_t)m + std::max<size_t>(5 * mm, 4 * (size_t)m * SMALL_NC));
+  return sizeof(double2) * (6 * mm + 2 * (size_t)m + std::max<size_t>(5 * mm, 4 * (size_t)m * SMALL_VS));
 }
 
 // Whether a call runs on k_small_prop (sets smem). Rows, m, shared memory
