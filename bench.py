@@ -68,6 +68,8 @@ def parse():
     p.add_argument("--batch-orient", type=int, default=4)
     p.add_argument("--batch-window-ns", type=float, default=20.0)
     p.add_argument("--batch-krylov", type=int, default=20)
+    p.add_argument("--batch-sample-path", default="auto", choices=["auto", "on", "off"],
+                   help="one-CTA-per-sample kernel for the batched call (per-instance calls keep auto)")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient leg")
     p.add_argument("--no-batch-adjoint", action="store_true", help="skip the batched-adjoint leg")
     p.add_argument("--batch-adjoint-window-ns", type=float, default=10.0)
@@ -364,6 +366,13 @@ def batched_leg(args, sampler, local_rank):
                                           1e-5, out_dev.data_ptr() + 8 * k * 4 * T)
 
     def batched():
+        sampler.set_sample_path(args.batch_sample_path)
+        try:
+            batched_calls()
+        finally:
+            sampler.set_sample_path("auto")
+
+    def batched_calls():
         for grp in groups:
             sampler.build_h_batch([systems[i] for i in grp], [fields[i] for i in grp], "general")
             sampler.trace_sampling_batch_device(zk_dev.data_ptr() + 16 * int(offs[grp[0]]), [Ms[i] for i in grp],
@@ -565,10 +574,16 @@ def symmetry_leg(args, sampler):
 
     g, t_g = timed(lambda: S.symmetrised_yield_gradient(sysp, sim, [0, 0, 0.05], sampler=sampler,
                                                         directions=dirs, n_quad=args.adjoint_quad))
+    # the stepwise forward the gradient differentiates, same jobs, yields only
+    y, t_f = timed(lambda: S.symmetrised_yield_gradient(sysp, sim, [0, 0, 0.05], sampler=sampler,
+                                                        directions=dirs, n_quad=args.adjoint_quad,
+                                                        gradient=False))
     _, t_p = timed(lambda: S.symmetrised_dynamics(sysp, sim, sampler=sampler, field=0.05 * dirs[0]))
     work_g = len(bl) * args.sym_samples * len(dirs)
     T_steps = 2 * (num_time_points(sim.dt, sim.t_end) // 2) - 2  # steps of the Simpson grid
     return {"value": work_g * T_steps / t_g, "unit": "sample-steps/s", "seconds": t_g,
+            "stepwise_forward_value": work_g * T_steps / t_f, "cost_vs_stepwise_forward": t_g / t_f,
+            "max_abs_dPhi_S_gradient_vs_forward_sweep": float(max(abs(a["Phi_S"] - b["Phi_S"]) for a, b in zip(g, y))),
             "plain_batched_forward_value": len(bl) * args.sym_samples * int(round(sim.t_end / sim.dt)) / t_p,
             "blocks": len(bl), "block_dims": [min(dims), max(dims)], "sum_block_dims": int(sum(dims)),
             "full_dim": int(4 * sysp.Z), "samples_per_block": args.sym_samples, "directions": len(dirs),

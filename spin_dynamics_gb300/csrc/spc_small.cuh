@@ -500,7 +500,10 @@ static bool small_path_fits(Handle* h, const std::vector<JobSpec>& jobs, int m, 
     G += j.M;
     bytes += 16.0 * (double)(m + 2) * j.n * j.M;
     const double me = std::min(m, j.n), n = j.n;
-    wmax = std::max(wmax, 4.0 * me * (double)j.nnz + 16.0 * me * n + 2.0 * n * me * me + 48.0 * me * me * me);
+    // MGS rounds (rates unequal, or MGS requested) add ~m^2 n/2 complex FMAs
+    const bool mgs = !(h->krylov_method == 1 || h->krylov_method == 2) || !j.herm_shift;
+    wmax = std::max(wmax, 4.0 * me * (double)j.nnz + 16.0 * me * n + 2.0 * n * me * me + 48.0 * me * me * me +
+                              (mgs ? 2.0 * me * me * n : 0.0));
   }
   if (G > INT32_MAX) return false;
   bytes += 32.0 * T * (double)G + 16.0 * (double)G;

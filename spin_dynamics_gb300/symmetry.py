@@ -301,7 +301,7 @@ def symmetrised_dynamics(sys_: SysParam, sim: SimParam, out: Optional[str] = Non
 
 def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, directions=None,
                                n_quad: int = 6, checkpoint_every: int = 0, wS: float = 1.0,
-                               wT: float = 0.0, exact_blocks: bool = False) -> list:
+                               wT: float = 0.0, exact_blocks: bool = False, gradient: bool = True) -> list:
     """Yields of the block decomposition and their gradient with respect to
     the field vector, J, D, kS and kT (the field set of
     spc_yield_gradient_batch), for the field B (mT, 3-vector) or for each of
@@ -310,7 +310,8 @@ def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, d
     memory). Block results enter with their weights. Returns one dict per
     direction: Phi_S, Phi_T, B (3), J, D (3 x 3), kS, kT, and for directions
     the derivatives with respect to the polar and azimuthal angles theta, phi
-    of the field."""
+    of the field. gradient=False runs the forward sweep alone (the stepwise
+    yields; derivatives zero)."""
     from . import dynamics
     from .dynamics import batch_groups, padded_samples
     sp = sampler or dynamics.default_sampler()
@@ -331,7 +332,7 @@ def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, d
         got = sp.yield_gradient_batch(systems, [fields[jobs[q][0]] for q in grp], [zks[jobs[q][1]] for q in grp],
                                       sim.dt, sim.t_end, sim.N_krylov, n_quad=n_quad,
                                       checkpoint_every=checkpoint_every, wS=wS, wT=wT, hyperfine=False,
-                                      init_state=sim.init_state)
+                                      init_state=sim.init_state, gradient=gradient)
         for q, g in zip(grp, got):
             f, j = jobs[q]
             w = sel[j][1]
