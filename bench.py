@@ -632,6 +632,13 @@ def adjoint_leg(args, sampler, plain_value):
         _, t_auto = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=args.adjoint_quad,
                                                          checkpoint_every=0))
         kept_auto = bool(sampler.stats()["rounds"])
+        # fewer Gauss-Legendre nodes per step: cost, and the gradient's
+        # distance from an 8-node reference at the same checkpoints
+        g5, t_auto5 = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=5, checkpoint_every=0))
+        g8 = sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=8, checkpoint_every=0)
+        gscale = float(np.max(np.abs(g8.raw)))
+        rel5 = float(np.max(np.abs(g5.raw - g8.raw))) / gscale
+        rel6 = float(np.max(np.abs(g.raw - g8.raw))) / gscale
         # the stepwise model's accuracy at this m: the same forward at m = 30
         y30 = sampler.stepwise_yields(sysp, B, zk, dt, t_end, 30)
     finally:
@@ -641,6 +648,8 @@ def adjoint_leg(args, sampler, plain_value):
     return {"value": work / t_grad, "unit": "sample-steps/s", "seconds": t_grad,
             "stepwise_forward_value": work / t_fwd, "cost_vs_stepwise_forward": t_grad / t_fwd,
             "cost_vs_stepwise_forward_memory_sized_checkpoints": t_auto / t_fwd,
+            "cost_vs_stepwise_forward_memory_sized_5_nodes": t_auto5 / t_fwd,
+            "grad_max_rel_diff_vs_8_nodes": {"6": rel6, "5": rel5},
             "memory_sized_node_states_kept": kept_auto,
             "cost_vs_plain_forward": t_grad / (work / plain_value),
             "params": int(g.raw.size), "samples": M, "dt_steps": int(steps), "krylov": m,
