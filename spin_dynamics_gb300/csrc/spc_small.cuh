@@ -194,13 +194,16 @@ __device__ void small_projectors_any(int m, int me, int n, int Z, const double2*
 }
 
 // Grid: one CTA of SMALL_THREADS per sample (global sample s = blockIdx.x).
-// work + soff[s]: the sample's basis (m x n), work vector (n) and state (n).
-// Dynamic shared memory: A, E (m^2 each), P (4 m^2), c and c' (m each), and
-// max(5 m^2, 4 m SMALL_VS) of expm / projector scratch, all complex.
+// work + soff[s]: the sample's basis (m x n), work vector (n) and state (n);
+// with vec_smem they live in shared memory instead (every job's (m+2) n
+// complex fits there), which cuts the latency of the row sweeps.
+// Dynamic shared memory: A, E (m^2 each), P (4 m^2), c and c' (m each),
+// max(5 m^2, 4 m SMALL_VS) of expm / projector scratch, all complex, then
+// the vectors when vec_smem.
 __global__ void __launch_bounds__(SMALL_THREADS, 2)
     k_small_prop(const SmallJob* __restrict__ jobs, const int* __restrict__ sjob, const int* __restrict__ scol,
                  const int64_t* __restrict__ soff, double2* __restrict__ work, Theta th, int m, int T, double dt,
-                 double t_end, double tol, int lanczos, double* __restrict__ obs,
+                 double t_end, double tol, int lanczos, int vec_smem, double* __restrict__ obs,
                  long long* __restrict__ nsteps, unsigned long long* __restrict__ counts, int* __restrict__ err) {
   extern __shared__ double2 smem[];
   __shared__ double rowsum[SPC_MAX_M];
@@ -222,7 +225,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
   double2* cA = P + 4 * mm;
   double2* cB = cA + m;
   double2* X = cB + m;
-  double2* Q = work + soff[s];
+  double2* Q = vec_smem ? X + std::max<size_t>(5 * mm, 4 * (size_t)m * SMALL_VS) : work + soff[s];
   double2* p = Q + (size_t)m * n;
   double2* psi = p + n;
   const bool herm = J.kappa != nullptr;
@@ -481,7 +484,8 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
   }
 }
 
-// Dynamic shared memory of k_small_prop for Krylov dimension m (bytes).
+// Dynamic shared memory of k_small_prop for Krylov dimension m (bytes),
+// without the vectors.
 static size_t small_smem_bytes(int m) {
   const size_t mm = (size_t)m * m;
   return sizeof(double2) * (6 * mm + 2 * (size_t)m + std::max<size_t>(5 * mm, 4 * (size_t)m * SMALL_VS));
@@ -580,6 +584,12 @@ static int propagate_small(Handle* h, const double* theta, const double* init_po
   h->count_launch();
   Theta th;
   for (int e = 0; e < 4; ++e) th.v[e] = make_double2(theta[2 * e], theta[2 * e + 1]);
+  // the vectors in shared memory when every job's fit beside the matrices
+  int nmax = 0;
+  for (const JobSpec& j : jobs) nmax = std::max(nmax, j.n);
+  const size_t vbytes = sizeof(double2) * (size_t)(m + 2) * nmax;
+  const bool vec_smem = smem + vbytes + 8192 <= h->smem_optin;
+  if (vec_smem) smem += vbytes;
   CK(cudaFuncSetAttribute(k_small_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int* d_err = (int*)h->err.p;
   long long* d_nsteps = (long long*)((char*)h->err.p + 8);
@@ -587,7 +597,8 @@ static int propagate_small(Handle* h, const double* theta, const double* init_po
   int pe = h->prof.begin(st);
   k_small_prop<<<G, SMALL_THREADS, smem, st>>>((const SmallJob*)plan, (const int*)(plan + o_sjob),
                                                (const int*)(plan + o_scol), (const int64_t*)(plan + o_soff),
-                                               (double2*)h->Q.p, th, m, T, dt, t_end, tol, lanczos ? 1 : 0, d_obs,
+                                               (double2*)h->Q.p, th, m, T, dt, t_end, tol, lanczos ? 1 : 0,
+                                               vec_smem ? 1 : 0, d_obs,
                                                d_nsteps, d_counts, d_err);
   h->prof.end(st, pe, PK_SAMPLE, 0.0, 0.0);
   h->count_launch();
