@@ -169,3 +169,26 @@ def test_auto_mode_picks_by_size(sampler, oracle):
     zk = W.random_phase_samples(big.Z, 2, seed=1)
     sampler.trace_sampling(zk, DT, 3 * DT, 8, 1e-5)
     assert sampler.stats()["kernel_launches"] > 10
+
+
+@pytest.mark.parametrize("m", [1, 2])
+@pytest.mark.parametrize("rates", [(1.0, 1.0), (2.0, 1.0)])
+def test_pair_without_nuclei(sampler, oracle, m, rates):
+    """Dimension 4 (no nuclei, one nuclear row), Krylov dimensions 1 and 2,
+    Lanczos (equal rates) and MGS (unequal): both paths against the oracle."""
+    from spin_dynamics_gb300.spinsys import Electron, SysParam
+
+    s = SysParam.from_input_units(Electron(g_I=[], A=[]), Electron(g_I=[], A=[]), J=0.1,
+                                  kS_per_us=rates[0], kT_per_us=rates[1])
+    rp, col, val = iso_csr(oracle, s, 0.3)
+    zk = np.ones((3, s.Z), complex)
+    ref = oracle.trace_sampling(rp, col, val, zk, DT, 20 * DT, m, 1e-6)
+
+    def run():
+        sampler.set_h(rp, col, val)
+        return sampler.trace_sampling(zk, DT, 20 * DT, m, 1e-6)
+
+    r = _both(sampler, run, "auto")
+    for mode in ("on", "off"):
+        assert _err(r[mode][0], ref) <= ABS_TOL
+        assert r[mode][1]["krylov_builds"] == int(ref["n_builds"].sum())
