@@ -192,3 +192,15 @@ def test_pair_without_nuclei(sampler, oracle, m, rates):
     for mode in ("on", "off"):
         assert _err(r[mode][0], ref) <= ABS_TOL
         assert r[mode][1]["krylov_builds"] == int(ref["n_builds"].sum())
+
+
+def test_mode_switch_errors(sampler):
+    """The C ABI refuses unknown modes; the Python binding refuses unknown names."""
+    from spin_dynamics_gb300 import _native as nat
+    from spin_dynamics_gb300._native import SpcError
+
+    with pytest.raises(SpcError, match="sample-path mode"):
+        nat.check(nat.lib().spc_set_sample_path(sampler.handle, 7))
+    with pytest.raises(KeyError):
+        sampler.set_sample_path("sometimes")
+    sampler.set_sample_path("auto")
