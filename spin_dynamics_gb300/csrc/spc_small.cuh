@@ -7,15 +7,17 @@
 // tile, one launch per phase) kernels of microseconds, so a build round of
 // ~90 launches is bound by launch and synchronisation latency, not by the
 // FP64 pipe. Here a sample's build is ~1e6 DFMA on its own SM with
-// block-level barriers only. Used when every job has at most SMALL_NMAX rows,
-// m <= 32 and the samples fill at most a few waves (propagate_batch).
+// block-level barriers only. Used (SPC_SAMPLE_AUTO) when every job has at
+// most SMALL_NMAX rows, m <= 32, a small estimated build and the samples fill
+// at most two waves of CTAs (small_path_fits).
 //
 // Per sample the arithmetic is the tiled path's: the SpMM row loop of k_spmm,
 // real-coefficient Lanczos on the Hermitian part (orthonormality checked from
 // the projector Grams, MGS rebuild when it fails) or MGS, expm_one, the four
 // Hermitian projector Grams, the reference's dt-loop semantics. Reductions
-// are two-level and in a fixed order (warp tree, then the warps in order), so
-// results repeat bit for bit; they differ from the tiled path's by rounding.
+// are two-level and in a fixed order (a warp tree, then warp 0's tree over the
+// warps' partials), so results repeat bit for bit; they differ from the tiled
+// path's by rounding.
 // Control flow is uniform across the CTA: every barrier is reached by all
 // threads, and a sample leaves the loop only when the whole CTA does.
 #define SMALL_THREADS 256
