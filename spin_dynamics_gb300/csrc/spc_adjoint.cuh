@@ -264,6 +264,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
           x.split = (const int*)HB.split.p + HB.rp_off[sy];
           x.col = (const int*)HB.col.p + HB.nz_off[sy];
           x.val = (const double2*)HB.val.p + HB.nz_off[sy];
+          x.vsum = (const double*)HB.vsum.p + HB.nz_off[sy];
           x.kappa = HB.herm[sy] ? &((const HMeta*)HB.meta.p)[sy].kappa : nullptr;
         }
         for (int l = 0; l < SPC_LANES; ++l) {
@@ -337,11 +338,12 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     const double held = (double)h->gck.bytes + h->gseg.bytes + h->gnu.bytes + h->Q.bytes + h->gmu.bytes +
-                        h->glam.bytes + h->P.bytes;
+                        h->glam.bytes + h->P.bytes + h->xsum.bytes;
     const double avail = 0.85 * ((double)free_b + held) - (double)(1 << 28);
     const double sb = sizeof(double2) * (double)S;
     auto need = [&](int k, bool keep) {
-      return sb * ((double)m + 4.0 + (nsteps / k + 1) + k + 1.0 + (keep ? (double)k * nq : (double)nq));
+      // + 0.5: the Re + Im plane of the current Krylov vector beside P
+      return sb * ((double)m + 4.5 + (nsteps / k + 1) + k + 1.0 + (keep ? (double)k * nq : (double)nq));
     };
     if (K == 0) {
       // among the spacings whose states fit, the one that recomputes the
@@ -378,7 +380,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
   if (h->ensure(h->gck, sizeof(double2) * S * n_ck) || h->ensure(h->gseg, sizeof(double2) * S * n_seg) ||
       h->ensure(h->gnu, sizeof(double2) * S * n_nu) || h->ensure(h->gmu, sizeof(double2) * S) ||
       h->ensure(h->glam, sizeof(double2) * S * 2) || h->ensure(h->Q, sizeof(double2) * m * S) ||
-      h->ensure(h->P, sizeof(double2) * S) ||
+      h->ensure(h->P, sizeof(double2) * S) || h->ensure(h->xsum, sizeof(double) * S) ||
       h->ensure(h->partial, sizeof(double2) * std::max<size_t>((size_t)items_cap * SPC_LANES, part_cap)) ||
       h->ensure(h->counters, sizeof(unsigned) * std::max<size_t>(ntiles, npairs)) ||
       h->ensure(h->coef, sizeof(double2) * nslots) || h->ensure(h->rbeta, sizeof(double) * nslots) ||
@@ -393,6 +395,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
   double2 *ck = (double2*)h->gck.p, *seg = (double2*)h->gseg.p, *gnu = (double2*)h->gnu.p;
   double2 *gmu = (double2*)h->gmu.p, *lam = (double2*)h->glam.p, *ulam = lam + S;
   double2 *d_Q = (double2*)h->Q.p, *d_P = (double2*)h->P.p, *d_part = (double2*)h->partial.p;
+  double* d_xs = (double*)h->xsum.p;
   unsigned* d_cnt = (unsigned*)h->counters.p;
   double2 *d_A = (double2*)h->Ahess.p, *d_E = (double2*)h->Aexp.p, *d_c = (double2*)h->cvec.p;
   double2* d_c2 = (double2*)h->cvec2.p;
@@ -423,9 +426,10 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
   plan_items(tile_n, resident((const void*)k_spmm), fs, csn, items_s);
   const int nip = (int)items_p.size(), nis = (int)items_s.size();
   if (nip > items_cap || nis > items_cap) return set_error(SPC_ERR_ARG, "internal: work plan exceeds its buffer");
-  // SpMM work per sample column: all entries (bytes); FLOPs 8 per complex
-  // entry, 4 per real one (forward and adjoint Hamiltonians of a job share the
-  // pattern), plus 4 per row for the -i*kappa shift outside Lanczos
+  // SpMM work per sample column: all entries (bytes); FP64 operations issued
+  // 6 per complex entry, 4 per real one, 3 per row closing the three-product
+  // sums (forward and adjoint Hamiltonians of a job share the pattern), plus
+  // 4 per row for the -i*kappa shift outside Lanczos
   int64_t nnz_tiles = 0;
   double spmm_flops = 0.0, herm_rows = 0.0;
   for (int t = 0; t < ntiles; ++t) {
@@ -435,7 +439,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
     tf[t].nis = tb[t].nis = csn[t];
     const int sy = jobs[tile_job[t]].sys;
     nnz_tiles += HB.nnz[sy];
-    spmm_flops += 8.0 * (double)HB.nnz_cplx[sy] + 4.0 * (double)(HB.nnz[sy] - HB.nnz_cplx[sy]);
+    spmm_flops += 6.0 * (double)HB.nnz_cplx[sy] + 4.0 * (double)(HB.nnz[sy] - HB.nnz_cplx[sy]) + 3.0 * tile_n[t];
     if (HB.herm[sy]) herm_rows += tile_n[t];
   }
   CK(cudaMemcpyAsync(d_tf, tf.data(), sizeof(TileInfo) * ntiles, cudaMemcpyHostToDevice, st));
@@ -501,12 +505,12 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
     k_rowpass<PASS_NORM_GATHER><<<nip, blk, 0, st>>>(pa);
     h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
     pe = h->prof.begin(st);
-    k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 1, 0, pa.rbeta, d_Q);
+    k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 1, 0, pa.rbeta, d_Q, d_xs);
     h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
     h->count_launch(2);
     for (int i = 0; i < m; ++i) {
       pe = h->prof.begin(st);
-      k_spmm<<<nis, blk, 0, st>>>(tiles, d_items_s, d_map, i, d_Q, d_P, lanczos ? 0 : 1);
+      k_spmm<<<nis, blk, 0, st>>>(tiles, d_items_s, d_map, i, d_Q, d_xs, d_P, lanczos ? 0 : 1);
       h->prof.end(st, pe, PK_SPMM, (spmm_flops + (lanczos ? 0.0 : 4.0 * herm_rows)) * SPC_LANES,
                   20.0 * (double)nnz_tiles + 32.0 * elems);
       h->count_launch();
@@ -547,7 +551,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
           k_rowpass<PASS_AXPY_NORM><<<nip, blk, 0, st>>>(pa);
         h->prof.end(st, pe, PK_AXPY_NORM, (lanczos ? 8.0 : 12.0) * elems, 48.0 * elems);
         pe = h->prof.begin(st);
-        k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 0, i + 1, pa.rbeta, d_Q);
+        k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 0, i + 1, pa.rbeta, d_Q, d_xs);
         h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
         h->count_launch(2);
       }

@@ -281,6 +281,7 @@ static int batch_jobs(spc_handle* h, int n_jobs, const int* job_sys, const int* 
     j.split = (const int*)B.split.p + B.rp_off[s];
     j.col = (const int*)B.col.p + B.nz_off[s];
     j.val = (const double2*)B.val.p + B.nz_off[s];
+    j.vsum = (const double*)B.vsum.p + B.nz_off[s];
     j.zk = zk_dev + zoff;
     j.out = out_dev + (size_t)k * 4 * T;
     j.herm_shift = B.herm[s] != 0;

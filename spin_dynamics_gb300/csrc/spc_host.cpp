@@ -67,7 +67,7 @@ int Handle::ensure_h_entries(size_t count) {
 Handle::~Handle() {
   Buf* all[] = {&psi, &Q,  &P,    &partial, &counters, &coef, &rbeta, &Ahess, &Aexp, &proj, &projpart,
                 &cvec, &tt, &kk, &done, &map, &obs, &out, &zk, &err, &nbuild, &flag, &xcol, &xval, &xsplit, &plan, &jobtab,
-                &hmeta, &hb.rowptr, &hb.split, &hb.col, &hb.val, &hb.meta, &gck, &gseg, &gnu, &gmu, &glam, &cvec2,
+                &hmeta, &xvs, &xsum, &hb.rowptr, &hb.split, &hb.col, &hb.val, &hb.vsum, &hb.meta, &gck, &gseg, &gnu, &gmu, &glam, &cvec2,
                 &gslots, &gracc, &gfacc, &bcnt, &bnuc, &btot, &btab, &tune_out, &tune_zk};
   for (Buf* b : all)
     if (b->p) cudaFree(b->p);
@@ -104,8 +104,8 @@ static cd pair_el(int k, int r, int e, int ep) {
   return s1 == t1 ? spin_half_el(r, s2, t2) : cd{0.0, 0.0};
 }
 
-// <a|I_c|b> for multiplicity g, states m = I, I-1, ...; the device builder's
-// formula with the same rounding points
+// <a|I_c|b> for multiplicity g, states m = I, I-1, ...; ladder elements
+// sqrt(I(I+1) - m_a m_b) as get_spinop_sp forms them (src/spinop.f90:88-92)
 static cd nuc_el(int g, int c, int a, int b) {
   const double I = (g - 1) / 2.0;
   const double ma = I - a, mb = I - b;
@@ -116,8 +116,10 @@ static cd nuc_el(int g, int c, int a, int b) {
   return a == b - 1 ? cd{0.0, -0.5 * l} : cd{0.0, 0.5 * l};
 }
 
-// Entry tables of the general builder (see HostSystem::gen_tab): the values
-// k_gen_fill would compute per row, in the same operation order.
+// Entry tables of the general builder (see HostSystem::gen_tab): per
+// nucleus, the matrix elements of its hyperfine and Zeeman terms between
+// (e, m_j) and (ep, m_j + d - 1), in the operation order of
+// getH_dense's S.A.I sum (src/hamiltonian.f90:279-311).
 static void general_tables(HostSystem& hs) {
   hs.gen_tab.clear();
   for (NucInfo& q : hs.nuc) {

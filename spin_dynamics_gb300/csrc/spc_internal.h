@@ -121,6 +121,9 @@ struct Handle {
   };
   Buf psi, Q, P, partial, counters, coef, rbeta, Ahess, Aexp, proj, projpart, cvec, tt, kk, done,
       map, obs, out, zk, err, nbuild, flag, xcol, xval, xsplit, plan, jobtab, hmeta;
+  // execution copy: Re + Im of every entry (xvs, nnz doubles); Re + Im of
+  // the current Krylov vector of every tile (xsum, beside P)
+  Buf xvs, xsum;
   // Hamiltonian build scratch: row counts, nucleus tables, nonzero totals
   Buf bcnt, bnuc, btot, btab;
   // autotuner outputs and sample subsets
@@ -134,7 +137,7 @@ struct Handle {
     std::vector<int64_t> nnz, rp_off, nz_off;
     std::vector<char> herm;
     std::vector<int64_t> nnz_cplx;
-    Buf rowptr, split, col, val, meta;  // meta: one HMeta per system
+    Buf rowptr, split, col, val, vsum, meta;  // meta: one HMeta per system; vsum: Re + Im per entry
   } hb;
   // Krylov method: 0 full MGS (the reference's get_krylov), 1 Lanczos, 2 auto
   int krylov_method = 0;
@@ -174,6 +177,7 @@ struct JobSpec {
   const int* split = nullptr;
   const int* col = nullptr;
   const double2* val = nullptr;
+  const double* vsum = nullptr;  // Re + Im of every entry of the execution copy
   const double2* zk = nullptr;  // device, M x n/4 complex, sample-major
   double* out = nullptr;        // device, 4*T
   bool herm_shift = false;
@@ -213,9 +217,10 @@ int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode)
 // Row split of a CSR for k_spmm (complex entries first), enqueued on st.
 // herm: H = A - i*kappa*1 with A Hermitian; the copy then holds A (diagonal
 // entries real) and meta->kappa the shift. meta->ncplx (zeroed by the caller)
-// receives the copy's count of entries with a nonzero imaginary part.
+// receives the copy's count of entries with a nonzero imaginary part. xvs[k]
+// = Re + Im of the copy's entry k (the third product of k_spmm's 3M form).
 void enqueue_split_rows(int64_t N, const int* rowptr, const int* col, const double2* val, int* xcol,
-                        double2* xval, int* split, bool herm, HMeta* meta, cudaStream_t st);
+                        double2* xval, double* xvs, int* split, bool herm, HMeta* meta, cudaStream_t st);
 int propagate(Handle* h, const double* theta, const double* init_pop, const double* zk_dev,
               int M, double dt, double t_end, int m, double tol, double* out_dev, int T);
 int propagate_batch(Handle* h, const double* theta, const double* init_pop,

@@ -57,6 +57,7 @@ struct TileInfo {
   const int* split;
   const int* col;
   const double2* val;
+  const double* vsum;  // Re + Im of every entry of the execution copy
   // non-null: the execution copy holds the Hermitian part A of
   // H_eff = A - i*kappa*1 (real diagonal) and *kappa the shift
   const double* kappa;
@@ -219,13 +220,14 @@ __global__ void __launch_bounds__(256) k_rowpass(PassArgs a) {
   }
 }
 
-// Q_{jd} = P / ||P||  (or Q_0 = psi[:, scol] / ||psi|| when gather != 0);
-// grid = pass items.
+// Q_{jd} = P / ||P||  (or Q_0 = psi[:, scol] / ||psi|| when gather != 0),
+// and beside it XS = Re + Im of the stored Q_{jd} (the operand k_spmm's
+// three-product form reads); grid = pass items. XS has P's layout (p_off).
 __global__ void __launch_bounds__(256)
     k_scale(const TileInfo* __restrict__ tiles, const int2* __restrict__ items,
             const int* __restrict__ map, const int* __restrict__ scol,
             const double2* __restrict__ psi, const double2* __restrict__ P, int gather, int jd,
-            const double* __restrict__ rbeta, double2* __restrict__ Q) {
+            const double* __restrict__ rbeta, double2* __restrict__ Q, double* __restrict__ XS) {
   const int2 it = items[blockIdx.x];
   const TileInfo& T = tiles[it.x];
   if (!gather && jd >= T.m) return;
@@ -236,32 +238,42 @@ __global__ void __launch_bounds__(256)
   const int n = T.n;
   const int stride = T.nip * SPC_WARPS;
   double2* dst = Q + T.q_off + (size_t)jd * n * SPC_LANES + tx;
+  double* xs = XS + T.p_off + tx;
   if (gather) {
     const double2* src = psi + T.psi_off + scol[w];
     for (int r = it.y * SPC_WARPS + threadIdx.y; r < n; r += stride) {
       const double2 x = src[(size_t)r * T.ldp];
-      dst[(size_t)r * SPC_LANES] = make_double2(x.x * rb, x.y * rb);
+      const double2 q = make_double2(x.x * rb, x.y * rb);
+      dst[(size_t)r * SPC_LANES] = q;
+      xs[(size_t)r * SPC_LANES] = q.x + q.y;
     }
   } else {
     const double2* src = P + T.p_off + tx;
     for (int r = it.y * SPC_WARPS + threadIdx.y; r < n; r += stride) {
       const double2 x = src[(size_t)r * SPC_LANES];
-      dst[(size_t)r * SPC_LANES] = make_double2(x.x * rb, x.y * rb);
+      const double2 q = make_double2(x.x * rb, x.y * rb);
+      dst[(size_t)r * SPC_LANES] = q;
+      xs[(size_t)r * SPC_LANES] = q.x + q.y;
     }
   }
 }
 
 // P_t = H Q_t[i] for the tile of a SpMM item; one warp per row at a time, the
-// row's (col, val) entries broadcast to all lanes. Rows are stored in the
-// execution order of k_split_rows: entries with a nonzero imaginary part
-// first (4 DFMA each), then real ones from split[r] on (2 DFMA each). A tile
-// whose copy holds the Hermitian part A of A - i*kappa*1 gets A x, plus
-// -i*kappa x when `shift` is set (full H_eff for MGS rounds; Lanczos rounds
-// run on A).
+// row's (col, val) entries broadcast to all lanes, one sample per lane.
+// Complex products in the three-multiplication form (Gauss; Higham, SIAM J.
+// Matrix Anal. Appl. 13 (1992) 681-687): with v = a + ib, x = c + id,
+//   t1 += a c,  t2 += b d,  t3 += (a + b)(c + d);  y = (t1 - t2, t3 - t1 - t2)
+// where a + b is stored with the execution copy (vsum) and c + d beside the
+// basis vector (XS, written by k_scale): 3 DFMA per entry instead of 4 on
+// GB300's narrow FP64 pipe. Rows are in the execution order of k_split_rows:
+// entries with a nonzero imaginary part first, then real ones from split[r]
+// on (b = 0: t1 and t3 only, 2 DFMA). A tile whose copy holds the Hermitian
+// part A of A - i*kappa*1 gets A x, plus -i*kappa x when `shift` is set (full
+// H_eff for MGS rounds; Lanczos rounds run on A).
 __global__ void __launch_bounds__(256)
     k_spmm(const TileInfo* __restrict__ tiles, const int2* __restrict__ items,
            const int* __restrict__ map, int i, const double2* __restrict__ Q,
-           double2* __restrict__ Pout, int shift) {
+           const double* __restrict__ XS, double2* __restrict__ Pout, int shift) {
   const int2 it = items[blockIdx.x];
   const TileInfo& T = tiles[it.x];
   if (i >= T.m) return;
@@ -274,52 +286,41 @@ __global__ void __launch_bounds__(256)
   const int* __restrict__ split = T.split;
   const int* __restrict__ col = T.col;
   const double2* __restrict__ val = T.val;
+  const double* __restrict__ vsum = T.vsum;
   const double2* X = Q + T.q_off + (size_t)i * n * SPC_LANES + tx;
+  const double* Xs = XS + T.p_off + tx;
   double2* Y = Pout + T.p_off + tx;
   const int stride = T.nis * SPC_WARPS;
   for (int r = it.y * SPC_WARPS + threadIdx.y; r < n; r += stride) {
     const int k0 = __ldg(rowptr + r), ks = __ldg(split + r), k1 = __ldg(rowptr + r + 1);
-    double2 a0 = cz(), a1 = cz();
+    double t1 = 0.0, t2 = 0.0, t3 = 0.0;
     int k = k0;
-    for (; k + 1 < ks; k += 2) {
-      const int c0 = __ldg(col + k), c1 = __ldg(col + k + 1);
-      const double2 v0 = __ldg(val + k), v1 = __ldg(val + k + 1);
+#pragma unroll 4
+    for (; k < ks; ++k) {
+      const int c = __ldg(col + k);
+      const double2 v = __ldg(val + k);
+      const double vs = __ldg(vsum + k);
       if (act) {
-        const double2 x0 = X[(size_t)c0 * SPC_LANES];
-        const double2 x1 = X[(size_t)c1 * SPC_LANES];
-        a0 = cfma(v0, x0, a0);
-        a1 = cfma(v1, x1, a1);
+        const double2 x = X[(size_t)c * SPC_LANES];
+        const double xs = Xs[(size_t)c * SPC_LANES];
+        t1 = fma(v.x, x.x, t1);
+        t2 = fma(v.y, x.y, t2);
+        t3 = fma(vs, xs, t3);
       }
     }
-    if (k < ks) {
-      const int c0 = __ldg(col + k);
-      const double2 v0 = __ldg(val + k);
-      if (act) a0 = cfma(v0, X[(size_t)c0 * SPC_LANES], a0);
-      k++;
-    }
-    for (; k + 1 < k1; k += 2) {
-      const int c0 = __ldg(col + k), c1 = __ldg(col + k + 1);
-      const double v0 = __ldg(&val[k].x), v1 = __ldg(&val[k + 1].x);
+#pragma unroll 4
+    for (; k < k1; ++k) {
+      const int c = __ldg(col + k);
+      const double v = __ldg(&val[k].x);
       if (act) {
-        const double2 x0 = X[(size_t)c0 * SPC_LANES];
-        const double2 x1 = X[(size_t)c1 * SPC_LANES];
-        a0.x = fma(v0, x0.x, a0.x);
-        a0.y = fma(v0, x0.y, a0.y);
-        a1.x = fma(v1, x1.x, a1.x);
-        a1.y = fma(v1, x1.y, a1.y);
-      }
-    }
-    if (k < k1) {
-      const int c0 = __ldg(col + k);
-      const double v0 = __ldg(&val[k].x);
-      if (act) {
-        const double2 x0 = X[(size_t)c0 * SPC_LANES];
-        a0.x = fma(v0, x0.x, a0.x);
-        a0.y = fma(v0, x0.y, a0.y);
+        const double xr = X[(size_t)c * SPC_LANES].x;
+        const double xs = Xs[(size_t)c * SPC_LANES];
+        t1 = fma(v, xr, t1);
+        t3 = fma(v, xs, t3);
       }
     }
     if (act) {
-      double2 y = cadd(a0, a1);
+      double2 y = make_double2(t1 - t2, t3 - t1 - t2);
       if (sh) {  // -i*kappa*x_r
         const double2 xr = X[(size_t)r * SPC_LANES];
         y.x = fma(kp, xr.y, y.x);
@@ -332,14 +333,14 @@ __global__ void __launch_bounds__(256)
 
 // Execution copy of a CSR for k_spmm: each row's entries reordered so that
 // those with a nonzero imaginary part come first (original order kept within
-// each class); split[r] is the index of the row's first real entry. herm
-// (H = A - i*kappa*1, A Hermitian): diagonal entries are stored with their
-// imaginary part removed (real class) and row 0's removed sum is kappa.
-// meta->ncplx counts the copy's complex entries.
+// each class); split[r] is the index of the row's first real entry, and
+// xvs[k] = Re + Im of entry k. herm (H = A - i*kappa*1, A Hermitian): diagonal
+// entries are stored with their imaginary part removed (real class) and row
+// 0's removed sum is kappa. meta->ncplx counts the copy's complex entries.
 __global__ void k_split_rows(int64_t N, const int* __restrict__ rowptr, const int* __restrict__ col,
                              const double2* __restrict__ val, int* __restrict__ xcol,
-                             double2* __restrict__ xval, int* __restrict__ split, int herm,
-                             HMeta* __restrict__ meta) {
+                             double2* __restrict__ xval, double* __restrict__ xvs, int* __restrict__ split,
+                             int herm, HMeta* __restrict__ meta) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long nc = 0;
   if (r < N) {
@@ -350,6 +351,7 @@ __global__ void k_split_rows(int64_t N, const int* __restrict__ rowptr, const in
       if (cplx(k)) {
         xcol[o] = col[k];
         xval[o] = val[k];
+        xvs[o] = val[k].x + val[k].y;
         o++;
       }
     split[r] = o;
@@ -359,6 +361,7 @@ __global__ void k_split_rows(int64_t N, const int* __restrict__ rowptr, const in
       if (!cplx(k)) {
         xcol[o] = col[k];
         xval[o] = herm ? make_double2(val[k].x, 0.0) : val[k];
+        xvs[o] = val[k].x;
         if (herm && col[k] == r) shift += val[k].y;
         o++;
       }
@@ -369,23 +372,24 @@ __global__ void k_split_rows(int64_t N, const int* __restrict__ rowptr, const in
 }
 
 void enqueue_split_rows(int64_t N, const int* rowptr, const int* col, const double2* val, int* xcol,
-                        double2* xval, int* split, bool herm, HMeta* meta, cudaStream_t st) {
+                        double2* xval, double* xvs, int* split, bool herm, HMeta* meta, cudaStream_t st) {
   if (N > 0)
-    k_split_rows<<<(int)((N + 255) / 256), 256, 0, st>>>(N, rowptr, col, val, xcol, xval, split,
+    k_split_rows<<<(int)((N + 255) / 256), 256, 0, st>>>(N, rowptr, col, val, xcol, xval, xvs, split,
                                                           herm ? 1 : 0, meta);
 }
 
 int prepare_spmm_rows(Handle* h) {
   const int64_t N = h->n, nnz = h->nnz;
   if (h->ensure(h->xcol, sizeof(int) * (nnz > 0 ? nnz : 1)) ||
-      h->ensure(h->xval, sizeof(double2) * (nnz > 0 ? nnz : 1)) || h->ensure(h->xsplit, sizeof(int) * N) ||
+      h->ensure(h->xval, sizeof(double2) * (nnz > 0 ? nnz : 1)) ||
+      h->ensure(h->xvs, sizeof(double) * (nnz > 0 ? nnz : 1)) || h->ensure(h->xsplit, sizeof(int) * N) ||
       h->ensure(h->hmeta, sizeof(HMeta)))
     return SPC_ERR_ALLOC;
   HMeta meta{};
   if (cudaMemsetAsync(h->hmeta.p, 0, sizeof(HMeta), h->stream) != cudaSuccess)
     return set_error(SPC_ERR_CUDA, "row split of the Hamiltonian failed");
   enqueue_split_rows(N, h->d_rowptr, h->d_col, h->d_val, (int*)h->xcol.p, (double2*)h->xval.p,
-                     (int*)h->xsplit.p, h->herm_shift, (HMeta*)h->hmeta.p, h->stream);
+                     (double*)h->xvs.p, (int*)h->xsplit.p, h->herm_shift, (HMeta*)h->hmeta.p, h->stream);
   h->count_launch();
   cudaError_t e = cudaMemcpyAsync(&meta, h->hmeta.p, sizeof(HMeta), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -652,17 +656,32 @@ static cudaError_t set_expm_smem(int m) {
 // still issue their (predicated-off) DFMAs and hold the FP64 pipe. A
 // sample with Z nuclear rows uses min(nsplit, ceil(Z/rps)) splits of about
 // rps rows (proj_splits), so CTAs of an uneven batch carry similar work.
-#define PROJ_NC 32
+//
+// Each conj(a) b is formed with three products (Gauss; Higham 1992):
+//   t1 += ar br,  t2 += ai bi,  t3 += (ar - ai)(br + bi)
+//   Re = t1 + t2,  Im = t3 - t1 + t2
+// with ar - ai and br + bi staged once per element beside the chunk, so a
+// pair costs 3 DFMA instead of 4. Chunks of PROJ_NC rows; the staged rows
+// are padded to PROJ_LD elements so that the eight lanes of a 16-byte
+// shared load that read consecutive basis vectors hit distinct banks.
+#define PROJ_NC 16
+#define PROJ_LD (PROJ_NC + 1)
 __host__ __device__ __forceinline__ int proj_splits(int nsplit, int64_t rps, int64_t Z) {
   const int64_t c = (Z + rps - 1) / rps;
   return (int)(c < 1 ? 1 : (c > nsplit ? nsplit : c));
+}
+// dynamic shared memory of k_proj at Krylov dimension m
+__host__ __device__ __forceinline__ size_t proj_smem_bytes(int m) {
+  return (sizeof(double2) + 2 * sizeof(double)) * 4 * (size_t)m * PROJ_LD;
 }
 template <int MAXC>
 __global__ void __launch_bounds__(256)
     k_proj(const TileInfo* __restrict__ tiles, const int* __restrict__ map, int m, int ncombo,
            const unsigned* __restrict__ combos, const double2* __restrict__ Q, int nsplit, int64_t rps,
            double2* __restrict__ part) {
-  extern __shared__ double2 V[];  // [4][m][PROJ_NC]
+  extern __shared__ double2 V[];  // [4][m][PROJ_LD] complex, then Re - Im and Re + Im of each
+  double* Vd = (double*)(V + 4 * m * PROJ_LD);
+  double* Vs = Vd + 4 * m * PROJ_LD;
   const int w = blockIdx.x;
   if (map[w] < 0) return;
   const TileInfo& Ti = tiles[w / SPC_LANES];
@@ -676,17 +695,17 @@ __global__ void __launch_bounds__(256)
   const int64_t per = (Z + nsp - 1) / nsp;
   const int64_t n0 = (int64_t)split * per;
   const int64_t n1 = min(Z, n0 + per);
-  double2 acc[MAXC];
+  double t1[MAXC], t2[MAXC], t3[MAXC];
   int oi[MAXC], oj[MAXC];
 #pragma unroll
   for (int q = 0; q < MAXC; ++q) {
-    acc[q] = cz();
+    t1[q] = t2[q] = t3[q] = 0.0;
     const int cid = tid + q * nth;
     if (cid < ncombo) {
       const unsigned cb = combos[cid];
       const int t = cb >> 16, i = (cb >> 8) & 255, j = cb & 255;
-      oi[q] = (t * m + i) * PROJ_NC;
-      oj[q] = (t * m + j) * PROJ_NC;
+      oi[q] = (t * m + i) * PROJ_LD;
+      oj[q] = (t * m + j) * PROJ_LD;
     } else {
       oi[q] = oj[q] = 0;
     }
@@ -706,17 +725,26 @@ __global__ void __launch_bounds__(256)
         q3 = base[(size_t)(2 * Z + n) * SPC_LANES];
         q4 = base[(size_t)(3 * Z + n) * SPC_LANES];
       }
-      V[(0 * m + j) * PROJ_NC + nn] = q1;
-      V[(1 * m + j) * PROJ_NC + nn] = csub(q2, q3);
-      V[(2 * m + j) * PROJ_NC + nn] = cadd(q2, q3);
-      V[(3 * m + j) * PROJ_NC + nn] = q4;
+      const double2 v[4] = {q1, csub(q2, q3), cadd(q2, q3), q4};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int o = (t * m + j) * PROJ_LD + nn;
+        V[o] = v[t];
+        Vd[o] = v[t].x - v[t].y;
+        Vs[o] = v[t].x + v[t].y;
+      }
     }
     __syncthreads();
 #pragma unroll 4
     for (int nn = 0; nn < len; ++nn) {
 #pragma unroll
       for (int q = 0; q < MAXC; ++q)
-        if (tid + q * nth < ncombo) acc[q] = cjfma(V[oi[q] + nn], V[oj[q] + nn], acc[q]);
+        if (tid + q * nth < ncombo) {
+          const double2 a = V[oi[q] + nn], b = V[oj[q] + nn];
+          t1[q] = fma(a.x, b.x, t1[q]);
+          t2[q] = fma(a.y, b.y, t2[q]);
+          t3[q] = fma(Vd[oi[q] + nn], Vs[oj[q] + nn], t3[q]);
+        }
     }
     __syncthreads();
   }
@@ -724,7 +752,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int q = 0; q < MAXC; ++q) {
     const int cid = tid + q * nth;
-    if (cid < ncombo) out[cid] = acc[q];
+    if (cid < ncombo) out[cid] = make_double2(t1[q] + t2[q], t3[q] - t1[q] + t2[q]);
   }
 }
 
@@ -741,6 +769,7 @@ __global__ void k_proj_reduce(const TileInfo* __restrict__ tiles, int nslots, co
   const unsigned cb = combos[cid];
   const int t = cb >> 16, i = (cb >> 8) & 255, j = cb & 255;
   if (t == 1 || t == 2) s = make_double2(0.5 * s.x, 0.5 * s.y);
+  if (i == j) s.y = 0.0;  // a Gram's diagonal is real; the three-product form leaves rounding there
   double2* P = proj + ((size_t)w * 4 + t) * m * m;
   P[i + j * m] = s;
   if (i != j) P[j + i * m] = make_double2(s.x, -s.y);
@@ -1196,7 +1225,8 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   // tiles, the capacities scaled down by one factor. States, populations and
   // clocks stay resident for every sample either way.
   const double slot_fixed = 16.0 * (6.0 * mm + m + 1 + (double)nsplit_max * ncombo) + 8.0 + 4.0 + 8.0;
-  const double need_fl = 16.0 * (double)(qcap + pcap) + slot_fixed * slots_cap +
+  // basis + work vector (complex) + the current vector's Re + Im plane (XS)
+  const double need_fl = 16.0 * (double)qcap + 24.0 * (double)pcap + slot_fixed * slots_cap +
                          (double)(sizeof(TileInfo) + sizeof(unsigned)) * tiles_cap;
   const double need_global = 16.0 * (double)psi_total + 8.0 * 4.0 * (double)T * G + 16.0 * G;
   double budget;
@@ -1204,7 +1234,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     double held = 0.0;
-    for (const Handle::Buf* b : {&h->Q, &h->P, &h->coef, &h->rbeta, &h->Ahess, &h->Aexp, &h->proj,
+    for (const Handle::Buf* b : {&h->Q, &h->P, &h->xsum, &h->coef, &h->rbeta, &h->Ahess, &h->Aexp, &h->proj,
                                  &h->projpart, &h->cvec, &h->flag, &h->plan, &h->counters, &h->psi,
                                  &h->obs, &h->tt, &h->kk, &h->done})
       held += (double)b->bytes;
@@ -1220,7 +1250,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
     pfl = std::max<int64_t>((int64_t)(f * (double)pcap), (int64_t)nmax * SPC_LANES);
     tiles_fl = std::max(1, (int)(f * tiles_cap));
     slots_fl = tiles_fl * SPC_LANES;
-    const double fl = 16.0 * (double)(qfl + pfl) + slot_fixed * slots_fl +
+    const double fl = 16.0 * (double)qfl + 24.0 * (double)pfl + slot_fixed * slots_fl +
                       (double)(sizeof(TileInfo) + sizeof(unsigned)) * tiles_fl;
     if (fl > budget)
       return set_error(SPC_ERR_ALLOC,
@@ -1231,7 +1261,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   // upper bound on work items per round: one wave of the most resident kernel plus one per tile
   const int items_cap = h->sm_count * 32 + tiles_fl;
   if (h->ensure(h->psi, sizeof(double2) * psi_total) || h->ensure(h->Q, sizeof(double2) * qfl) ||
-      h->ensure(h->P, sizeof(double2) * pfl) ||
+      h->ensure(h->P, sizeof(double2) * pfl) || h->ensure(h->xsum, sizeof(double) * pfl) ||
       h->ensure(h->partial, sizeof(double2) * (size_t)items_cap * SPC_LANES) ||
       h->ensure(h->counters, sizeof(unsigned) * tiles_fl) ||
       h->ensure(h->coef, sizeof(double2) * slots_fl) || h->ensure(h->rbeta, sizeof(double) * slots_fl) ||
@@ -1251,6 +1281,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   double2* d_psi = (double2*)h->psi.p;
   double2* d_Q = (double2*)h->Q.p;
   double2* d_P = (double2*)h->P.p;
+  double* d_xs = (double*)h->xsum.p;
   double2* d_part = (double2*)h->partial.p;
   unsigned* d_cnt = (unsigned*)h->counters.p;
   double2* d_coef = (double2*)h->coef.p;
@@ -1315,7 +1346,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   h->count_launch();
   CK(cudaGetLastError());
 
-  const size_t proj_smem = sizeof(double2) * 4 * m * PROJ_NC;
+  const size_t proj_smem = proj_smem_bytes(m);
   CK(set_expm_smem(m));
   // combinations per thread (an instantiated count) and threads per CTA (a
   // multiple of 32, at most 256): the pair with the fewest padded slots, the
@@ -1412,6 +1443,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
         ti.split = jobs[k].split;
         ti.col = jobs[k].col;
         ti.val = jobs[k].val;
+        ti.vsum = jobs[k].vsum;
         ti.kappa = jobs[k].herm_shift ? jobs[k].kappa : nullptr;
         ti.m = std::min(m, ti.n);
         qo += (int64_t)m * ti.n * SPC_LANES;
@@ -1511,26 +1543,28 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
       pa.partial = d_part;
       pa.counters = d_cnt;
       pa.lanczos = lanczos ? 1 : 0;
-      // SpMM work of the round: all entries (bytes) and FLOPs (8 per complex
-      // entry, 4 per real one, 4 per row for the -i*kappa shift of MGS rounds)
+      // SpMM work of the round: all entries (bytes) and the FP64 operations
+      // issued (3 DFMA per complex entry, 2 per real one, 3 DADD per row to
+      // close the three-product sums, 2 DFMA per row for the -i*kappa shift
+      // of MGS rounds; a DFMA counts 2)
       int64_t nnz_work = 0;
       double spmm_flops = 0.0;
       for (const TileInfo& ti : tiles) {
         const JobSpec& J = jobs[ti.job];
         nnz_work += J.nnz;
-        spmm_flops += 8.0 * (double)J.nnz_cplx + 4.0 * (double)(J.nnz - J.nnz_cplx) +
+        spmm_flops += 6.0 * (double)J.nnz_cplx + 4.0 * (double)(J.nnz - J.nnz_cplx) + 3.0 * ti.n +
                       (!lanczos && ti.kappa ? 4.0 * ti.n : 0.0);
       }
       int pe = h->prof.begin(st);
       k_rowpass<PASS_NORM_GATHER><<<nip, blk, 0, st>>>(pa);
       h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
       pe = h->prof.begin(st);
-      k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 1, 0, d_rb, d_Q);
+      k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 1, 0, d_rb, d_Q, d_xs);
       h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
       h->count_launch(2);
       for (int i = 0; i < m; ++i) {
         pe = h->prof.begin(st);
-        k_spmm<<<nis, blk, 0, st>>>(d_tiles, d_items_s, d_map, i, d_Q, d_P, lanczos ? 0 : 1);
+        k_spmm<<<nis, blk, 0, st>>>(d_tiles, d_items_s, d_map, i, d_Q, d_xs, d_P, lanczos ? 0 : 1);
         // algorithmic traffic: H once per tile, X once, Y once
         h->prof.end(st, pe, PK_SPMM, spmm_flops * SPC_LANES, 20.0 * (double)nnz_work + 32.0 * elems);
         h->count_launch();
@@ -1575,7 +1609,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
           h->prof.end(st, pe, PK_AXPY_NORM, (lanczos ? 8.0 : 12.0) * elems, 48.0 * elems);
           pe = h->prof.begin(st);
           k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 0, i + 1, d_rb,
-                                       d_Q);
+                                       d_Q, d_xs);
           h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
           h->count_launch(2);
         }
@@ -1594,7 +1628,9 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
                         (void*)&d_Q, (void*)&ns, (void*)&rps, (void*)&d_ppart};
         CK(cudaLaunchKernel(proj_fn, pgrid, dim3(proj_threads), args, proj_smem, st));
       }
-      h->prof.end(st, pe, PK_PROJ, 8.0 * (double)ncombo * zsum + 4.0 * (double)m * zsum,
+      // 3 DFMA per (pair, row), 12 DADD per (vector, row) to stage the four
+      // vector types with their Re - Im and Re + Im
+      h->prof.end(st, pe, PK_PROJ, 6.0 * (double)ncombo * zsum + 12.0 * (double)m * zsum,
                   64.0 * (double)m * zsum);
       {
         const int64_t tot = (int64_t)nslots * ncombo;
@@ -1757,6 +1793,7 @@ int propagate(Handle* h, const double* theta, const double* init_pop, const doub
   j.split = (const int*)h->xsplit.p;
   j.col = (const int*)h->xcol.p;
   j.val = (const double2*)h->xval.p;
+  j.vsum = (const double*)h->xvs.p;
   j.kappa = h->herm_shift ? &((const HMeta*)h->hmeta.p)->kappa : nullptr;
   j.nnz_cplx = h->nnz_cplx;
   j.zk = (const double2*)zk_dev;
