@@ -124,20 +124,23 @@ int spc_build_h(spc_handle* h, const spc_system* sys, int mode);
 int spc_set_h(spc_handle* h, const spc_csr* H);
 
 /* Allocation-free Hamiltonian build (no counterpart in the reference). For
- * callers that cannot allocate device memory: code under CUDA stream capture,
- * hosts with a fixed device-memory budget, or plugins that only pass buffers
- * they own. It builds the same CSR as spc_build_h (same modes, bit-identical
- * output) into caller-owned DEVICE buffers rowptr_dev (n+1), col_dev and
- * val_dev (cap_nnz entries) on `stream` (a cudaStream_t, NULL = default
- * stream) of the current device, without a handle, and calls no cudaMalloc
- * or cudaFree. Its scratch (per-row counts, nucleus table) is a file-scope
- * device array of about 4.2 MB that every GPU loading the library holds
- * until exit; systems above 2^20 rows or 64 nuclei are rejected with
- * SPC_ERR_ARG. The first call on a device looks up that array's address,
- * so make it before any stream capture. All calls share the array: calls
- * that overlap on the GPU race and must be serialised by the caller. On
- * return *n_out and *nnz_out hold the size (also when cap_nnz was too
- * small, which returns SPC_ERR_ARG before the fill). */
+ * callers that cannot allocate device memory: hosts that run inside a
+ * device-memory pool with a budget fixed up front, or plugins and Fortran
+ * programs that only pass buffers they own. It builds the same CSR as
+ * spc_build_h (same modes, bit-identical output) into caller-owned DEVICE
+ * buffers rowptr_dev (n+1), col_dev and val_dev (cap_nnz entries) on `stream`
+ * (a cudaStream_t, NULL = default stream) of the current device, without a
+ * handle, and calls no cudaMalloc, cudaFree or allocating library routine.
+ * Its scratch (per-row counts, nucleus table, entry tables) is a file-scope
+ * device array of about 5.3 MB that every GPU loading the library holds until
+ * exit; systems above 2^20 rows, 64 nuclei or 65536 entry-table elements are
+ * rejected with SPC_ERR_ARG. The first call under a device's context looks up
+ * that array's device address (again after cudaDeviceReset). The size comes
+ * from the closed-form nonzero count: *n_out and *nnz_out are set, and a
+ * cap_nnz that is too small returns SPC_ERR_ARG before anything is launched
+ * or written. The call waits for `stream` twice (after the count and after
+ * the fill). All calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
 int spc_build_h_noalloc(const spc_system* sys, int mode, int32_t* rowptr_dev, int32_t* col_dev,
                         double* val_dev, int64_t cap_nnz, int32_t* n_out, int64_t* nnz_out,
                         void* stream);

@@ -131,30 +131,6 @@ __global__ void k_ref_fill(int64_t N, int64_t Z, int nn, const NucInfo* __restri
 
 // ---------------------------------------------------------------------------
 // general builder (mirrors the ascending-column generator of the oracle)
-__device__ __forceinline__ double2 spin_half_el(int r, int a, int b) {
-  if (r == 2) return a == b ? make_double2(a == 0 ? 0.5 : -0.5, 0.0) : cz();
-  if (a == b) return cz();
-  if (r == 0) return make_double2(0.5, 0.0);
-  return a == 0 ? make_double2(0.0, -0.5) : make_double2(0.0, 0.5);
-}
-__device__ __forceinline__ double2 pair_el(int k, int r, int e, int ep) {
-  int s1 = e >> 1, s2 = e & 1, t1 = ep >> 1, t2 = ep & 1;
-  if (k == 0) return s2 == t2 ? spin_half_el(r, s1, t1) : cz();
-  return s1 == t1 ? spin_half_el(r, s2, t2) : cz();
-}
-__device__ __forceinline__ double2 nuc_el(int g, int c, int a, int b) {
-  double I = (g - 1) / 2.0;
-  double ma = I - a, mb = I - b;
-  if (c == 2) return a == b ? make_double2(ma, 0.0) : cz();
-  double l;
-  if (a == b - 1 || a == b + 1)
-    l = __dsqrt_rn(__dsub_rn(__dmul_rn(I, __dadd_rn(I, 1.0)), __dmul_rn(ma, mb)));
-  else
-    return cz();
-  if (c == 0) return make_double2(__dmul_rn(0.5, l), 0.0);
-  return a == b - 1 ? make_double2(0.0, __dmul_rn(-0.5, l)) : make_double2(0.0, __dmul_rn(0.5, l));
-}
-
 __device__ int gen_row_count(int64_t row, int64_t Z, int nn, const NucInfo* nuc) {
   int64_t n = row % Z;
   int cnt = 4;
@@ -181,73 +157,10 @@ __global__ void k_gen_count(int64_t N, int64_t Z, int nn, const NucInfo* __restr
 // delta = +stride_j for the nuclei (descending) that it raises. Strides of
 // nuclei with multiplicity >= 2 are distinct and |delta| < Z, so this is the
 // sorted order and no column repeats.
-__global__ void k_gen_fill(int64_t N, int64_t Z, int nn, const NucInfo* __restrict__ nuc,
-                           GenElectron el, const int* __restrict__ rowptr, int* __restrict__ col,
-                           double2* __restrict__ val) {
-  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= N) return;
-  int e = (int)(row / Z);
-  int64_t nidx = row - (int64_t)e * Z;
-  int base = rowptr[row];
-  auto couples = [&](int k, int ep) { return k == 0 ? ((e & 1) == (ep & 1)) : ((e >> 1) == (ep >> 1)); };
-  // entries below and above the diagonal per electron block
-  int nminus[4] = {0, 0, 0, 0}, nplus[4] = {0, 0, 0, 0};
-  for (int j = 0; j < nn; ++j) {
-    const NucInfo& q = nuc[j];
-    const int mj = nuc_state(q, nidx);
-    for (int ep = 0; ep < 4; ++ep)
-      if (couples(q.owner, ep)) {
-        nminus[ep] += mj > 0;
-        nplus[ep] += mj < q.g - 1;
-      }
-  }
-  int off[4];
-  off[0] = base;
-  for (int ep = 1; ep < 4; ++ep) off[ep] = off[ep - 1] + nminus[ep - 1] + 1 + nplus[ep - 1];
-  double2 d[4];
-  for (int ep = 0; ep < 4; ++ep) d[ep] = el.H[e][ep];
-  int seen_minus[4] = {0, 0, 0, 0}, seen_plus[4] = {0, 0, 0, 0};
-  for (int j = 0; j < nn; ++j) {
-    const NucInfo& q = nuc[j];
-    int g = q.g, k = q.owner;
-    int mj = nuc_state(q, nidx);
-    for (int mp = mj - 1; mp <= mj + 1; ++mp) {
-      if (mp < 0 || mp >= g) continue;
-      int64_t nc = nidx + (int64_t)(mp - mj) * q.stride;
-      double2 ie[3];
-      for (int c = 0; c < 3; ++c) ie[c] = nuc_el(g, c, mj, mp);
-      for (int ep = 0; ep < 4; ++ep) {
-        if (!couples(k, ep)) continue;
-        double2 v = cz();
-        for (int r = 0; r < 3; ++r) {
-          double2 se = pair_el(k, r, e, ep);
-          for (int c = 0; c < 3; ++c) v = xadd(v, xrscale(q.A[r * 3 + c], xmul(se, ie[c])));
-        }
-        if (ep == e)
-          for (int c = 0; c < 3; ++c) v = xadd(v, xrscale(q.zeta[c], ie[c]));
-        int pos;
-        if (mp == mj) {
-          d[ep] = xadd(d[ep], v);
-          continue;
-        } else if (mp < mj) {
-          pos = off[ep] + seen_minus[ep]++;
-        } else {
-          pos = off[ep] + nminus[ep] + 1 + (nplus[ep] - 1 - seen_plus[ep]++);
-        }
-        col[pos] = (int)((int64_t)ep * Z + nc);
-        val[pos] = v;
-      }
-    }
-  }
-  for (int ep = 0; ep < 4; ++ep) {
-    col[off[ep] + nminus[ep]] = (int)((int64_t)ep * Z + nidx);
-    val[off[ep] + nminus[ep]] = d[ep];
-  }
-}
-
-// k_gen_fill with the entry values read from the host-built tables
-// (HostSystem::gen_tab): the same values, without the per-row FP64 work that
-// dominates a build on a part with a narrow FP64 pipe.
+// Entry values come from the host-built tables (HostSystem::gen_tab), which
+// hold every nucleus' matrix elements rounded as the per-row arithmetic would
+// round them: a row does no FP64 work of its own, which would dominate a
+// build on a part with a narrow FP64 pipe.
 __global__ void k_gen_fill_tab(int64_t N, int64_t Z, int nn, const NucInfo* __restrict__ nuc,
                                GenElectron el, const double2* __restrict__ tab,
                                const int* __restrict__ rowptr, int* __restrict__ col,
@@ -346,6 +259,7 @@ struct BuildSlice {
   double2* val;
   int* xcol;            // execution-order copy for k_spmm (nnz)
   double2* xval;
+  double* xvs;          // Re + Im of every entry of the copy (nnz)
   int* split;           // N
   long long* total;     // 1
   bool herm;            // H = A - i*kappa*1: the execution copy holds A
@@ -387,7 +301,7 @@ static int build_slices(Handle* h, std::vector<BuildSlice>& sl, const std::vecto
       k_ref_fill<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->ref, b.rowptr, b.col, b.val);
     else
       k_gen_fill_tab<<<blocks, threads, 0, st>>>(N, Z, nn, b.nuc, b.hs->gen, b.tab, b.rowptr, b.col, b.val);
-    enqueue_split_rows(N, b.rowptr, b.col, b.val, b.xcol, b.xval, b.split, b.herm, b.meta, st);
+    enqueue_split_rows(N, b.rowptr, b.col, b.val, b.xcol, b.xval, b.xvs, b.split, b.herm, b.meta, st);
     h->count_launch(2);
   }
   if (cudaStreamSynchronize(st) != cudaSuccess)
@@ -436,7 +350,8 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode) {
   if (rc) return rc;
   if (h->ensure_rowptr(N + 1) || h->ensure_h_entries(nnz) || h->ensure(h->bcnt, sizeof(int) * N) ||
       h->ensure(h->btot, sizeof(long long)) || h->ensure(h->xcol, sizeof(int) * std::max<int64_t>(nnz, 1)) ||
-      h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nnz, 1)) || h->ensure(h->xsplit, sizeof(int) * N) ||
+      h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nnz, 1)) ||
+      h->ensure(h->xvs, sizeof(double) * std::max<int64_t>(nnz, 1)) || h->ensure(h->xsplit, sizeof(int) * N) ||
       h->ensure(h->hmeta, sizeof(HMeta)))
     return SPC_ERR_ALLOC;
   if (cudaMemsetAsync(h->hmeta.p, 0, sizeof(HMeta), h->stream) != cudaSuccess)
@@ -444,7 +359,8 @@ int build_h_device(Handle* h, const HostSystem& hs, int mode) {
   std::vector<BuildSlice> sl(1);
   sl[0] = BuildSlice{&hs, (const NucInfo*)h->bnuc.p, (const double2*)h->btab.p, (int*)h->bcnt.p, h->d_rowptr,
                      h->d_col, h->d_val,
-                     (int*)h->xcol.p, (double2*)h->xval.p, (int*)h->xsplit.p, (long long*)h->btot.p,
+                     (int*)h->xcol.p, (double2*)h->xval.p, (double*)h->xvs.p, (int*)h->xsplit.p,
+                     (long long*)h->btot.p,
                      hs.herm_shift, (HMeta*)h->hmeta.p};
   rc = build_slices(h, sl, {nnz}, mode);
   if (rc) return rc;
@@ -489,6 +405,7 @@ int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode)
   if (h->ensure(B.rowptr, sizeof(int) * rp_tot) || h->ensure(B.split, sizeof(int) * rp_tot) ||
       h->ensure(B.col, sizeof(int) * std::max<int64_t>(nz_tot, 1)) ||
       h->ensure(B.val, sizeof(double2) * std::max<int64_t>(nz_tot, 1)) ||
+      h->ensure(B.vsum, sizeof(double) * std::max<int64_t>(nz_tot, 1)) ||
       h->ensure(h->xcol, sizeof(int) * std::max<int64_t>(nz_tot, 1)) ||
       h->ensure(h->xval, sizeof(double2) * std::max<int64_t>(nz_tot, 1)) ||
       h->ensure(h->bcnt, sizeof(int) * std::max<int64_t>(n_tot, 1)) || h->ensure(h->btot, sizeof(long long) * ns) ||
@@ -502,7 +419,8 @@ int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode)
     sl[k] = BuildSlice{&hs[k], (const NucInfo*)h->bnuc.p + noff[k], (const double2*)h->btab.p, (int*)h->bcnt.p + coff,
                        (int*)B.rowptr.p + B.rp_off[k], (int*)h->xcol.p + B.nz_off[k],
                        (double2*)h->xval.p + B.nz_off[k], (int*)B.col.p + B.nz_off[k],
-                       (double2*)B.val.p + B.nz_off[k], (int*)B.split.p + B.rp_off[k],
+                       (double2*)B.val.p + B.nz_off[k], (double*)B.vsum.p + B.nz_off[k],
+                       (int*)B.split.p + B.rp_off[k],
                        (long long*)h->btot.p + k, hs[k].herm_shift, (HMeta*)B.meta.p + k};
     coff += hs[k].N;
   }
@@ -526,53 +444,99 @@ int build_h_batch_device(Handle* h, const std::vector<HostSystem>& hs, int mode)
 // Allocation-free Hamiltonian build (spc_build_h_noalloc).
 //
 // For callers that must not allocate device memory themselves or through
-// the library: code running under a CUDA stream capture or inside a memory
-// pool whose budget is fixed up front, or hosts (Fortran programs, plugins)
-// that only hand over buffers they own. The caller passes the system and the
-// CSR output buffers; the per-row counts, the nucleus table and the nonzero
-// total live in the file-scope array below, which every GPU that loads the
-// library holds until the process exits (about 4.2 MB).
+// the library: hosts that run inside a device-memory pool whose budget is
+// fixed up front, or that only hand over buffers they own (Fortran programs,
+// plugins). The caller passes the system and the CSR output buffers; the
+// per-row counts, the nucleus table, the general builder's entry tables and
+// the nonzero total live in the file-scope array below, which every GPU that
+// loads the library holds until the process exits (about 5.2 MB).
 //
-// Limits: at most SPC_NOALLOC_MAX_ROWS rows (Hilbert dimension) and
-// SPC_NOALLOC_MAX_NUC nuclei; larger systems are rejected with SPC_ERR_ARG.
-// Every call on a device shares the one array and it keeps the last call's
-// contents (counts and table are rewritten before use); calls that overlap
-// on the GPU (different streams, or different host threads on one device)
-// race on it and must be serialised by the caller.
+// Limits: at most SPC_NOALLOC_MAX_ROWS rows (Hilbert dimension),
+// SPC_NOALLOC_MAX_NUC nuclei and SPC_NOALLOC_MAX_TAB entry-table elements
+// (48 per nucleus and unit of multiplicity); larger systems are rejected with
+// SPC_ERR_ARG. Every call on a device shares the one array and it keeps the
+// last call's contents (counts and tables are rewritten before use); calls
+// that overlap on the GPU (different streams, or different host threads on
+// one device) race on it and must be serialised by the caller. The call
+// waits for its own stream twice (after the count and after the fill).
+#include <cuda.h>
+
 #include <mutex>
 
 #define SPC_NOALLOC_MAX_ROWS (1 << 20)
 #define SPC_NOALLOC_MAX_NUC 64
+#define SPC_NOALLOC_MAX_TAB (1 << 16)
 #define SPC_NOALLOC_MAX_DEVICES 64
 
 namespace {
 struct NoAllocScratch {
   int cnt[SPC_NOALLOC_MAX_ROWS];
   spc::NucInfo nuc[SPC_NOALLOC_MAX_NUC];
+  double2 tab[SPC_NOALLOC_MAX_TAB];
   long long total;
 };
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
-// Device address of g_noalloc_scratch for each device, looked up once per
-// device (with that device current) on the first call there.
-static void* g_noalloc_ptr[SPC_NOALLOC_MAX_DEVICES];
+// Set-up: the device address of g_noalloc_scratch, looked up with
+// cudaGetSymbolAddress once per device context (with that device current)
+// and kept with the context's unique id. The address belongs to the
+// context: after cudaDeviceReset, or under another context of the device,
+// the id differs and the address is looked up again. If the driver's
+// context queries cannot be resolved, the address is looked up on every call.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+static struct {
+  unsigned long long ctx_id;
+  void* ptr;
+} g_noalloc_cache[SPC_NOALLOC_MAX_DEVICES];
 static std::mutex g_noalloc_mu;
+
+static bool current_context_id(unsigned long long* id) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (PfnCtxGetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PfnCtxGetId)f;
+  });
+  CUcontext ctx = nullptr;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 static int noalloc_scratch(int device, NoAllocScratch** out) {
   if (device < 0 || device >= SPC_NOALLOC_MAX_DEVICES)
     return spc::set_error(SPC_ERR_ARG, "device %d above the supported range", device);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return spc::set_error(SPC_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed: %s",
-                            cudaGetErrorString(e));
-    g_noalloc_ptr[device] = p;
+  unsigned long long id = 0;
+  const bool have_id = current_context_id(&id);
+  if (have_id && g_noalloc_cache[device].ptr && g_noalloc_cache[device].ctx_id == id) {
+    *out = (NoAllocScratch*)g_noalloc_cache[device].ptr;
+    return SPC_OK;
   }
-  *out = (NoAllocScratch*)g_noalloc_ptr[device];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return spc::set_error(SPC_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed: %s",
+                          cudaGetErrorString(e));
+  // the lookup makes the device's primary context current if none was
+  unsigned long long id2 = 0;
+  if (current_context_id(&id2)) {
+    g_noalloc_cache[device].ctx_id = id2;
+    g_noalloc_cache[device].ptr = p;
+  } else {
+    g_noalloc_cache[device].ptr = nullptr;
+  }
+  *out = (NoAllocScratch*)p;
   return SPC_OK;
 }
 
@@ -589,8 +553,24 @@ extern "C" int spc_build_h_noalloc(const spc_system* sys, int mode, int32_t* row
                           "spc_build_h_noalloc: dimension %lld above the %d rows of its scratch",
                           (long long)hs.N, SPC_NOALLOC_MAX_ROWS);
   if ((int)hs.nuc.size() > SPC_NOALLOC_MAX_NUC)
-    return spc::set_error(SPC_ERR_ARG, "spc_build_h_noalloc: more than %d nuclei",
+    return spc::set_error(SPC_ERR_ARG, "spc_build_h_noalloc: more than %d nuclei for its scratch",
                           SPC_NOALLOC_MAX_NUC);
+  const size_t ntab = mode == SPC_H_REFERENCE ? 0 : hs.gen_tab.size();
+  if (ntab > SPC_NOALLOC_MAX_TAB)
+    return spc::set_error(SPC_ERR_ARG,
+                          "spc_build_h_noalloc: entry tables of %zu elements above the %d of its scratch", ntab,
+                          SPC_NOALLOC_MAX_TAB);
+  // the closed-form count decides the size before anything is launched: a
+  // capacity that is too small is refused with every output buffer untouched
+  const int64_t predicted = spc::predict_nnz(hs, mode);
+  if (predicted > INT32_MAX)
+    return spc::set_error(SPC_ERR_ARG, "Hamiltonian has %lld nonzeros, above the int32 CSR limit",
+                          (long long)predicted);
+  *n_out = (int32_t)hs.N;
+  *nnz_out = predicted;
+  if (predicted > cap_nnz)
+    return spc::set_error(SPC_ERR_ARG, "spc_build_h_noalloc: %lld nonzeros exceed the capacity %lld",
+                          (long long)predicted, (long long)cap_nnz);
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess)
     return spc::set_error(SPC_ERR_CUDA, "cudaGetDevice failed");
@@ -600,32 +580,45 @@ extern "C" int spc_build_h_noalloc(const spc_system* sys, int mode, int32_t* row
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t N = hs.N, Z = hs.Z;
   const int nn = (int)hs.nuc.size();
+  // pageable host sources: each copy has left the host buffer on return
   if (nn > 0 && cudaMemcpyAsync(scr->nuc, hs.nuc.data(), sizeof(spc::NucInfo) * nn,
                                 cudaMemcpyHostToDevice, st) != cudaSuccess)
     return spc::set_error(SPC_ERR_CUDA, "copy of the nucleus table failed");
+  if (ntab > 0 && cudaMemcpyAsync(scr->tab, hs.gen_tab.data(), sizeof(double2) * ntab, cudaMemcpyHostToDevice,
+                                  st) != cudaSuccess)
+    return spc::set_error(SPC_ERR_CUDA, "copy of the entry tables failed");
   const int threads = 256;
   const int blocks = (int)((N + threads - 1) / threads);
   if (mode == SPC_H_REFERENCE)
     spc::k_ref_count<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, scr->cnt);
   else
     spc::k_gen_count<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, scr->cnt);
-  spc::k_scan_rows<<<1, 1024, 0, st>>>(scr->cnt, rowptr_dev, N, &scr->total);
-  long long nnz = 0;
-  cudaMemcpyAsync(&nnz, &scr->total, sizeof(long long), cudaMemcpyDeviceToHost, st);
-  cudaError_t e = cudaStreamSynchronize(st);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    spc::k_scan_rows<<<1, 1024, 0, st>>>(scr->cnt, rowptr_dev, N, &scr->total);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess)
+    return spc::set_error(SPC_ERR_CUDA, "Hamiltonian count/scan launch failed: %s", cudaGetErrorString(e));
+  // the scanned total must equal the closed form before the fill writes
+  // through rowptr (it bounds every write to col/val by cap_nnz)
+  long long total = -1;
+  e = cudaMemcpyAsync(&total, &scr->total, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess)
     return spc::set_error(SPC_ERR_CUDA, "Hamiltonian count/scan failed: %s", cudaGetErrorString(e));
-  *n_out = (int32_t)N;
-  *nnz_out = nnz;
-  if (nnz > cap_nnz)
-    return spc::set_error(SPC_ERR_ARG, "spc_build_h_noalloc: %lld nonzeros exceed the capacity %lld",
-                          nnz, (long long)cap_nnz);
+  if (total != predicted)
+    return spc::set_error(SPC_ERR_STATE, "internal: %lld nonzeros counted, %lld predicted", total,
+                          (long long)predicted);
   if (mode == SPC_H_REFERENCE)
     spc::k_ref_fill<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, hs.ref, rowptr_dev, col_dev,
                                                 (double2*)val_dev);
   else
-    spc::k_gen_fill<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, hs.gen, rowptr_dev, col_dev,
-                                                (double2*)val_dev);
+    spc::k_gen_fill_tab<<<blocks, threads, 0, st>>>(N, Z, nn, scr->nuc, hs.gen, scr->tab, rowptr_dev, col_dev,
+                                                    (double2*)val_dev);
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return spc::set_error(SPC_ERR_CUDA, "Hamiltonian fill launch failed: %s", cudaGetErrorString(e));
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess)
     return spc::set_error(SPC_ERR_CUDA, "Hamiltonian fill failed: %s", cudaGetErrorString(e));
