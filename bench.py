@@ -5,10 +5,9 @@ Workload (one "step"): the single large radical pair (radical A = two 14N +
 five 1H, radical B = one 14N + four 1H; anisotropic hyperfine tensors, tilted
 0.05 mT field, J = 0.01 mT, axial D = -0.4 mT, kS = kT = 1/us), M = 512
 random-phase sample vectors, Krylov dimension 30, dt = 1 ns, propagated over
-a window of --window-ns (default 100 ns = 100 dt steps, about four Krylov
-builds per sample, the steady-state build/reuse ratio of the full 2 us run).
-A step is the whole hot path: device Hamiltonian build (general builder) +
-batched propagation + sample average.
+a window of --window-ns (default 2000 ns = 2000 dt steps, the configuration's
+whole 2 us window). A step is the whole hot path: device Hamiltonian build
+(general builder) + batched propagation + sample average.
 
 Metric: sample-steps/s = M * (dt steps per sample) / wall time.
   value  device-resident inputs (spc_trace_sampling_device)
@@ -37,15 +36,14 @@ from spin_dynamics_gb300 import workloads as W  # noqa: E402
 
 # The headline metric as named for this path; `value` is the plain (per-instance) trace
 # sampling at dim 55296, `adjoint` / `batched_adjoint` the gradient legs, `accuracy` the
-# |Delta Phi_S| check against the oracle on the CPU leg's vectors.
+# |Delta Phi_S| check against the oracle on the first vectors of the timed set.
 METRIC = "sample-steps/s at dim 55296: batched+adjoint vs plain on GB300 at |\u0394\u03a6S|\u22641e-10"
 
 # DRAM traffic per k_spmm launch (dram__bytes_read.sum + dram__bytes_write.sum)
-# from one ncu capture at 64 sample columns (profiles/k_spmm_dim55296_M64_full.md:
-# 180 MB = 33 MB of Hamiltonian + 147 MB that scales with the columns), scaled
-# to the launch's column count.
+# from one ncu capture at 64 sample columns (392 MB = 33 MB of Hamiltonian +
+# 359 MB that scales with the columns), scaled to the launch's column count.
 SPMM_TRAFFIC_H = 33.2e6
-SPMM_TRAFFIC_PER_COLUMN = (180.1e6 - 33.2e6) / 64
+SPMM_TRAFFIC_PER_COLUMN = (392.2e6 - 33.2e6) / 64
 
 
 def parse():
@@ -63,9 +61,15 @@ def parse():
                    help="CPU sample size (0 = cores x max(1, 1200 / dt steps): one vector per core at 2 us)")
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=5,
+                   help="steps of the end-to-end leg (at most --steps)")
     p.add_argument("--no-batch", action="store_true", help="skip the batched uneven-set leg")
-    p.add_argument("--batch-pairs", type=int, default=16)
-    p.add_argument("--batch-orient", type=int, default=4)
+    p.add_argument("--batch-pairs", type=int, default=256)
+    p.add_argument("--batch-orient", type=int, default=64)
+    p.add_argument("--batch-tiled-arm", action="store_true",
+                   help="also time the per-instance calls kept on the tiled path")
+    p.add_argument("--badj-pairs", type=int, default=16, help="pairs of the batched-adjoint leg")
+    p.add_argument("--badj-orient", type=int, default=4, help="orientations of the batched-adjoint leg")
     p.add_argument("--batch-window-ns", type=float, default=20.0)
     p.add_argument("--batch-krylov", type=int, default=20)
     p.add_argument("--batch-sample-path", default="auto", choices=["auto", "on", "off"],
@@ -78,12 +82,18 @@ def parse():
     p.add_argument("--sym-samples", type=int, default=32)
     p.add_argument("--sym-window-ns", type=float, default=4.0)
     p.add_argument("--sym-directions", type=int, default=2)
+    p.add_argument("--no-sym-full-forward", dest="sym_full_forward", action="store_false",
+                   help="skip the one-direction plain forward at M = 128 over 1 us")
     p.add_argument("--adjoint-samples", type=int, default=256)
-    p.add_argument("--adjoint-window-ns", type=float, default=20.0)
-    p.add_argument("--adjoint-checkpoint", type=int, default=10)
-    p.add_argument("--adjoint-quad", type=int, default=6)
-    p.add_argument("--adjoint-krylov", type=int, default=16,
+    p.add_argument("--adjoint-window-ns", type=float, default=400.0,
+                   help="adjoint window (400 ns = four segments of the 100-step checkpoint spacing)")
+    p.add_argument("--adjoint-checkpoint", type=int, default=100)
+    p.add_argument("--adjoint-quad", type=int, default=0,
+                   help="Gauss-Legendre nodes per step (0 = the library's rule from the norm bound of H)")
+    p.add_argument("--adjoint-krylov", type=int, default=30,
                    help="Krylov dimension of the stepwise model (one basis per dt step)")
+    p.add_argument("--adjoint-variants", action="store_true",
+                   help="also time memory-sized checkpoints, 5 and 8 nodes and m = 16 on a 20-step window")
     return p.parse_args()
 
 
@@ -126,41 +136,80 @@ def oracle_csr(sysp, B):
                                               sysp.J, sysp.D, sysp.kS, sysp.kT)
 
 
-def cpu_leg(args, sysp, B, sim, threads):
+def timed_vectors(args, sysp, rank=0):
+    """The headline's M random-phase vectors (rank's own set)."""
+    return W.random_phase_samples(sysp.Z, args.samples, seed=7 + rank)
+
+
+def cpu_sample_size(args, sim, threads):
+    steps = int(round(sim.t_end / sim.dt))
+    return args.cpu_samples or threads * max(1, round(1200 / steps))
+
+
+def cpu_leg(args, sysp, B, sim, threads, zk):
     """Time the oracle (fast build) on a bounded sample of the same workload:
-    the whole window on fewer vectors (one per core at 2 us)."""
+    the whole window on the first vectors of the timed set (one per core at
+    2 us)."""
     pyoracle, (rp, col, val) = oracle_csr(sysp, B)
     steps = int(round(sim.t_end / sim.dt))
-    ns = args.cpu_samples or threads * max(1, round(1200 / steps))
-    zk = W.random_phase_samples(sysp.Z, ns)
+    ns = zk.shape[0]
     t0 = time.perf_counter()
     r = pyoracle.trace_sampling(rp, col, val, zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol,
                                 fast=True, threads=threads)
     el = time.perf_counter() - t0
-    cpu_leg.last = (sim, zk, r)  # the window, vectors and oracle populations, for the accuracy check
+    cpu_leg.last = r  # the oracle populations on these vectors, for the accuracy check
     return {"value": ns * steps / el, "unit": "sample-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{ns} samples x {steps} dt steps of the same system (Krylov builds "
-                      f"{int(r['n_builds'].sum())}), oracle -O3 native OpenMP, {el:.2f} s, "
+            "sample": f"{ns} samples (the first of the timed set) x {steps} dt steps of the same system "
+                      f"(Krylov builds {int(r['n_builds'].sum())}), oracle -O3 native OpenMP, {el:.2f} s, "
                       f"CPU {cpu_model()}"}
 
 
-def accuracy_check(sysp, B, sim, zk, ref):
-    """|Delta Phi_S| and max |Delta P_S| between the GPU path and the oracle on
-    the same vectors (same system, window, m, tol)."""
-    from spin_dynamics_gb300.dynamics import TraceSampler
+def accuracy_check(sampler, method, sysp, B, sim, zk, ref_fast, threads):
+    """GPU against the oracle on the first vectors of the timed set over the
+    whole window (same system, m, tol), through the timed handle: in the
+    headline's Krylov mode and in MGS. Beside them, the oracle's parity build
+    (no FMA contraction) against its -O3 FMA build on the same vectors: the
+    reference algorithm's own sensitivity to rounding over a long window."""
     from spin_dynamics_gb300.observables import Observables
 
-    with TraceSampler(0) as s:
-        s.build_h(sysp, B, "general")
-        got = s.trace_sampling(zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol)
-    cpu = Observables(ref["P_S"].copy(), ref["P_T0"].copy(), ref["P_Tp"].copy(), ref["P_Tm"].copy())
-    got.get_kinetics(sim.dt, sysp.kS, sysp.kT)
-    cpu.get_kinetics(sim.dt, sysp.kS, sysp.kT)
-    return {"max_abs_dPhi_S": float(np.max(np.abs(got.Phi_S - cpu.Phi_S))),
-            "max_abs_dP_S": float(np.max(np.abs(got.P_S - cpu.P_S))), "Phi_S": float(got.Phi_S[-1]),
-            "samples": int(zk.shape[0]), "window_ns": round(sim.t_end / sim.dt),
-            "bound": 1e-10,
-            "reference": "oracle (C++ restatement of the Fortran path) on the same vectors"}
+    pyoracle, (rp, col, val) = oracle_csr(sysp, B)
+    ref = pyoracle.trace_sampling(rp, col, val, zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol,
+                                  threads=threads)
+
+    def obs(r):
+        o = Observables(r["P_S"].copy(), r["P_T0"].copy(), r["P_Tp"].copy(), r["P_Tm"].copy())
+        o.get_kinetics(sim.dt, sysp.kS, sysp.kT)
+        return o
+
+    def diff(a, b):
+        return {"max_abs_dPhi_S": float(np.max(np.abs(a.Phi_S - b.Phi_S))),
+                "max_abs_dP_S": float(np.max(np.abs(a.P_S - b.P_S))),
+                "max_abs_dP_all": float(max(np.max(np.abs(getattr(a, k) - getattr(b, k)))
+                                            for k in ("P_S", "P_T0", "P_Tp", "P_Tm")))}
+
+    o_ref = obs(ref)
+    lanczos = method in ("auto", "lanczos") and sysp.kS == sysp.kT
+    modes = [("lanczos" if lanczos else "mgs", method)] + ([("mgs", "mgs")] if lanczos else [])
+    out = {"samples": int(zk.shape[0]), "vectors": "the first of the timed set",
+           "window_ns": round(sim.t_end / sim.dt), "bound": 1e-10, "bound_on": "Phi_S",
+           "reference": "oracle parity build (C++ restatement of the Fortran path, no FMA contraction)"}
+    try:
+        for name, m in modes:
+            sampler.set_krylov(m)
+            sampler.build_h(sysp, B, "general")
+            got = sampler.trace_sampling(zk, sim.dt, sim.t_end, sim.N_krylov, sim.tol)
+            got.get_kinetics(sim.dt, sysp.kS, sysp.kT)
+            d = diff(got, o_ref)
+            d["lanczos_fallbacks"] = int(sampler.stats()["lanczos_fallbacks"])
+            d["Phi_S"] = float(got.Phi_S[-1])
+            out[name] = d
+    finally:
+        sampler.set_krylov(method)
+    first = out[modes[0][0]]
+    out.update(max_abs_dPhi_S=first["max_abs_dPhi_S"], max_abs_dP_S=first["max_abs_dP_S"],
+               method=modes[0][0], Phi_S=first["Phi_S"],
+               oracle_fast_vs_parity_build=diff(obs(ref_fast), o_ref))
+    return out
 
 
 class Clocks:
@@ -236,7 +285,7 @@ def run_ours(args, rank, world, local_rank):
     steps_per_sample = int(round(sim.t_end / sim.dt))
     sampler = TraceSampler(local_rank)
     sampler.set_krylov(args.method)
-    zk_host = W.random_phase_samples(sysp.Z, M, seed=7 + rank)
+    zk_host = timed_vectors(args, sysp, rank)
     zk_dev = torch.from_numpy(zk_host).to(f"cuda:{local_rank}")
     out_dev = torch.empty(4 * T, dtype=torch.float64, device=f"cuda:{local_rank}")
     # one stream for the library's launches and the timing events
@@ -257,8 +306,8 @@ def run_ours(args, rank, world, local_rank):
     for _ in range(args.warmup):
         step_device()
     torch.cuda.synchronize()
-    # timed region, device-resident inputs; kernel classes timed with events
-    nat.check(nat.lib().spc_set_profiling(sampler.handle, 1))
+    # timed region: device-resident inputs, no per-launch timing (build
+    # rounds of a repeating shape replay as CUDA graphs)
     launches = 0
     builds = 0
     fallbacks = 0
@@ -278,8 +327,13 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
     barrier()
     ms = e0.elapsed_time(e1) / args.steps
+    # one more step with per-kernel-class CUDA events, for the kernel shares
+    # and the roofline of the dominant kernel (not part of the timed steps)
     prof = {}
     import ctypes as C
+    nat.check(nat.lib().spc_set_profiling(sampler.handle, 1))
+    step_device()
+    torch.cuda.synchronize()
     for k in range(nat.SPC_KERNEL_KINDS):
         a, n, f, b = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
         nat.lib().spc_get_profile(sampler.handle, k, C.byref(a), C.byref(n), C.byref(f), C.byref(b))
@@ -291,7 +345,8 @@ def run_ours(args, rank, world, local_rank):
         ms = float(t.item())
     value = world * M * steps_per_sample / (ms / 1e3)
 
-    # e2e through the C ABI with host buffers
+    # e2e through the C ABI with host buffers (pinned), over at most
+    # --e2e-steps of the timed steps
     e2e = None
     if not args.no_e2e:
         zk_pin = torch.from_numpy(zk_host).pin_memory()
@@ -299,20 +354,28 @@ def run_ours(args, rank, world, local_rank):
         step_host = lambda: (sampler.build_h(sysp, B, "general"),
                              sampler.trace_sampling(zk_np, sim.dt, sim.t_end, m, sim.tol))
         step_host()
+        n_e2e = max(1, min(args.steps, args.e2e_steps))
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(n_e2e):
             res = step_host()[1]
         torch.cuda.synchronize()
-        el = (time.perf_counter() - t0) / args.steps
+        el = (time.perf_counter() - t0) / n_e2e
         if world > 1:
             t = torch.tensor([el], device=f"cuda:{local_rank}")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             el = float(t.item())
         e2e = {"value": world * M * steps_per_sample / el, "unit": "sample-steps/s",
                "h2d_bytes_per_step": int(zk_host.nbytes), "d2h_bytes_per_step": int(4 * T * 8),
-               "ms_per_step": el * 1e3}
+               "ms_per_step": el * 1e3, "steps": n_e2e}
+    # parity of the timed path: oracle on the first vectors of the timed set
+    cpu = accuracy = None
+    if rank == 0 and not args.no_cpu:
+        threads = host_cores()
+        zs = zk_host[:cpu_sample_size(args, sim, threads)]
+        cpu = cpu_leg(args, sysp, B, sim, threads, zs)
+        accuracy = accuracy_check(sampler, args.method, sysp, B, sim, zs, cpu_leg.last, threads)
     batched = None if args.no_batch else batched_leg(args, sampler, local_rank)
     adjoint = None if args.no_adjoint else adjoint_leg(args, sampler, value / world)
     batch_adjoint = None if args.no_batch_adjoint else batched_adjoint_leg(args, sampler, local_rank)
@@ -321,22 +384,36 @@ def run_ours(args, rank, world, local_rank):
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
     return dict(ms=ms, value=value, e2e=e2e, batched=batched, adjoint=adjoint, batch_adjoint=batch_adjoint,
-                symmetry=symmetry, small=small,
+                symmetry=symmetry, small=small, cpu=cpu, accuracy=accuracy,
                 prof=prof, clocks=clk.summary(), launches=launches,
                 builds=builds, fallbacks=fallbacks, fp64_peak=fp64.value * 1e12, M=M, steps_per_sample=steps_per_sample,
                 sysp=sysp, B=B, sim=sim)
 
 
+def fp64_peak(device):
+    """FP64 FMA peak of the device in FLOP/s, from the library's DFMA probe."""
+    import ctypes as C
+
+    from spin_dynamics_gb300 import _native as nat
+    v = C.c_double()
+    nat.check(nat.lib().spc_fp64_peak(device, C.byref(v)))
+    return v.value * 1e12
+
+
 def batched_leg(args, sampler, local_rank):
     """The uneven set: pairs of dims 16..9216 x field orientations, every job
-    with its own Hamiltonian and 32-256 samples. Times one batched call
-    (spc_build_h_batch + spc_trace_sampling_batch_device) against the same
-    jobs as per-instance calls (spc_build_h + spc_trace_sampling_device)."""
+    with its own Hamiltonian and 32-256 samples (full size by default: 256
+    pairs x 64 orientations). Times the batched calls (spc_build_h_batch +
+    spc_trace_sampling_batch_device, split into consecutive job groups by
+    device memory) against the same jobs as per-instance calls (spc_build_h +
+    spc_trace_sampling_device). The FP64 operations the batched run issues,
+    at the measured FP64 peak, bound how fast any schedule could run them:
+    `ratio_bound_fp64` is the per-instance time over that minimum."""
     import torch
 
     from spin_dynamics_gb300.dynamics import batch_groups, device_memory, num_time_points, padded_samples
 
-    pairs, dirs, systems, fields, zks = uneven_jobs(args)
+    pairs, dirs, systems, fields, zks = uneven_jobs(args.batch_pairs, args.batch_orient)
     Ms = [z.shape[0] for z in zks]
     dt = 1.0 * 176.08596 / 1000
     t_end = args.batch_window_ns * 176.08596 / 1000
@@ -359,8 +436,8 @@ def batched_leg(args, sampler, local_rank):
                           free * 0.5 / (16.0 * (m + 4)))
     stream = torch.cuda.current_stream()
 
-    def per_instance():
-        for k in range(len(zks)):
+    def per_instance(jobs=None):
+        for k in (range(len(zks)) if jobs is None else jobs):
             sampler.build_h(systems[k], fields[k], "general")
             sampler.trace_sampling_device(zk_dev.data_ptr() + 16 * int(offs[k]), Ms[k], dt, t_end, m,
                                           1e-5, out_dev.data_ptr() + 8 * k * 4 * T)
@@ -368,18 +445,15 @@ def batched_leg(args, sampler, local_rank):
     def batched():
         sampler.set_sample_path(args.batch_sample_path)
         try:
-            batched_calls()
+            for grp in groups:
+                sampler.build_h_batch([systems[i] for i in grp], [fields[i] for i in grp], "general")
+                sampler.trace_sampling_batch_device(zk_dev.data_ptr() + 16 * int(offs[grp[0]]),
+                                                    [Ms[i] for i in grp], dt, t_end, m, 1e-5,
+                                                    out_dev.data_ptr() + 8 * grp[0] * 4 * T)
         finally:
             sampler.set_sample_path("auto")
 
-    def batched_calls():
-        for grp in groups:
-            sampler.build_h_batch([systems[i] for i in grp], [fields[i] for i in grp], "general")
-            sampler.trace_sampling_batch_device(zk_dev.data_ptr() + 16 * int(offs[grp[0]]), [Ms[i] for i in grp],
-                                                dt, t_end, m, 1e-5, out_dev.data_ptr() + 8 * grp[0] * 4 * T)
-
     def timed(fn):
-        fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -390,34 +464,44 @@ def batched_leg(args, sampler, local_rank):
 
     steps = int(round(t_end / dt))
     work = sum(Ms) * steps
-    batched()  # first launches of the leg are the batched call's (allocation, page-in)
-    t_single = timed(per_instance)
-    # the same per-instance calls kept on the tiled path (small jobs otherwise
-    # take the one-CTA-per-sample kernel)
-    sampler.set_sample_path("off")
-    try:
-        t_single_tiles = timed(per_instance)
-    finally:
-        sampler.set_sample_path("auto")
+    # first run of the leg: allocation and page-in, with per-kernel-class timing
     breakdown = profiled(sampler, batched)
     t_batch = timed(batched)
+    per_instance(range(min(len(zks), 64)))  # warm-up of the per-instance calls
+    t_single = timed(per_instance)
+    out = {}
+    if args.batch_tiled_arm:
+        # the same per-instance calls kept on the tiled path (small jobs
+        # otherwise take the one-CTA-per-sample kernel)
+        sampler.set_sample_path("off")
+        try:
+            t_tiles = timed(per_instance)
+        finally:
+            sampler.set_sample_path("auto")
+        out.update(per_instance_tiled_value=work / t_tiles, ratio_vs_tiled_per_instance=t_tiles / t_batch)
     t_build = timed(lambda: [sampler.build_h_batch([systems[i] for i in grp], [fields[i] for i in grp], "general")
                              for grp in groups])
+    flops = sum(v["gflop"] for v in breakdown.values()) * 1e9
+    peak = fp64_peak(local_rank)
+    t_min = flops / peak
     dims = [4 * s.Z for s in systems]
-    return {"value": work / t_batch, "per_instance_value": work / t_single,
-            "ratio": t_single / t_batch, "per_instance_tiled_value": work / t_single_tiles,
-            "ratio_vs_tiled_per_instance": t_single_tiles / t_batch, "unit": "sample-steps/s", "jobs": len(zks),
-            "pairs": len(pairs), "orientations": len(dirs), "dims": [min(dims), max(dims)],
-            "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m, "kernel_breakdown": breakdown,
-            "seconds": t_batch, "build_seconds": t_build, "per_instance_seconds": t_single,
-            "krylov_autotune_rates": tune_rates, "batches": len(groups),
-            "workload": "uneven pairs (2-10 nuclei from 1H/14N, anisotropic) x Fibonacci-sphere "
-                        "orientations at 0.05 mT, own Hamiltonian per job"}
+    out.update({"value": work / t_batch, "per_instance_value": work / t_single,
+                "ratio": t_single / t_batch, "ratio_bound_fp64": t_single / t_min,
+                "fp64_issued_gflop": flops / 1e9, "fp64_peak_tflops": peak / 1e12,
+                "fp64_frac_batched": t_min / t_batch, "fp64_frac_per_instance": t_min / t_single,
+                "unit": "sample-steps/s", "jobs": len(zks),
+                "pairs": len(pairs), "orientations": len(dirs), "dims": [min(dims), max(dims)],
+                "samples": int(sum(Ms)), "dt_steps": steps, "krylov": m, "kernel_breakdown": breakdown,
+                "seconds": t_batch, "build_seconds": t_build, "per_instance_seconds": t_single,
+                "krylov_autotune_rates": tune_rates, "batches": len(groups),
+                "workload": "uneven pairs (2-10 nuclei from 1H/14N, anisotropic) x Fibonacci-sphere "
+                            "orientations at 0.05 mT, own Hamiltonian per job"})
+    return out
 
 
 def profiled(sampler, fn):
     """Run fn once with per-kernel-class CUDA-event timing on; returns
-    {class: {ms, launches, tflops}} (an untimed warm-up run)."""
+    {class: {ms, launches, tflops, gflop}} (an untimed run)."""
     import ctypes as C
 
     from spin_dynamics_gb300 import _native as nat
@@ -429,15 +513,15 @@ def profiled(sampler, fn):
         nat.lib().spc_get_profile(sampler.handle, k, C.byref(a), C.byref(n), C.byref(f), C.byref(b))
         if n.value:
             out[nat.lib().spc_kernel_kind_name(k).decode()] = {
-                "ms": round(a.value, 3), "launches": n.value,
+                "ms": round(a.value, 3), "launches": n.value, "gflop": round(f.value / 1e9, 3),
                 "tflops": round(f.value / (a.value / 1e3) / 1e12, 4) if a.value else None}
     nat.check(nat.lib().spc_set_profiling(sampler.handle, 0))
     return out
 
 
-def uneven_jobs(args):
-    pairs = W.uneven_pairs(args.batch_pairs)
-    dirs = W.fibonacci_sphere(args.batch_orient)
+def uneven_jobs(n_pairs, n_orient):
+    pairs = W.uneven_pairs(n_pairs)
+    dirs = W.fibonacci_sphere(n_orient)
     systems, fields, zks = [], [], []
     for p, (s, M) in enumerate(pairs):
         z = W.random_phase_samples(s.Z, M, seed=100 + p)  # shared by the pair's orientations
@@ -456,7 +540,7 @@ def batched_adjoint_leg(args, sampler, local_rank):
     jobs over the same window. Host vectors in, results out, in every arm."""
     import torch
 
-    pairs, dirs, systems, fields, zks = uneven_jobs(args)
+    pairs, dirs, systems, fields, zks = uneven_jobs(args.badj_pairs, args.badj_orient)
     dt = 1.0 * 176.08596 / 1000
     t_end = args.batch_adjoint_window_ns * 176.08596 / 1000
     m = args.batch_krylov
@@ -550,7 +634,10 @@ def symmetry_leg(args, sampler):
     --sym-directions Fibonacci-sphere directions at 0.05 mT, every (block,
     direction) job in one batched adjoint sweep (split only by device memory),
     against the plain batched forward of the same blocks (Krylov reuse) for
-    the first direction. Bounded window and samples per block."""
+    the first direction. Bounded window and samples per block for the
+    gradient, with the configuration's full map (32 directions, M = 128, 1 us)
+    projected from its measured rate; the plain forward also runs at the
+    configuration's own size for one direction."""
     import torch
 
     from spin_dynamics_gb300 import symmetry as S
@@ -581,6 +668,21 @@ def symmetry_leg(args, sampler):
     _, t_p = timed(lambda: S.symmetrised_dynamics(sysp, sim, sampler=sampler, field=0.05 * dirs[0]))
     work_g = len(bl) * args.sym_samples * len(dirs)
     T_steps = 2 * (num_time_points(sim.dt, sim.t_end) // 2) - 2  # steps of the Simpson grid
+    # the configuration's own size for one direction, plain forward: M = 128
+    # per block over the whole 1 us window (Krylov reuse, batched blocks)
+    full = None
+    if args.sym_full_forward:
+        sim_f = SimParam.from_input_units(type="symmetry_dynamics", B=[0.05], init_state="singlet",
+                                          seed=(42, 99), N_samples=128, t_end_ns=1000.0, dt_ns=1.0,
+                                          N_krylov=args.batch_krylov, tol=1e-5, M1=3, M2=2, block_tol=0.0)
+        r_f, t_full = timed(lambda: S.symmetrised_dynamics(sysp, sim_f, sampler=sampler, field=0.05 * dirs[0]))
+        r_f.get_kinetics(sim_f.dt, sysp.kS, sysp.kT)
+        full = {"value": len(bl) * 128 * 1000 / t_full, "seconds": t_full, "samples_per_block": 128,
+                "dt_steps": 1000, "directions": 1, "Phi_S": float(r_f.Phi_S[-1]),
+                "workload": "all blocks, M = 128 per block, 1 us at dt 1 ns, one direction, plain forward"}
+    # the configuration's full gradient map (32 directions, M = 128 per
+    # block, 1000 steps) at the bounded leg's measured gradient rate
+    work_cfg = len(bl) * 128 * 1000 * 32
     return {"value": work_g * T_steps / t_g, "unit": "sample-steps/s", "seconds": t_g,
             "stepwise_forward_value": work_g * T_steps / t_f, "cost_vs_stepwise_forward": t_g / t_f,
             "max_abs_dPhi_S_gradient_vs_forward_sweep": float(max(abs(a["Phi_S"] - b["Phi_S"]) for a, b in zip(g, y))),
@@ -590,6 +692,10 @@ def symmetry_leg(args, sampler):
             "dt_steps": T_steps, "krylov": args.batch_krylov,
             "Phi_S": [d["Phi_S"] for d in g], "dPhi_S_dtheta": [d["dtheta"] for d in g],
             "dPhi_S_dphi": [d["dphi"] for d in g],
+            "full_forward_one_direction": full,
+            "full_config_gradient_map": {"sample_steps": work_cfg, "directions": 32, "samples_per_block": 128,
+                                         "dt_steps": 1000,
+                                         "projected_seconds_at_measured_gradient_rate": work_cfg / (work_g * T_steps / t_g)},
             "workload": "symmetry-reduced large pair (14N + 3x4 equivalent 1H | 14N + 2x4 equivalent 1H), "
                         "compass directions at 0.05 mT, batched + adjoint"}
 
@@ -597,69 +703,86 @@ def symmetry_leg(args, sampler):
 def adjoint_leg(args, sampler, plain_value):
     """Yields and their gradient with respect to all 15 + 9*12 parameters of
     the large pair (spc_yield_gradient, host sample vectors in, gradient out)
-    against the stepwise forward it differentiates and the plain Krylov-reuse
-    forward of the headline measurement."""
+    at the adjoint configuration's settings (M = 256, m = 30, checkpoints
+    every 100 steps) over --adjoint-window-ns, against the stepwise forward it
+    differentiates and the plain Krylov-reuse forward of the headline.
+
+    Projection to the 2000-step window: the gradient runs N forward steps,
+    N - K recomputed ones (every segment but the last) and N backward steps
+    (costate build, node states, contractions), the stepwise forward N
+    steps. With a forward step costing f and a backward step c, the cost
+    ratio is (2N - K) f / (N f) + c / f, so from a window of N1 steps to
+    N2 = 2000 it grows by (N2 - K)/N2 - (N1 - K)/N1."""
     import torch
+
+    from spin_dynamics_gb300.dynamics import gradient_nodes
 
     sysp, B = W.large_pair()
     dt = 1.0 * 176.08596 / 1000
     t_end = args.adjoint_window_ns * 176.08596 / 1000
-    M, m = args.adjoint_samples, args.adjoint_krylov
+    M, m, K = args.adjoint_samples, args.adjoint_krylov, args.adjoint_checkpoint
+    nq = args.adjoint_quad or gradient_nodes(sysp, B, dt)
     zk = W.random_phase_samples(sysp.Z, M, seed=11)
     method = "lanczos" if args.method in ("auto", "lanczos") and sysp.kS == sysp.kT else "mgs"
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
     sampler.set_krylov(method)
+    out = {}
     try:
-        def grad():
-            return sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=args.adjoint_quad,
-                                          checkpoint_every=args.adjoint_checkpoint)
-
-        def fwd():
-            return sampler.stepwise_yields(sysp, B, zk, dt, t_end, m)
-
-        def timed(fn):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            r = fn()
-            torch.cuda.synchronize()
-            return r, time.perf_counter() - t0
-
-        # untimed first call (allocation, page-in) with per-kernel-class timing
-        breakdown = profiled(sampler, grad)
-        g, t_grad = timed(grad)
+        # untimed short run (allocation, page-in) with per-kernel-class timing
+        breakdown = profiled(sampler, lambda: sampler.yield_gradient(sysp, B, zk, dt, 20 * dt, m, n_quad=nq,
+                                                                     checkpoint_every=10))
+        g, t_grad = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=nq,
+                                                         checkpoint_every=K))
         st = sampler.stats()
-        y, t_fwd = timed(fwd)
-        # the same with the checkpoint spacing chosen by device memory (fewest recomputed steps)
-        _, t_auto = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=args.adjoint_quad,
-                                                         checkpoint_every=0))
-        kept_auto = bool(sampler.stats()["rounds"])
-        # fewer Gauss-Legendre nodes per step: cost, and the gradient's
-        # distance from an 8-node reference at the same checkpoints
-        g5, t_auto5 = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=5, checkpoint_every=0))
-        g8 = sampler.yield_gradient(sysp, B, zk, dt, t_end, m, n_quad=8, checkpoint_every=0)
-        gscale = float(np.max(np.abs(g8.raw)))
-        rel5 = float(np.max(np.abs(g5.raw - g8.raw))) / gscale
-        rel6 = float(np.max(np.abs(g.raw - g8.raw))) / gscale
-        # the stepwise model's accuracy at this m: the same forward at m = 30
-        y30 = sampler.stepwise_yields(sysp, B, zk, dt, t_end, 30)
+        y, t_fwd = timed(lambda: sampler.stepwise_yields(sysp, B, zk, dt, t_end, m))
+        steps = st["sample_steps"] // M
+        cost = t_grad / t_fwd
+        n2 = 2000
+        proj = cost + (n2 - K) / n2 - (steps - K) / steps if steps > K else None
+        if args.adjoint_variants:
+            # 20-step window: memory-sized checkpoints, 5 and 8 nodes, m = 16 vs m = 30
+            t20 = 20 * dt
+            _, t_f20 = timed(lambda: sampler.stepwise_yields(sysp, B, zk, dt, t20, m))
+            gq, t_q = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t20, m, n_quad=nq, checkpoint_every=0))
+            g5, t_5 = timed(lambda: sampler.yield_gradient(sysp, B, zk, dt, t20, m, n_quad=5, checkpoint_every=0))
+            g8 = sampler.yield_gradient(sysp, B, zk, dt, t20, m, n_quad=8, checkpoint_every=0)
+            gs = float(np.max(np.abs(g8.raw)))
+            y16 = sampler.stepwise_yields(sysp, B, zk, dt, t20, 16)
+            y30 = sampler.stepwise_yields(sysp, B, zk, dt, t20, 30)
+            out["variants_20_steps"] = {
+                "cost_vs_stepwise_forward_memory_sized": t_q / t_f20,
+                "cost_vs_stepwise_forward_memory_sized_5_nodes": t_5 / t_f20,
+                "grad_max_rel_diff_vs_8_nodes": {str(nq): float(np.max(np.abs(gq.raw - g8.raw))) / gs,
+                                                 "5": float(np.max(np.abs(g5.raw - g8.raw))) / gs},
+                "abs_dPhi_S_m16_vs_m30": abs(y16[0] - y30[0])}
     finally:
         sampler.set_krylov(args.method)
-    steps = st["sample_steps"] // M
     work = M * steps
-    return {"value": work / t_grad, "unit": "sample-steps/s", "seconds": t_grad,
-            "stepwise_forward_value": work / t_fwd, "cost_vs_stepwise_forward": t_grad / t_fwd,
-            "cost_vs_stepwise_forward_memory_sized_checkpoints": t_auto / t_fwd,
-            "cost_vs_stepwise_forward_memory_sized_5_nodes": t_auto5 / t_fwd,
-            "grad_max_rel_diff_vs_8_nodes": {"6": rel6, "5": rel5},
-            "memory_sized_node_states_kept": kept_auto,
-            "cost_vs_plain_forward": t_grad / (work / plain_value),
-            "params": int(g.raw.size), "samples": M, "dt_steps": int(steps), "krylov": m,
-            "krylov_method": method, "quadrature_nodes": args.adjoint_quad,
-            "checkpoint_every": args.adjoint_checkpoint, "node_states_kept": bool(st["rounds"]),
-            "krylov_builds": int(st["krylov_builds"]), "kernel_launches": int(st["kernel_launches"]),
-            "Phi_S": g.Phi_S, "Phi_S_forward_only": y[0], "Phi_S_stepwise_m30": y30[0],
-            "abs_dPhi_S_vs_m30": abs(y[0] - y30[0]), "kernel_breakdown": breakdown,
-            "workload": "large pair dim 55296 (anisotropic), gradient of Phi_S over B, J, D, kS, kT "
-                        "and every hyperfine tensor element; h2d of the sample vectors inside"}
+    out.update({"value": work / t_grad, "unit": "sample-steps/s", "seconds": t_grad,
+                "stepwise_forward_value": work / t_fwd, "stepwise_forward_seconds": t_fwd,
+                "cost_vs_stepwise_forward": cost,
+                "projected_cost_vs_stepwise_forward_2000_steps": proj,
+                "cost_vs_plain_forward": t_grad / (work / plain_value),
+                "params": int(g.raw.size), "samples": M, "dt_steps": int(steps), "krylov": m,
+                "krylov_method": method, "quadrature_nodes": nq,
+                "quadrature_nodes_rule": "smallest n with Gauss-Legendre remainder bound <= 1e-8 at the norm "
+                                         "bound of H_eff" if not args.adjoint_quad else "fixed",
+                "checkpoint_every": K, "segments": -(-int(steps) // K),
+                "node_states_kept": bool(st["rounds"]),
+                "krylov_builds_per_sample_step": st["krylov_builds"] / max(1, work),
+                "kernel_launches": int(st["kernel_launches"]),
+                "Phi_S": g.Phi_S, "Phi_S_forward_only": y[0], "abs_dPhi_S_gradient_vs_forward": abs(g.Phi_S - y[0]),
+                "kernel_breakdown_20_steps": breakdown,
+                "workload": "large pair dim 55296 (anisotropic), gradient of Phi_S over B, J, D, kS, kT "
+                            "and every hyperfine tensor element; h2d of the sample vectors inside"})
+    return out
 
 
 def main():
@@ -675,11 +798,12 @@ def main():
             return
         sysp, B, sim = workload(args)
         threads = host_cores()
+        zs = timed_vectors(args, sysp)[:cpu_sample_size(args, sim, threads)]
         vals = []
         for _ in range(max(1, args.warmup // 3)):
-            cpu_leg(args, sysp, B, sim, threads)  # warm-up (page-in, OpenMP pool)
+            cpu_leg(args, sysp, B, sim, threads, zs)  # warm-up (page-in, OpenMP pool)
         for _ in range(args.steps):
-            vals.append(cpu_leg(args, sysp, B, sim, threads))
+            vals.append(cpu_leg(args, sysp, B, sim, threads, zs))
         v = float(np.median([x["value"] for x in vals]))
         cb = dict(vals[0])
         cb["value"] = v
@@ -705,11 +829,7 @@ def main():
     avg_s = ms_tot / max(nl, 1) / 1e3
     ach_gbs = (by / max(nl, 1)) / avg_s / 1e9 if nl else None
     ach_tf = (fl / max(nl, 1)) / avg_s / 1e12 if nl else None
-    cpu = None
-    accuracy = None
-    if not args.no_cpu:
-        cpu = cpu_leg(args, r["sysp"], r["B"], r["sim"], host_cores())
-        accuracy = accuracy_check(r["sysp"], r["B"], *cpu_leg.last)
+    cpu, accuracy = r["cpu"], r["accuracy"]
     share = {k: round(v[0] / max(1e-9, sum(x[0] for x in prof.values())), 4) for k, v in prof.items()}
     line = dict(base, value=r["value"], ms_per_step=r["ms"], scaling="weak",
                 config={"workload": workload_name(args, r["M"], r["sim"].N_krylov, r["sim"].tol),

@@ -220,6 +220,13 @@ int spc_trace_sampling_batch_device(spc_handle* h, int n_jobs, const int* job_sy
  * 15 + 9 * (n_nuc1 + n_nuc2), or -1 for a bad argument. */
 int spc_yield_gradient_size(const spc_system* sys);
 
+/* Gauss-Legendre node count (no counterpart in the reference) that
+ * spc_yield_gradient uses with n_quad = 0 for `sys` at step dt: the smallest
+ * n whose remainder bound (2 b dt)^(2n) (n!)^4 / ((2n+1) ((2n)!)^3) is at
+ * most 1e-8, with b = sqrt(max row sum * max column sum) of |H_eff| >=
+ * ||H_eff||_2. Host only. */
+int spc_gradient_nodes(const spc_system* sys, double dt, int* n_quad);
+
 /* Singlet and triplet yields and the gradient of wS*Phi_S + wT*Phi_T with
  * respect to every parameter of `sys`, by the discrete adjoint of a stepwise
  * propagation. The reference computes the yields only (get_kinetics,
@@ -234,8 +241,8 @@ int spc_yield_gradient_size(const spc_system* sys);
  * spc_num_time_points(dt, t_end) grid (its last value).
  *   zkets            M x Z complex, host memory, sample-major
  *   n_quad           Gauss-Legendre nodes per step for the derivative of
- *                    exp(-i H dt) (1..16; 6 gives ~1e-8 relative error at
- *                    ||H|| dt ~ 5)
+ *                    exp(-i H dt) (1..16), or 0: the count
+ *                    spc_gradient_nodes picks (largest over the jobs)
  *   checkpoint_every forward states kept every this many steps (0 = among
  *                    the spacings that fit in device memory, the one that
  *                    recomputes the fewest steps)

@@ -83,6 +83,7 @@ SIGNATURES = {
     "spc_trace_sampling_batch": (_I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _I, _D, _P, _I]),
     "spc_trace_sampling_batch_device": (_I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _I, _D, _P, _I]),
     "spc_yield_gradient_size": (_I, [C.POINTER(spc_system)]),
+    "spc_gradient_nodes": (_I, [C.POINTER(spc_system), _D, C.POINTER(_I)]),
     "spc_yield_gradient": (_I, [_P, C.POINTER(spc_system), _P, _P, _I, _D, _D, _I, _I, _I, _D, _D, _P,
                                 _P]),
     "spc_yield_gradient_batch": (_I, [_P, _I, _P, _P, _P, _P, _D, _D, _I, _I, _I, _D, _D, _I, _P, _P]),

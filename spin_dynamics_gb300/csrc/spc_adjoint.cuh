@@ -506,13 +506,13 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
     h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
     pe = h->prof.begin(st);
     k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 1, 0, pa.rbeta, d_Q, d_xs);
-    h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
+    h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 40.0 * elems);
     h->count_launch(2);
     for (int i = 0; i < m; ++i) {
       pe = h->prof.begin(st);
       k_spmm<<<nis, blk, 0, st>>>(tiles, d_items_s, d_map, i, d_Q, d_xs, d_P, lanczos ? 0 : 1);
       h->prof.end(st, pe, PK_SPMM, (spmm_flops + (lanczos ? 0.0 : 4.0 * herm_rows)) * SPC_LANES,
-                  20.0 * (double)nnz_tiles + 32.0 * elems);
+                  28.0 * (double)nnz_tiles + 40.0 * elems);
       h->count_launch();
       pa.col_i = i;
       int j0 = 0;
@@ -552,7 +552,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
         h->prof.end(st, pe, PK_AXPY_NORM, (lanczos ? 8.0 : 12.0) * elems, 48.0 * elems);
         pe = h->prof.begin(st);
         k_scale<<<nip, blk, 0, st>>>(tiles, d_items, d_map, d_scol, x, d_P, 0, i + 1, pa.rbeta, d_Q, d_xs);
-        h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
+        h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 40.0 * elems);
         h->count_launch(2);
       }
     }

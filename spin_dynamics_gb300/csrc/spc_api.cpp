@@ -527,6 +527,76 @@ int spc_yield_gradient_size(const spc_system* sys) {
   return 15 + 9 * (sys->n_nuc1 + sys->n_nuc2);
 }
 
+// Upper bound on ||H_eff||_2 of the general builder's Hamiltonian:
+// sqrt(max row sum * max column sum) of |H| (Holder), each sum bounded by the
+// triangle inequality over the electronic 4x4 block and every nucleus' entry
+// table (its largest row / column over the nuclear states).
+static double h_norm_bound(const spc::HostSystem& hs) {
+  double rmax = 0.0, cmax = 0.0;
+  for (int e = 0; e < 4; ++e) {
+    double r = 0.0, c = 0.0;
+    for (int f = 0; f < 4; ++f) {
+      r += std::hypot(hs.gen.H[e][f].x, hs.gen.H[e][f].y);
+      c += std::hypot(hs.gen.H[f][e].x, hs.gen.H[f][e].y);
+    }
+    for (const spc::NucInfo& q : hs.nuc) {
+      const int g = q.g;
+      double rj = 0.0, cj = 0.0;
+      // row (e, m): entries to (f, m + d - 1); column (e, m'): entries from
+      // (f, m' - d + 1)
+      for (int m = 0; m < g; ++m) {
+        double rs = 0.0, cs = 0.0;
+        for (int f = 0; f < 4; ++f)
+          for (int d = 0; d < 3; ++d) {
+            const double2 v = hs.gen_tab[q.tab_off + ((size_t)(e * 4 + f) * g + m) * 3 + d];
+            rs += std::hypot(v.x, v.y);
+            const int ms = m - d + 1;
+            if (ms >= 0 && ms < g) {
+              const double2 w = hs.gen_tab[q.tab_off + ((size_t)(f * 4 + e) * g + ms) * 3 + d];
+              cs += std::hypot(w.x, w.y);
+            }
+          }
+        rj = std::max(rj, rs);
+        cj = std::max(cj, cs);
+      }
+      r += rj;
+      c += cj;
+    }
+    rmax = std::max(rmax, r);
+    cmax = std::max(cmax, c);
+  }
+  return std::sqrt(rmax * cmax);
+}
+
+// Gauss-Legendre nodes for the per-step derivative integral
+// int_0^dt <exp(iH^H(dt-s)) lam| dH/dp |exp(-iHs) psi> ds. Its 2n-th
+// derivative is at most (2||H|| )^(2n) times the integrand's scale, so the
+// n-node rule's relative error is at most
+//   (2||H|| dt)^(2n) (n!)^4 / ((2n+1) ((2n)!)^3)
+// (the Gauss-Legendre remainder); the count is the smallest n with that
+// below 1e-8, two orders under the 1e-6 agreement asked of the gradient.
+static int nodes_for(double hnorm, double dt) {
+  const double x = 2.0 * hnorm * dt;
+  for (int n = 1; n <= 16; ++n) {
+    double lf = 0.0;  // log of (n!)^4 / ((2n+1) ((2n)!)^3)
+    for (int k = 2; k <= n; ++k) lf += 4.0 * std::log((double)k);
+    for (int k = 2; k <= 2 * n; ++k) lf -= 3.0 * std::log((double)k);
+    lf -= std::log(2.0 * n + 1.0);
+    const double le = (x > 0.0 ? 2.0 * n * std::log(x) : -1e300) + lf;
+    if (le <= std::log(1e-8)) return n;
+  }
+  return 16;
+}
+
+int spc_gradient_nodes(const spc_system* sys, double dt, int* n_quad) {
+  if (!sys || !n_quad || !(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "spc_gradient_nodes: bad argument");
+  spc::HostSystem hs;
+  const int rc = spc::make_host_system(sys, SPC_H_GENERAL, hs);
+  if (rc) return rc;
+  *n_quad = nodes_for(h_norm_bound(hs), dt);
+  return SPC_OK;
+}
+
 // Gradient of one job from its sample sums (pair slot first; then either
 // (electron, nucleus) slots or nucleus-only slots per nucleus with g >= 2).
 static void gradient_from_sums(const spc_system* sys, const spc::HostSystem& hs, int which, int M,
@@ -618,7 +688,7 @@ int spc_yield_gradient_batch(spc_handle* h, int n_jobs, const spc_system* system
     return spc::set_error(SPC_ERR_ARG, "spc_yield_gradient_batch: null argument");
   if (!(dt > 0.0)) return spc::set_error(SPC_ERR_ARG, "dt must be positive");
   if (m < 1 || m > 48) return spc::set_error(SPC_ERR_ARG, "Krylov dimension %d outside [1, 48]", m);
-  if (n_quad < 1 || n_quad > 16) return spc::set_error(SPC_ERR_ARG, "n_quad %d outside [1, 16]", n_quad);
+  if (n_quad < 0 || n_quad > 16) return spc::set_error(SPC_ERR_ARG, "n_quad %d outside [0, 16]", n_quad);
   if (checkpoint_every < 0) return spc::set_error(SPC_ERR_ARG, "checkpoint_every must be >= 0");
   if (which != SPC_GRAD_ALL && which != SPC_GRAD_FIELD)
     return spc::set_error(SPC_ERR_ARG, "unknown gradient set %d", which);
@@ -639,6 +709,8 @@ int spc_yield_gradient_batch(spc_handle* h, int n_jobs, const spc_system* system
     ztot += (int64_t)M[k] * hs[k].Z;
     gtot += 15 + 9 * (int64_t)hs[k].nuc.size();
   }
+  if (n_quad == 0)  // the count the per-step bound asks for, the largest over the jobs
+    for (int k = 0; k < n_jobs; ++k) n_quad = std::max(n_quad, nodes_for(h_norm_bound(hs[k]), dt));
   CKR(cudaSetDevice(h->h.device));
   spc::Handle& H = h->h;
   if (grad) std::fill(grad, grad + gtot, 0.0);

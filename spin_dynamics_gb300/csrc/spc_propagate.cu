@@ -1560,13 +1560,14 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
       h->prof.end(st, pe, PK_DOT, 4.0 * elems, 16.0 * elems);
       pe = h->prof.begin(st);
       k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 1, 0, d_rb, d_Q, d_xs);
-      h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
+      h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 40.0 * elems);
       h->count_launch(2);
       for (int i = 0; i < m; ++i) {
         pe = h->prof.begin(st);
         k_spmm<<<nis, blk, 0, st>>>(d_tiles, d_items_s, d_map, i, d_Q, d_xs, d_P, lanczos ? 0 : 1);
-        // algorithmic traffic: H once per tile, X once, Y once
-        h->prof.end(st, pe, PK_SPMM, spmm_flops * SPC_LANES, 20.0 * (double)nnz_work + 32.0 * elems);
+        // algorithmic traffic: H (with its Re + Im) once per tile, X and its
+        // Re + Im plane once, Y once
+        h->prof.end(st, pe, PK_SPMM, spmm_flops * SPC_LANES, 28.0 * (double)nnz_work + 40.0 * elems);
         h->count_launch();
         pa.col_i = i;
         // MGS (get_krylov :453-456) projects p on Q_0..Q_i in order. Lanczos
@@ -1610,7 +1611,7 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
           pe = h->prof.begin(st);
           k_scale<<<nip, blk, 0, st>>>(d_tiles, d_items_p, d_map, d_scol, d_psi, d_P, 0, i + 1, d_rb,
                                        d_Q, d_xs);
-          h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 32.0 * elems);
+          h->prof.end(st, pe, PK_SCALE, 2.0 * elems, 40.0 * elems);
           h->count_launch(2);
         }
       }

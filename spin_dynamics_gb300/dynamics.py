@@ -371,12 +371,13 @@ class TraceSampler:
             C.c_void_p(zk_ptr), float(dt), float(t_end), int(m), float(tol), C.c_void_p(out_ptr), T))
 
     def yield_gradient(self, sys: SysParam, B, zkets, dt: float, t_end: float, m: int,
-                       n_quad: int = 6, checkpoint_every: int = 0, wS: float = 1.0, wT: float = 0.0,
+                       n_quad: int = 0, checkpoint_every: int = 0, wS: float = 1.0, wT: float = 0.0,
                        init_state: str = "singlet") -> "YieldGradient":
         """Yields (Phi_S, Phi_T) of the stepwise propagation and the gradient
         of wS*Phi_S + wT*Phi_T with respect to every parameter of the system
         (internal units: mT for B, J, D, A; kS, kT as stored), by the discrete
-        adjoint; the general Hamiltonian (anisotropic A, field vector)."""
+        adjoint; the general Hamiltonian (anisotropic A, field vector).
+        n_quad = 0 takes the Gauss-Legendre node count gradient_nodes gives."""
         st, keep = make_system(sys, B)
         npar = nat.lib().spc_yield_gradient_size(C.byref(st))
         zk = np.ascontiguousarray(zkets, np.complex128)
@@ -391,7 +392,7 @@ class TraceSampler:
         return YieldGradient.unpack(y, g, len(sys.e1.g_I), len(sys.e2.g_I))
 
     def yield_gradient_batch(self, systems, fields, zkets_list, dt: float, t_end: float, m: int,
-                             n_quad: int = 6, checkpoint_every: int = 0, wS: float = 1.0,
+                             n_quad: int = 0, checkpoint_every: int = 0, wS: float = 1.0,
                              wT: float = 0.0, hyperfine: bool = True, init_state: str = "singlet",
                              gradient: bool = True) -> list:
         """spc_yield_gradient_batch: job k = (systems[k], fields[k],
@@ -461,6 +462,16 @@ class TraceSampler:
         s = nat.spc_stats()
         nat.check(nat.lib().spc_get_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in nat.spc_stats._fields_}
+
+
+def gradient_nodes(sys: SysParam, B, dt: float) -> int:
+    """Gauss-Legendre nodes per step the yield gradient takes with n_quad = 0
+    (spc_gradient_nodes: the smallest count whose remainder bound at the
+    norm bound of H_eff is below 1e-8). Host only."""
+    st, keep = make_system(sys, B)
+    n = C.c_int()
+    nat.check(nat.lib().spc_gradient_nodes(C.byref(st), float(dt), C.byref(n)))
+    return n.value
 
 
 # ---------------------------------------------------------------------------

@@ -300,7 +300,7 @@ def symmetrised_dynamics(sys_: SysParam, sim: SimParam, out: Optional[str] = Non
 
 
 def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, directions=None,
-                               n_quad: int = 6, checkpoint_every: int = 0, wS: float = 1.0,
+                               n_quad: int = 0, checkpoint_every: int = 0, wS: float = 1.0,
                                wT: float = 0.0, exact_blocks: bool = False, gradient: bool = True) -> list:
     """Yields of the block decomposition and their gradient with respect to
     the field vector, J, D, kS and kT (the field set of
@@ -326,11 +326,14 @@ def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, d
     acc = [dict(Phi_S=0.0, Phi_T=0.0, B=np.zeros(3), J=0.0, D=np.zeros((3, 3)), kS=0.0, kT=0.0)
            for _ in fields]
     sizes = [4 * sel[j][3] * padded_samples(zks[j].shape[0]) for _, j in jobs]
+    # nodes per step: as given, or the largest count the norm bound asks of
+    # any (block, field) job (what the batched call takes with n_quad = 0)
+    nq = n_quad or max(dynamics.gradient_nodes(sel[j][2], fields[f], sim.dt) for f, j in jobs)
     # states per vector entry held by the sweep: basis, checkpoints, segment, node states
-    for grp in batch_groups(sizes, _budget_entries(sim.N_krylov + 6 + 8 * (n_quad + 1))):
+    for grp in batch_groups(sizes, _budget_entries(sim.N_krylov + 6 + 8 * (nq + 1))):
         systems = [sel[jobs[q][1]][2] for q in grp]
         got = sp.yield_gradient_batch(systems, [fields[jobs[q][0]] for q in grp], [zks[jobs[q][1]] for q in grp],
-                                      sim.dt, sim.t_end, sim.N_krylov, n_quad=n_quad,
+                                      sim.dt, sim.t_end, sim.N_krylov, n_quad=nq,
                                       checkpoint_every=checkpoint_every, wS=wS, wT=wT, hyperfine=False,
                                       init_state=sim.init_state, gradient=gradient)
         for q, g in zip(grp, got):

@@ -66,7 +66,7 @@ class _Yield(torch.autograd.Function):
 
 
 def yield_objective(params: torch.Tensor, sampler: TraceSampler, template: SysParam, zkets,
-                    dt: float, t_end: float, m: int, n_quad: int = 6, checkpoint_every: int = 0,
+                    dt: float, t_end: float, m: int, n_quad: int = 0, checkpoint_every: int = 0,
                     wS: float = 1.0, wT: float = 0.0) -> torch.Tensor:
     """wS*Phi_S + wT*Phi_T at `params` (float64, C layout); differentiable
     with respect to params through the adjoint sweep."""

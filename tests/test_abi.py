@@ -82,3 +82,50 @@ def test_yield_gradient_size_is_host_only():
     st, keep = make_system(s, 0.05)
     assert nat.lib().spc_yield_gradient_size(C.byref(st)) == 15 + 9 * 5
     assert nat.lib().spc_yield_gradient_size(None) == -1
+
+
+def _gl_integral(H, lam, V, psi, dt, n):
+    """n-node Gauss-Legendre value of int_0^dt <exp(iH^H(dt-s)) lam| V |exp(-iHs) psi> ds."""
+    from scipy.linalg import expm
+    x, w = np.polynomial.legendre.leggauss(n)
+    s = 0.5 * dt * (x + 1.0)
+    tot = 0.0j
+    for sk, wk in zip(s, w):
+        u = expm(1j * H.conj().T * (dt - sk)) @ lam
+        v = expm(-1j * H * sk) @ psi
+        tot += 0.5 * dt * wk * np.vdot(u, V @ v)
+    return tot
+
+
+@pytest.mark.parametrize("scale,dt", [(1.0, 0.17608596), (3.0, 0.17608596), (0.2, 0.5)])
+def test_gradient_node_rule_bounds_the_quadrature_error(scale, dt):
+    """spc_gradient_nodes (the count n_quad = 0 takes): its norm bound is at
+    least ||H_eff||_2, and n nodes integrate the derivative integrand of a
+    step to 1e-8 of the integrand's scale (a 20-node rule as reference)."""
+    import dense
+    from spin_dynamics_gb300 import workloads as W
+    from spin_dynamics_gb300.dynamics import gradient_nodes
+    s = W.notebook_pair()
+    rng = np.random.default_rng(3)
+    s.e1.A = [scale * (a + 0.3 * rng.standard_normal((3, 3))) for a in s.e1.A]
+    s.e2.A = [scale * (a + 0.3 * rng.standard_normal((3, 3))) for a in s.e2.A]
+    s.e1.A = [0.5 * (a + a.T) for a in s.e1.A]
+    s.e2.A = [0.5 * (a + a.T) for a in s.e2.A]
+    s.kS, s.kT = 0.011, 0.004
+    B = np.array([0.03, -0.02, 0.05])
+    n = gradient_nodes(s, B, dt)
+    assert 1 <= n <= 16
+    H = dense.hamiltonian(s.e1.g_I, s.e1.A, s.e2.g_I, s.e2.A, B, s.J, s.D, s.kS, s.kT,
+                          s.e1.gammas, s.e2.gammas)
+    psi = rng.standard_normal(H.shape[0]) + 1j * rng.standard_normal(H.shape[0])
+    lam = rng.standard_normal(H.shape[0]) + 1j * rng.standard_normal(H.shape[0])
+    psi /= np.linalg.norm(psi)
+    lam /= np.linalg.norm(lam)
+    V = dense.hamiltonian(s.e1.g_I, s.e1.A, s.e2.g_I, s.e2.A, B + [1e-3, 0, 0], s.J, s.D, s.kS, s.kT,
+                          s.e1.gammas, s.e2.gammas) - H  # a field-derivative direction
+    V /= np.linalg.norm(V, 2)
+    ref = _gl_integral(H, lam, V, psi, dt, 20)
+    got = _gl_integral(H, lam, V, psi, dt, n)
+    assert abs(got - ref) <= 1e-8 * dt
+    if n > 1:  # one node fewer is not always enough for the bound: the rule is not over-generous
+        assert abs(_gl_integral(H, lam, V, psi, dt, n - 1) - ref) <= 1.0 * dt

@@ -158,6 +158,59 @@ def test_full_size_directional_derivatives(sampler):
         assert abs(ad - fd) <= 1e-6 * np.linalg.norm(g.raw) * np.linalg.norm(d), (name, ad, fd)
 
 
+def richardson(f, x0, d, h):
+    """Central difference of f along d at x0, Richardson-extrapolated from
+    steps h and 2h (truncation O(h^4))."""
+    c = lambda k: (f(x0 + k * h * d) - f(x0 - k * h * d)) / (2 * k * h)
+    return (4.0 * c(1) - c(2)) / 3.0
+
+
+def test_gradient_components_within_1e6_relative_dense(sampler):
+    """Every gradient component above 1e-4 of the largest agrees with the
+    dense model's central difference to 1e-6 relative (dim 48, exact Krylov
+    space, the node count of the library's rule)."""
+    s = aniso_pair([2], [2, 3], seed=5, kS=1.3 / GAMMA_E * 50, kT=0.4 / GAMMA_E * 50)
+    B = np.array([0.11, -0.07, 0.2])
+    zk = W.random_phase_samples(s.Z, 3, seed=2)
+    t_end = 12 * DT
+    got = sampler.yield_gradient(s, B, zk, DT, t_end, m=48)
+    v0 = pack(s, B)
+    f = lambda v: dense_objective(s, v, zk, t_end, 1.0, 0.0)[0]
+    fd = np.array([richardson(f, v0, np.eye(v0.size)[i], 1e-4 * max(1.0, abs(v0[i]))) for i in range(v0.size)])
+    big = np.abs(fd) >= 1e-4 * np.max(np.abs(fd))
+    assert big.sum() >= 20
+    rel = np.abs(got.raw - fd)[big] / np.abs(fd)[big]
+    assert np.max(rel) <= 1e-6, (np.argmax(rel), np.max(rel))
+
+
+def test_full_size_gradient_components_within_1e6_relative(sampler):
+    """dim 55296: single gradient components (field, exchange, dipolar, rates
+    and hyperfine elements) above 1e-3 of the largest agree to 1e-6 relative
+    with Richardson central differences of the GPU's own stepwise yields."""
+    from spin_dynamics_gb300.torch_ops import pack_params, unpack_params
+    s, B = W.large_pair()
+    s.kS, s.kT = 20.0 / GAMMA_E, 20.0 / GAMMA_E
+    zk = W.random_phase_samples(s.Z, 2, seed=3)
+    t_end = 6 * DT
+    g = sampler.yield_gradient(s, B, zk, DT, t_end, m=30, checkpoint_every=2)
+    v0 = pack_params(s, B).numpy()
+
+    def f(v):
+        sv, Bv = unpack_params(s, v)
+        return sampler.stepwise_yields(sv, Bv, zk, DT, t_end, 30)[0]
+
+    idx = [0, 1, 2, 3, 4, 12, 13, 14, 15, 16, 19, 23, 15 + 9 * 7, 23 + 9 * 11]
+    scale = np.max(np.abs(g.raw))
+    checked = 0
+    for i in idx:
+        if abs(g.raw[i]) < 1e-3 * scale:
+            continue
+        fd = richardson(f, v0, np.eye(v0.size)[i], 1e-4 * max(abs(v0[i]), 1e-2))
+        assert abs(g.raw[i] - fd) <= 1e-6 * abs(fd), (i, g.raw[i], fd)
+        checked += 1
+    assert checked >= 6
+
+
 def test_torch_autograd_matches_adjoint(sampler):
     import torch
     from spin_dynamics_gb300.torch_ops import pack_params, yield_objective
@@ -253,7 +306,7 @@ def test_gradient_argument_and_capacity_errors(sampler):
     from spin_dynamics_gb300.spinsys import GAMMA_1H
     s = aniso_pair([2], [2], seed=1, kS=0.02, kT=0.01)
     zk = W.random_phase_samples(s.Z, 3, seed=1)
-    for kw in ({"m": 0}, {"m": 49}, {"n_quad": 0}, {"n_quad": 17}, {"checkpoint_every": -1}):
+    for kw in ({"m": 0}, {"m": 49}, {"n_quad": -1}, {"n_quad": 17}, {"checkpoint_every": -1}):
         args = dict(m=8, n_quad=4, checkpoint_every=0)
         args.update(kw)
         with pytest.raises(SpcError):
