@@ -376,11 +376,22 @@ def run_ours(args, rank, world, local_rank):
         zs = zk_host[:cpu_sample_size(args, sim, threads)]
         cpu = cpu_leg(args, sysp, B, sim, threads, zs)
         accuracy = accuracy_check(sampler, args.method, sysp, B, sim, zs, cpu_leg.last, threads)
-    batched = None if args.no_batch else batched_leg(args, sampler, local_rank)
-    adjoint = None if args.no_adjoint else adjoint_leg(args, sampler, value / world)
-    batch_adjoint = None if args.no_batch_adjoint else batched_adjoint_leg(args, sampler, local_rank)
-    symmetry = None if args.no_symmetry else symmetry_leg(args, sampler)
-    small = None if args.no_small else small_leg(args, sampler)
+    def leg(skip, fn, *a):
+        # a failing secondary leg is recorded in the line, not fatal to it
+        if skip:
+            return None
+        try:
+            return fn(*a)
+        except Exception as e:  # noqa: BLE001
+            import traceback
+            traceback.print_exc()
+            return {"error": f"{type(e).__name__}: {e}"}
+
+    batched = leg(args.no_batch, batched_leg, args, sampler, local_rank)
+    adjoint = leg(args.no_adjoint, adjoint_leg, args, sampler, value / world)
+    batch_adjoint = leg(args.no_batch_adjoint, batched_adjoint_leg, args, sampler, local_rank)
+    symmetry = leg(args.no_symmetry, symmetry_leg, args, sampler)
+    small = leg(args.no_small, small_leg, args, sampler)
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
     return dict(ms=ms, value=value, e2e=e2e, batched=batched, adjoint=adjoint, batch_adjoint=batch_adjoint,

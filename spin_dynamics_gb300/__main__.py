@@ -1,6 +1,6 @@
 """python -m spin_dynamics_gb300 input.ini — the Python twin of the `spinchem`
-executable (app/main.f90): read input.ini, loop over the fields, run the
-simulation type on the GPU library, write the output files."""
+executable (app/main.f90): read input.ini, run the simulation type for all
+the listed fields together on the GPU library, write the output files."""
 from __future__ import annotations
 
 import os
@@ -23,25 +23,23 @@ def main(argv=None) -> int:
         sampler = dynamics.TraceSampler(int(os.environ.get("SPINCHEM_DEVICE", "0")))
         if os.environ.get("SPINCHEM_KRYLOV"):
             sampler.set_krylov(os.environ["SPINCHEM_KRYLOV"])
+        folders = []
         for B in sim.B:
-            sys_.e1.w = -B  # app/main.f90:53-54
-            sys_.e2.w = -B
-            folder = os.path.join(sim.output_folder, field_folder_name(B))
-            os.makedirs(folder, exist_ok=True)
-            if sim.type == "trace_sampling":
-                dynamics.trace_sampling_para(sys_, sim, folder, sampler)
-            elif sim.type == "trace_sampling_serial":
-                dynamics.trace_sampling(sys_, sim, folder, sampler)
-            elif sim.type == "exact_dynamics":
-                dynamics.exact_dynamics(sys_, sim, folder, sampler)
-            elif sim.type == "symmetry_dynamics":
-                from . import symmetry
+            folders.append(os.path.join(sim.output_folder, field_folder_name(B)))
+            os.makedirs(folders[-1], exist_ok=True)
+        # every field of the list together (app/main.f90:48-79 loops them)
+        if sim.type in ("trace_sampling", "trace_sampling_serial", "exact_dynamics"):
+            dynamics.field_dynamics(sys_, sim, folders, sampler)
+        elif sim.type == "symmetry_dynamics":
+            from . import symmetry
+            for B in sim.B:
                 print(f" {B}")
-                symmetry.symmetrised_dynamics(sys_, sim, folder, sampler)
-            elif sim.type == "semi_classical":
+            symmetry.symmetrised_fields(sys_, sim, list(sim.B), folders, sampler)
+        elif sim.type == "semi_classical":
+            for _ in sim.B:
                 print(" method not yet implemented")
-            else:
-                raise SpinchemError("Error: Invalid simulation type entered.")
+        else:
+            raise SpinchemError("Error: Invalid simulation type entered.")
         sampler.close()
     except SpinchemError as e:
         print(str(e), file=sys.stderr)

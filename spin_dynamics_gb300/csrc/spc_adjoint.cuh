@@ -337,13 +337,27 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
   if (want_grad) {
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
-    const double held = (double)h->gck.bytes + h->gseg.bytes + h->gnu.bytes + h->Q.bytes + h->gmu.bytes +
-                        h->glam.bytes + h->P.bytes + h->xsum.bytes;
-    const double avail = 0.85 * ((double)free_b + held) - (double)(1 << 28);
+    const double avail = 0.85 * (double)free_b - (double)(1 << 28);
     const double sb = sizeof(double2) * (double)S;
+    // bytes of every state buffer of the sweep, and the device memory they
+    // take beyond what the handle already holds: a held buffer is reused up
+    // to the size asked of it (buffers only grow), so its excess over that
+    // size is no help
     auto need = [&](int k, bool keep) {
-      // + 0.5: the Re + Im plane of the current Krylov vector beside P
       return sb * ((double)m + 4.5 + (nsteps / k + 1) + k + 1.0 + (keep ? (double)k * nq : (double)nq));
+    };
+    auto extra = [&](int k, bool keep) {
+      double x = 0.0;
+      auto add = [&](const Handle::Buf& b, double bytes) { x += std::max(0.0, bytes - (double)b.bytes); };
+      add(h->Q, sb * m);
+      add(h->gmu, sb);
+      add(h->glam, 2.0 * sb);
+      add(h->P, sb);
+      add(h->xsum, 0.5 * sb);  // the Re + Im plane of the current Krylov vector beside P
+      add(h->gck, sb * (nsteps / k + 1));
+      add(h->gseg, sb * (k + 1));
+      add(h->gnu, sb * (keep ? (double)k * nq : (double)nq));
+      return x;
     };
     if (K == 0) {
       // among the spacings whose states fit, the one that recomputes the
@@ -351,7 +365,7 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
       // on a tie
       int64_t best = -1;
       for (int k = nsteps; k >= 1; --k) {
-        if (need(k, true) > avail) continue;
+        if (extra(k, true) > avail) continue;
         const int64_t recomputed = (int64_t)((nsteps - 1) / k) * k;
         if (best < 0 || recomputed < best) {
           best = recomputed;
@@ -363,9 +377,9 @@ int yield_gradient_run(Handle* h, const double* theta, const std::vector<GradJob
       else
         K = std::max(1, (int)std::lround(std::sqrt((double)nsteps)));
     } else {
-      cache = need(K, true) <= avail;
+      cache = extra(K, true) <= avail;
     }
-    if (!cache && need(K, false) > avail)
+    if (!cache && extra(K, false) > avail)
       return set_error(SPC_ERR_ALLOC,
                        "yield gradient needs %.1f GB of device memory at checkpoint spacing %d (%.1f GB free)",
                        need(K, false) / 1e9, K, free_b / 1e9);

@@ -1233,11 +1233,27 @@ int propagate_batch(Handle* h, const double* theta, const double* init_pop,
   {
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
+    // a held buffer is reused up to the size this call asks of it (buffers
+    // only grow), so only that much of it counts toward the budget
     double held = 0.0;
-    for (const Handle::Buf* b : {&h->Q, &h->P, &h->xsum, &h->coef, &h->rbeta, &h->Ahess, &h->Aexp, &h->proj,
-                                 &h->projpart, &h->cvec, &h->flag, &h->plan, &h->counters, &h->psi,
-                                 &h->obs, &h->tt, &h->kk, &h->done})
-      held += (double)b->bytes;
+    auto reuse = [&](const Handle::Buf& b, double bytes) { held += std::min((double)b.bytes, bytes); };
+    reuse(h->Q, 16.0 * (double)qcap);
+    reuse(h->P, 16.0 * (double)pcap);
+    reuse(h->xsum, 8.0 * (double)pcap);
+    reuse(h->psi, 16.0 * (double)psi_total);
+    reuse(h->obs, 8.0 * 4.0 * (double)T * G);
+    const double sl = (double)slots_cap;
+    reuse(h->coef, 16.0 * sl);
+    reuse(h->rbeta, 8.0 * sl);
+    reuse(h->Ahess, 16.0 * (double)mm * sl);
+    reuse(h->Aexp, 16.0 * (double)mm * sl);
+    reuse(h->proj, 64.0 * (double)mm * sl);
+    reuse(h->projpart, 16.0 * (double)nsplit_max * ncombo * sl);
+    reuse(h->cvec, 16.0 * m * sl);
+    reuse(h->flag, 4.0 * sl);
+    reuse(h->tt, 8.0 * G);
+    reuse(h->kk, 4.0 * G);
+    reuse(h->done, 4.0 * G);
     budget = (double)free_b + held - need_global - (512.0 * (1 << 20) + 0.02 * (double)total_b);
     if (h->mem_limit) budget = std::min(budget, (double)h->mem_limit - need_global);
   }

@@ -3,9 +3,10 @@
 //   spinchem input.ini
 //
 // reads the same input.ini keys with the same unit conversions and errors
-// (read_inp / check_inp / electron_init, src/spinsys.f90:60-235), loops over
-// the listed fields (app/main.f90:48-79), runs the selected simulation type
-// through libspinchem_gpu, and writes the same files into the same folders
+// (read_inp / check_inp / electron_init, src/spinsys.f90:60-235), runs the
+// selected simulation type for all the listed fields (app/main.f90:48-79)
+// together through libspinchem_gpu's batch calls, and writes the same files
+// into the same folders
 // (<output_folder>/<B in F0.3>/S_prob.data, Tp_prob.data, T0_prob.data,
 // Tm_prob.data; src/observables.f90:103-148). Where the reference stops with
 // a message, this prints the same message and exits with status 1.
@@ -249,30 +250,51 @@ struct Result {
   std::vector<double> PS, PT0, PTp, PTm;
 };
 
+int init_state_index(const Sim& sim) {
+  const int which = sim.init_state == "singlet" ? 0 : sim.init_state == "T0" ? 1 : sim.init_state == "Tp" ? 2
+                  : sim.init_state == "Tm" ? 3 : -1;
+  if (which < 0) stop("Error: Invalid initial radical pair state entered.");
+  return which;
+}
+
+// Consecutive groups of jobs whose vector entries (rows x samples padded to
+// tiles of 32) stay under a third of the device's free memory at m + 4
+// complex states per entry; a job larger than that is a group of its own.
+std::vector<std::vector<size_t>> batch_groups(const std::vector<double>& entries, int m) {
+  int64_t free_b = 0, total_b = 0;
+  check(spc_mem_info(0, &free_b, &total_b));
+  const double budget = std::max(1.0, (double)free_b / 3.0 / (16.0 * (m + 4)));
+  std::vector<std::vector<size_t>> out;
+  std::vector<size_t> cur;
+  double tot = 0.0;
+  for (size_t i = 0; i < entries.size(); ++i) {
+    if (!cur.empty() && tot + entries[i] > budget) {
+      out.push_back(cur);
+      cur.clear();
+      tot = 0.0;
+    }
+    cur.push_back(i);
+    tot += entries[i];
+  }
+  if (!cur.empty()) out.push_back(cur);
+  return out;
+}
+
+double padded(int M) { return (double)((M + 31) / 32 * 32); }
+
 // trace_sampling_para / trace_sampling / exact_dynamics (src/qm_dynamics.f90)
-Result run_dynamics(spc_handle* h, const Sys& sys, const Sim& sim, double B) {
+// for every field of the list (app/main.f90:48-79) in one batch: main
+// re-seeds the generator with sim%seed before each field (app/main.f90:50),
+// so every field propagates the same vectors. Each field's Hamiltonian
+// (getHiso_sp with w = -B) is one system of the batch store; groups of
+// fields bounded by device memory share one build and one propagation.
+std::vector<Result> run_fields(spc_handle* h, const Sys& sys, const Sim& sim) {
   if (!(sys.e1.isotropic() && sys.e2.isotropic()))
     stop("Anisotropic Hamiltoninans have not been implemented yet");
   std::vector<int> g1 = sys.e1.gI, g2 = sys.e2.gI;
-  spc_system s{};
-  s.n_nuc1 = (int)g1.size();
-  s.n_nuc2 = (int)g2.size();
-  s.mult1 = g1.data();
-  s.mult2 = g2.data();
-  s.A1 = sys.e1.A.data();
-  s.A2 = sys.e2.A.data();
-  s.B[2] = B;
-  s.J = sys.J;
-  std::memcpy(s.D, sys.D, sizeof(s.D));
-  s.kS = sys.kS;
-  s.kT = sys.kT;
-  check(spc_build_h(h, &s, SPC_H_REFERENCE));
   const long Z = sys.e1.Z() * sys.e2.Z();
-  int which = sim.init_state == "singlet" ? 0 : sim.init_state == "T0" ? 1 : sim.init_state == "Tp" ? 2
-            : sim.init_state == "Tm" ? 3 : -1;
-  if (which < 0) stop("Error: Invalid initial radical pair state entered.");
   double theta[8], pop[4];
-  check(spc_init_el_state(which, theta, pop));
+  check(spc_init_el_state(init_state_index(sim), theta, pop));
   std::vector<double> zk;
   int M;
   if (sim.type == "exact_dynamics") {
@@ -287,14 +309,43 @@ Result run_dynamics(spc_handle* h, const Sys& sys, const Sim& sim, double B) {
   }
   const int T = spc_num_time_points(sim.dt, sim.t_end);
   if (T < 1) stop("Error: Propagation timestep is missing");
-  Result r;
-  r.PS.resize(T);
-  r.PT0.resize(T);
-  r.PTp.resize(T);
-  r.PTm.resize(T);
-  check(spc_trace_sampling(h, theta, pop, zk.data(), M, sim.dt, sim.t_end, sim.N_krylov, sim.tol,
-                           r.PS.data(), r.PT0.data(), r.PTp.data(), r.PTm.data(), T));
-  return r;
+  const size_t nB = sim.B.size();
+  std::vector<Result> res(nB);
+  const std::vector<double> entries(nB, 4.0 * (double)Z * padded(M));
+  for (const std::vector<size_t>& grp : batch_groups(entries, sim.N_krylov)) {
+    std::vector<spc_system> systems(grp.size());
+    std::vector<double> zk_all;
+    for (size_t j = 0; j < grp.size(); ++j) {
+      spc_system& s = systems[j];
+      s = spc_system{};
+      s.n_nuc1 = (int)g1.size();
+      s.n_nuc2 = (int)g2.size();
+      s.mult1 = g1.data();
+      s.mult2 = g2.data();
+      s.A1 = sys.e1.A.data();
+      s.A2 = sys.e2.A.data();
+      s.B[2] = sim.B[grp[j]];
+      s.J = sys.J;
+      std::memcpy(s.D, sys.D, sizeof(s.D));
+      s.kS = sys.kS;
+      s.kT = sys.kT;
+      zk_all.insert(zk_all.end(), zk.begin(), zk.end());
+    }
+    check(spc_build_h_batch(h, (int)systems.size(), systems.data(), SPC_H_REFERENCE));
+    std::vector<int> Ms(grp.size(), M);
+    std::vector<double> out(grp.size() * 4 * (size_t)T);
+    check(spc_trace_sampling_batch(h, (int)grp.size(), nullptr, Ms.data(), theta, pop, zk_all.data(), sim.dt,
+                                   sim.t_end, sim.N_krylov, sim.tol, out.data(), T));
+    for (size_t j = 0; j < grp.size(); ++j) {
+      const double* o = &out[j * 4 * (size_t)T];
+      Result& r = res[grp[j]];
+      r.PS.assign(o, o + T);
+      r.PT0.assign(o + T, o + 2 * T);
+      r.PTp.assign(o + 2 * T, o + 3 * T);
+      r.PTm.assign(o + 3 * T, o + 4 * T);
+    }
+  }
+  return res;
 }
 
 // ---------------------------------------------------------------------------
@@ -599,36 +650,75 @@ std::vector<Block> blocks(const Sys& sys, int M1, int M2) {
   return out;
 }
 
-struct Observed {
-  std::vector<double> PS, PT0, PTp, PTm;
-};
+// One block's populations as trace_sampling_para writes them into its
+// folder (res%output(folder), src/qm_dynamics.f90:379-382), and read back.
+const char* kBlockFiles[4] = {"S_prob.data", "T0_prob.data", "Tp_prob.data", "Tm_prob.data"};
 
-// symmetrised_dynamics for one field: every block with weight >= block_tol
-// (from the restart block on) in one batched propagation, weighted sum in
-// block order, yields, output files.
-void symmetrised_dynamics(spc_handle* h, const Sys& sys, const Sim& sim, double B, const std::string& folder) {
+std::string block_folder(const std::string& field_folder, size_t i) {
+  return field_folder + "/hamiltonian_" + std::to_string(i + 1);
+}
+
+std::vector<double> read_data(const std::string& path, int T) {
+  std::ifstream f(path);
+  if (!f) stop("Error: restart: no saved block results in " + path);
+  std::vector<double> v;
+  std::string line;
+  while (std::getline(f, line))
+    if (!trim(line).empty()) v.push_back(std::strtod(line.c_str(), nullptr));
+  if ((int)v.size() != T)
+    stop("Error: restart: " + path + " holds " + std::to_string(v.size()) + " values, expected " +
+         std::to_string(T));
+  return v;
+}
+
+// symmetrised_dynamics (src/symmetry.f90:16-139) for every field of the list:
+// every (field, block) job with weight >= block_tol, from the restart block
+// on, in batches bounded by device memory. Each propagated block's
+// populations go to <field folder>/hamiltonian_<i>/ (the reference writes
+// them to <output_folder>/hamiltonian_<i>/, which every field overwrites);
+// blocks before the restart block are read back from there, so a run that
+// was stopped resumes where it left off (the reference leaves them
+// unallocated). Weighted sum in block order, yields, the seven files.
+void symmetrised_dynamics(spc_handle* h, const Sys& sys, const Sim& sim, const std::vector<std::string>& folders) {
   std::vector<Block> bl = blocks(sys, sim.M1, sim.M2);
   std::vector<uint64_t> seeds(std::max<size_t>(1, 2 * bl.size()));
   check(spc_rng_stream(sim.seed[0], sim.seed[1], (int)(2 * bl.size()), seeds.data()));
   const int start = sim.isRestart ? sim.restart : 1;
-  std::vector<size_t> sel;
+  std::vector<size_t> sel, run;  // blocks that count; of those, the ones to propagate
   for (size_t i = 0; i < bl.size(); ++i)
-    if ((int)i + 1 >= start && bl[i].w >= sim.block_tol) sel.push_back(i);
-  int which = sim.init_state == "singlet" ? 0 : sim.init_state == "T0" ? 1 : sim.init_state == "Tp" ? 2
-            : sim.init_state == "Tm" ? 3 : -1;
-  if (which < 0) stop("Error: Invalid initial radical pair state entered.");
+    if (bl[i].w >= sim.block_tol) {
+      sel.push_back(i);
+      if ((int)i + 1 >= start) run.push_back(i);
+    }
   double theta[8], pop[4];
-  check(spc_init_el_state(which, theta, pop));
+  check(spc_init_el_state(init_state_index(sim), theta, pop));
   const int T = spc_num_time_points(sim.dt, sim.t_end);
   if (T < 1) stop("Error: Propagation timestep is missing");
-  Observed res{std::vector<double>(T, 0.0), std::vector<double>(T, 0.0), std::vector<double>(T, 0.0),
-               std::vector<double>(T, 0.0)};
-  if (!sel.empty()) {
-    std::vector<spc_system> systems(sel.size());
-    std::vector<int> M(sel.size(), sim.N_samples);
-    std::vector<double> zk;
-    for (size_t j = 0; j < sel.size(); ++j) {
-      const Block& b = bl[sel[j]];
+  // the block vectors (the same for every field: seeds per block from sim%seed)
+  std::vector<std::vector<double>> zk(bl.size());
+  for (size_t i : run) {
+    zk[i].resize(2 * (size_t)bl[i].Z * sim.N_samples);
+    check(spc_seeded_samples((int64_t)seeds[2 * i], (int64_t)seeds[2 * i + 1], (int)bl[i].Z, sim.N_samples, 0,
+                             zk[i].data()));
+  }
+  // jobs block-major: a run stopped after some batches has finished every
+  // field of its first blocks, so restart = the first unfinished block
+  // resumes it
+  const size_t nB = sim.B.size();
+  std::vector<std::pair<size_t, size_t>> jobs;
+  std::vector<double> entries;
+  for (size_t i : run)
+    for (size_t k = 0; k < nB; ++k) {
+      jobs.push_back({k, i});
+      entries.push_back(4.0 * (double)bl[i].Z * padded(sim.N_samples));
+    }
+  std::map<std::pair<size_t, size_t>, std::vector<double>> out;  // (field, block) -> S|T0|Tp|Tm
+  for (const std::vector<size_t>& grp : batch_groups(entries, sim.N_krylov)) {
+    std::vector<spc_system> systems(grp.size());
+    std::vector<int> M(grp.size(), sim.N_samples);
+    std::vector<double> zk_all;
+    for (size_t j = 0; j < grp.size(); ++j) {
+      const Block& b = bl[jobs[grp[j]].second];
       spc_system& s = systems[j];
       s = spc_system{};
       s.n_nuc1 = (int)b.e1.gI.size();
@@ -639,42 +729,54 @@ void symmetrised_dynamics(spc_handle* h, const Sys& sys, const Sim& sim, double 
       s.A2 = b.e2.A.data();
       s.gamma1 = b.gam1.data();
       s.gamma2 = b.gam2.data();
-      s.B[2] = B;
+      s.B[2] = sim.B[jobs[grp[j]].first];
       s.J = sys.J;
       std::memcpy(s.D, sys.D, sizeof(s.D));
       s.kS = sys.kS;
       s.kT = sys.kT;
-      const size_t off = zk.size();
-      zk.resize(off + 2 * (size_t)b.Z * sim.N_samples);
-      const size_t i = sel[j];
-      check(spc_seeded_samples((int64_t)seeds[2 * i], (int64_t)seeds[2 * i + 1], (int)b.Z, sim.N_samples, 0,
-                               zk.data() + off));
+      const std::vector<double>& z = zk[jobs[grp[j]].second];
+      zk_all.insert(zk_all.end(), z.begin(), z.end());
     }
     check(spc_build_h_batch(h, (int)systems.size(), systems.data(), SPC_H_REFERENCE));
-    std::vector<double> out(sel.size() * 4 * (size_t)T);
-    check(spc_trace_sampling_batch(h, (int)sel.size(), nullptr, M.data(), theta, pop, zk.data(), sim.dt,
-                                   sim.t_end, sim.N_krylov, sim.tol, out.data(), T));
-    for (size_t j = 0; j < sel.size(); ++j) {
-      const double w = bl[sel[j]].w;
-      const double* o = &out[j * 4 * (size_t)T];
-      for (int t = 0; t < T; ++t) {  // res%scale(w) then res%update
-        res.PS[t] += o[t] * w;
-        res.PT0[t] += o[T + t] * w;
-        res.PTp[t] += o[2 * T + t] * w;
-        res.PTm[t] += o[3 * T + t] * w;
-      }
+    std::vector<double> o(grp.size() * 4 * (size_t)T);
+    check(spc_trace_sampling_batch(h, (int)grp.size(), nullptr, M.data(), theta, pop, zk_all.data(), sim.dt,
+                                   sim.t_end, sim.N_krylov, sim.tol, o.data(), T));
+    for (size_t j = 0; j < grp.size(); ++j) {  // block files as soon as the batch is done
+      const size_t k = jobs[grp[j]].first, i = jobs[grp[j]].second;
+      std::vector<double>& r = out[{k, i}];
+      r.assign(o.begin() + j * 4 * T, o.begin() + (j + 1) * 4 * T);
+      const std::string bf = block_folder(folders[k], i);
+      mkdir(bf.c_str(), 0755);
+      for (int c = 0; c < 4; ++c)
+        write_data(std::vector<double>(r.begin() + c * T, r.begin() + (c + 1) * T), bf, kBlockFiles[c]);
     }
   }
-  std::vector<double> phiS(T / 2), phiT(T / 2), iden(T);
-  check(spc_kinetics(T, res.PS.data(), res.PT0.data(), res.PTp.data(), res.PTm.data(), sim.dt, sys.kS, sys.kT,
-                     phiS.data(), phiT.data(), iden.data()));
-  write_data(res.PS, folder, "S_prob.data");
-  write_data(res.PTp, folder, "Tp_prob.data");
-  write_data(res.PT0, folder, "T0_prob.data");
-  write_data(res.PTm, folder, "Tm_prob.data");
-  write_data(iden, folder, "total_prob.data");
-  write_data(phiS, folder, "S_yield.data");
-  write_data(phiT, folder, "T_yield.data");
+  for (size_t k = 0; k < nB; ++k) {
+    std::printf(" %g\n", sim.B[k]);
+    std::vector<std::vector<double>> res(4, std::vector<double>(T, 0.0));  // S, T0, Tp, Tm
+    for (size_t i : sel) {
+      std::vector<std::vector<double>> P(4);
+      if ((int)i + 1 >= start) {
+        const std::vector<double>& o = out[{k, i}];
+        for (int c = 0; c < 4; ++c) P[c].assign(o.begin() + c * T, o.begin() + (c + 1) * T);
+      } else {
+        for (int c = 0; c < 4; ++c) P[c] = read_data(block_folder(folders[k], i) + "/" + kBlockFiles[c], T);
+      }
+      const double w = bl[i].w;
+      for (int c = 0; c < 4; ++c)  // res%scale(w) then res%update, block by block
+        for (int t = 0; t < T; ++t) res[c][t] += P[c][t] * w;
+    }
+    std::vector<double> phiS(T / 2), phiT(T / 2), iden(T);
+    check(spc_kinetics(T, res[0].data(), res[1].data(), res[2].data(), res[3].data(), sim.dt, sys.kS, sys.kT,
+                       phiS.data(), phiT.data(), iden.data()));
+    write_data(res[0], folders[k], "S_prob.data");
+    write_data(res[2], folders[k], "Tp_prob.data");
+    write_data(res[1], folders[k], "T0_prob.data");
+    write_data(res[3], folders[k], "Tm_prob.data");
+    write_data(iden, folders[k], "total_prob.data");
+    write_data(phiS, folders[k], "S_yield.data");
+    write_data(phiT, folders[k], "T_yield.data");
+  }
 }
 
 }  // namespace
@@ -695,24 +797,25 @@ int main(int argc, char** argv) {
     check(spc_set_krylov(h, std::strcmp(km, "lanczos") == 0 ? SPC_KRYLOV_LANCZOS
                             : std::strcmp(km, "auto") == 0  ? SPC_KRYLOV_AUTO
                                                             : SPC_KRYLOV_MGS));
+  std::vector<std::string> folders;
   for (double B : sim.B) {
-    const std::string folder = sim.output_folder + "/" + f0_3(B);
-    mkdir(folder.c_str(), 0755);
-    if (sim.type == "trace_sampling" || sim.type == "trace_sampling_serial" ||
-        sim.type == "exact_dynamics") {
-      Result r = run_dynamics(h, sys, sim, B);
-      write_data(r.PS, folder, "S_prob.data");
-      write_data(r.PTp, folder, "Tp_prob.data");
-      write_data(r.PT0, folder, "T0_prob.data");
-      write_data(r.PTm, folder, "Tm_prob.data");
-    } else if (sim.type == "symmetry_dynamics") {
-      std::printf(" %g\n", B);
-      symmetrised_dynamics(h, sys, sim, B, folder);
-    } else if (sim.type == "semi_classical") {
-      std::printf(" method not yet implemented\n");
-    } else {
-      stop("Error: Invalid simulation type entered.");
+    folders.push_back(sim.output_folder + "/" + f0_3(B));
+    mkdir(folders.back().c_str(), 0755);
+  }
+  if (sim.type == "trace_sampling" || sim.type == "trace_sampling_serial" || sim.type == "exact_dynamics") {
+    const std::vector<Result> rs = run_fields(h, sys, sim);
+    for (size_t k = 0; k < rs.size(); ++k) {
+      write_data(rs[k].PS, folders[k], "S_prob.data");
+      write_data(rs[k].PTp, folders[k], "Tp_prob.data");
+      write_data(rs[k].PT0, folders[k], "T0_prob.data");
+      write_data(rs[k].PTm, folders[k], "Tm_prob.data");
     }
+  } else if (sim.type == "symmetry_dynamics") {
+    symmetrised_dynamics(h, sys, sim, folders);
+  } else if (sim.type == "semi_classical") {
+    for (size_t k = 0; k < sim.B.size(); ++k) std::printf(" method not yet implemented\n");
+  } else {
+    stop("Error: Invalid simulation type entered.");
   }
   spc_destroy(h);
   const long secs =

@@ -526,6 +526,37 @@ def trace_sampling(sys: SysParam, sim: SimParam, out: Optional[str] = None,
     return res
 
 
+def field_dynamics(sys: SysParam, sim: SimParam, folders=None,
+                   sampler: Optional[TraceSampler] = None) -> list:
+    """The field loop of app/main.f90:48-79 for trace_sampling (parallel and
+    serial) and exact_dynamics, every field value of sim.B together: main
+    re-seeds the generator with sim.seed before each field (app/main.f90:50),
+    so every field propagates the same vectors. Each field's Hamiltonian
+    (getHiso_sp with w = -B) is one system of the batch store; groups of
+    fields bounded by device memory (a third of the free memory at m + 4
+    states per vector entry) share one build and one propagation. Writes
+    field k's files into folders[k] when given; returns one Observables per
+    field."""
+    _require_isotropic(sys)
+    sp = sampler or default_sampler()
+    if sim.type == "exact_dynamics":
+        zk = np.eye(sys.Z, dtype=np.complex128)
+    else:
+        zk = seeded_samples(sim.seed, sys.Z, sim.N_samples, serial=sim.type == "trace_sampling_serial")
+    free, _ = device_memory()
+    budget = max(1.0, free / 3.0 / (16.0 * (sim.N_krylov + 4)))
+    res = [None] * len(sim.B)
+    for grp in batch_groups([4 * sys.Z * padded_samples(zk.shape[0])] * len(sim.B), budget):
+        sp.build_h_batch([sys] * len(grp), [sim.B[k] for k in grp], "reference")
+        for k, r in zip(grp, sp.trace_sampling_batch([zk] * len(grp), sim.dt, sim.t_end, sim.N_krylov, sim.tol,
+                                                     sim.init_state)):
+            res[k] = r
+    if folders is not None:
+        for r, f in zip(res, folders):
+            r.output(f)
+    return res
+
+
 def exact_dynamics(sys: SysParam, sim: SimParam, out: Optional[str] = None,
                    sampler: Optional[TraceSampler] = None) -> Observables:
     """exact_dynamics (src/qm_dynamics.f90:24-137): the same propagator over

@@ -27,6 +27,7 @@ docstrings' source lines):
 from __future__ import annotations
 
 import math
+import os
 from itertools import product as _product
 from typing import Optional
 
@@ -234,18 +235,44 @@ def rng_stream(seed, n: int) -> np.ndarray:
     return out[:n]
 
 
-def _selected(sys_: SysParam, sim: SimParam):
-    """Blocks that run (weight >= sim.block_tol, from sim.restart on), with
-    their 1-based indices and per-block seeds drawn from sim.seed."""
+def _selected(sys_: SysParam, sim: SimParam, from_restart: bool = True):
+    """Blocks that count (weight >= sim.block_tol; from sim.restart on unless
+    from_restart is False), with their 1-based indices and per-block seeds
+    drawn from sim.seed."""
     bl = blocks(sys_, sim.M1, sim.M2)
     seeds = rng_stream(sim.seed, 2 * len(bl)).reshape(-1, 2) if bl else np.zeros((0, 2), np.uint64)
-    start = sim.restart if sim.isRestart else 1
+    start = sim.restart if sim.isRestart and from_restart else 1
     out = []
     for i, (w_k, sysb, Zb) in enumerate(bl, start=1):
         if i < start or w_k < sim.block_tol:
             continue
         out.append((i, w_k, sysb, Zb, (int(seeds[i - 1, 0]), int(seeds[i - 1, 1]))))
     return out
+
+
+BLOCK_FILES = (("S_prob.data", "P_S"), ("T0_prob.data", "P_T0"), ("Tp_prob.data", "P_Tp"),
+               ("Tm_prob.data", "P_Tm"))
+
+
+def block_folder(field_folder: str, i: int) -> str:
+    """Where block i (1-based) of a field keeps its populations."""
+    return os.path.join(field_folder, f"hamiltonian_{i}")
+
+
+def read_block(field_folder: str, i: int, T: int) -> Observables:
+    """A block's populations as its run wrote them (17 significant digits:
+    the same doubles)."""
+    arrs = {}
+    for name, key in BLOCK_FILES:
+        path = os.path.join(block_folder(field_folder, i), name)
+        if not os.path.exists(path):
+            raise SpinchemError(f"Error: restart: no saved block results in {path}")
+        with open(path) as f:
+            v = np.array([float(x) for x in f.read().split()], dtype=np.float64)
+        if v.size != T:
+            raise SpinchemError(f"Error: restart: {path} holds {v.size} values, expected {T}")
+        arrs[key] = v
+    return Observables(arrs["P_S"], arrs["P_T0"], arrs["P_Tp"], arrs["P_Tm"])
 
 
 def _block_vectors(sel, sim: SimParam, exact_blocks: bool):
@@ -265,38 +292,75 @@ def _budget_entries(states_per_entry: float) -> float:
 
 def symmetrised_dynamics(sys_: SysParam, sim: SimParam, out: Optional[str] = None, sampler=None,
                          exact_blocks: bool = False, field=None) -> Observables:
-    """symmetrised_dynamics (src/symmetry.f90:16-139): trace sampling over
-    every block whose weight reaches sim.block_tol (sim.N_samples vectors per
-    block, seeds drawn per block from sim.seed), each scaled by its weight,
-    summed in block order, then yields (get_kinetics) and the output files.
-    The blocks propagate together through the batch API (groups bounded by
-    device memory). With exact_blocks=True every block is traced exactly over
-    its basis states. field (a 3-vector, mT) switches to the general
-    Hamiltonian (anisotropic explicit nuclei, tilted field); by default the
-    reference's builder with the field -w along z."""
+    """symmetrised_dynamics (src/symmetry.f90:16-139) for one field: trace
+    sampling over every block whose weight reaches sim.block_tol
+    (sim.N_samples vectors per block, seeds drawn per block from sim.seed),
+    each scaled by its weight, summed in block order, then yields
+    (get_kinetics) and the output files. The blocks propagate together
+    through the batch API (groups bounded by device memory). With
+    exact_blocks=True every block is traced exactly over its basis states.
+    field (a 3-vector, mT) switches to the general Hamiltonian (anisotropic
+    explicit nuclei, tilted field); by default the reference's builder with
+    the field -w along z. With `out`, each propagated block's populations go
+    to out/hamiltonian_<i>/ and a restart reads the blocks before it from
+    there (symmetrised_fields)."""
+    if field is None:
+        return symmetrised_fields(sys_, sim, [-sys_.e1.w], [out] if out is not None else None, sampler,
+                                  exact_blocks)[0]
+    return symmetrised_fields(sys_, sim, [np.asarray(field, float)], [out] if out is not None else None,
+                              sampler, exact_blocks, mode="general")[0]
+
+
+def symmetrised_fields(sys_: SysParam, sim: SimParam, fields, folders=None, sampler=None,
+                       exact_blocks: bool = False, mode: str = "reference") -> list:
+    """symmetrised_dynamics for every field of `fields` (scalars along z for
+    the reference builder, 3-vectors for mode="general"): all (block, field)
+    jobs from the restart block on, block-major, in batches bounded by device
+    memory. With folders, block i's populations of field k go to
+    folders[k]/hamiltonian_<i>/ (the reference writes them to
+    <output_folder>/hamiltonian_<i>/, which every field overwrites), and the
+    blocks before sim.restart are read back from there instead of being left
+    unset: a stopped run resumes where it left off and writes the same files
+    as an uninterrupted one. Returns one Observables per field (with yields);
+    writes each field's seven files into folders[k]."""
     from . import dynamics
     from .dynamics import batch_groups, padded_samples
     sp = sampler or dynamics.default_sampler()
-    sel = _selected(sys_, sim)
-    zks = _block_vectors(sel, sim, exact_blocks)
+    sel = _selected(sys_, sim, from_restart=False)
+    start = sim.restart if sim.isRestart else 1
+    if start > 1 and folders is None:
+        raise SpinchemError("Error: restart needs the output folders that hold the earlier blocks")
+    run = [b for b in sel if b[0] >= start]
+    zks = _block_vectors(run, sim, exact_blocks)
     T = dynamics.num_time_points(sim.dt, sim.t_end)
-    res = Observables.zeros(T)
-    sizes = [4 * Zb * padded_samples(z.shape[0]) for (_, _, _, Zb, _), z in zip(sel, zks)]
+    # block-major: a run stopped after some batches has finished every field
+    # of its first blocks, so restart = the first unfinished block resumes it
+    jobs = [(k, r) for r in range(len(run)) for k in range(len(fields))]
+    sizes = [4 * run[r][3] * padded_samples(zks[r].shape[0]) for _, r in jobs]
+    got = {}
     for grp in batch_groups(sizes, _budget_entries(sim.N_krylov + 4)):
-        systems = [sel[j][2] for j in grp]
-        if field is None:
-            sp.build_h_batch(systems, [-s.e1.w for s in systems], "reference")
-        else:
-            sp.build_h_batch(systems, [np.asarray(field, float)] * len(systems), "general")
-        rs = sp.trace_sampling_batch([zks[j] for j in grp], sim.dt, sim.t_end, sim.N_krylov, sim.tol,
+        sp.build_h_batch([run[jobs[q][1]][2] for q in grp], [fields[jobs[q][0]] for q in grp], mode)
+        rs = sp.trace_sampling_batch([zks[jobs[q][1]] for q in grp], sim.dt, sim.t_end, sim.N_krylov, sim.tol,
                                      sim.init_state)
-        for j, r in zip(grp, rs):
-            r.scale(sel[j][1])
+        for q, r in zip(grp, rs):
+            k, i = jobs[q][0], run[jobs[q][1]][0]
+            got[(k, i)] = r
+            if folders is not None:  # as soon as the batch is done
+                bf = block_folder(folders[k], i)
+                os.makedirs(bf, exist_ok=True)
+                r.output(bf)
+    out = []
+    for k in range(len(fields)):
+        res = Observables.zeros(T)
+        for i, w_k, _, _, _ in sel:
+            r = got[(k, i)] if i >= start else read_block(folders[k], i, T)
+            r.scale(w_k)
             res.update(r)
-    res.get_kinetics(sim.dt, sys_.kS, sys_.kT)
-    if out is not None:
-        res.output(out)
-    return res
+        res.get_kinetics(sim.dt, sys_.kS, sys_.kT)
+        if folders is not None:
+            res.output(folders[k])
+        out.append(res)
+    return out
 
 
 def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, directions=None,
@@ -320,7 +384,7 @@ def symmetrised_yield_gradient(sys_: SysParam, sim: SimParam, B, sampler=None, d
         fields = [B]
     else:
         fields = [np.linalg.norm(B) * np.asarray(d, float) / np.linalg.norm(d) for d in directions]
-    sel = _selected(sys_, sim)
+    sel = _selected(sys_, sim, from_restart=False)
     zks = _block_vectors(sel, sim, exact_blocks)
     jobs = [(f, j) for f in range(len(fields)) for j in range(len(sel))]
     acc = [dict(Phi_S=0.0, Phi_T=0.0, B=np.zeros(3), J=0.0, D=np.zeros((3, 3)), kS=0.0, kT=0.0)

@@ -161,10 +161,13 @@ def test_symmetry_dynamics_in_both_drivers(tmp_path, case):
         r = subprocess.run(cmd + [str(ini)], capture_output=True, text=True, cwd=ROOT)
         assert r.returncode == 0, r.stderr
         outs.append(out / ".100")
-    files = sorted(os.listdir(outs[0]))
-    assert files == sorted(os.listdir(outs[1])) == sorted(
+    files = sorted(f for f in os.listdir(outs[0]) if os.path.isfile(outs[0] / f))
+    assert files == sorted(f for f in os.listdir(outs[1]) if os.path.isfile(outs[1] / f)) == sorted(
         ["S_prob.data", "T0_prob.data", "Tm_prob.data", "Tp_prob.data", "total_prob.data", "S_yield.data",
          "T_yield.data"])
+    # every block's populations beside them, for a restart
+    assert sorted(d for d in os.listdir(outs[0]) if d.startswith("hamiltonian_")) == [
+        f"hamiltonian_{i}" for i in range(1, 5)]
     for f in files:
         if case == "exact_groups":
             assert (outs[0] / f).read_text() == (outs[1] / f).read_text(), f
@@ -172,3 +175,40 @@ def test_symmetry_dynamics_in_both_drivers(tmp_path, case):
             assert np.max(np.abs(np.loadtxt(outs[0] / f) - np.loadtxt(outs[1] / f))) <= 1e-12, f
     ps = np.loadtxt(outs[0] / "S_prob.data")
     assert abs(ps[0] - 1.0) < 1e-12  # the block weights sum to one
+
+
+def test_symmetry_restart_reloads_the_saved_blocks(tmp_path):
+    """Two fields; the first run keeps every block's populations under
+    <field>/hamiltonian_<i>/. A second run given only blocks 1-2 of it and
+    restart = 3 propagates blocks 3-4 and reads 1-2 back: its files equal the
+    full run's (to the rounding of a batch of another composition), and the
+    two drivers' resumed files are byte-identical."""
+    import shutil
+    ini_txt = SYM_INI.replace("B = 0.1", "B = 0.1 0.3")
+    full = tmp_path / "full"
+    full.mkdir()
+    (tmp_path / "full.ini").write_text(ini_txt.format(a3="0.5", out=full))
+    exe = os.path.join(ROOT, "spin_dynamics_gb300", "_build", "spinchem")
+    r = subprocess.run([exe, str(tmp_path / "full.ini")], capture_output=True, text=True, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    resumed = []
+    for name, cmd in (("cpp", [exe]), ("py", [sys.executable, "-m", "spin_dynamics_gb300"])):
+        out = tmp_path / name
+        for fld in (".100", ".300"):
+            for i in (1, 2):
+                shutil.copytree(full / fld / f"hamiltonian_{i}", out / fld / f"hamiltonian_{i}")
+        (tmp_path / f"{name}.ini").write_text(ini_txt.format(a3="0.5", out=out) + "restart = 3\n")
+        r = subprocess.run(cmd + [str(tmp_path / f"{name}.ini")], capture_output=True, text=True, cwd=ROOT)
+        assert r.returncode == 0, r.stderr
+        resumed.append(out)
+    for fld in (".100", ".300"):
+        for f in ("S_prob.data", "T0_prob.data", "Tp_prob.data", "Tm_prob.data", "S_yield.data"):
+            a = np.loadtxt(full / fld / f)
+            assert np.max(np.abs(np.loadtxt(resumed[0] / fld / f) - a)) <= 1e-13, (fld, f)
+            assert (resumed[0] / fld / f).read_text() == (resumed[1] / fld / f).read_text(), (fld, f)
+    # without the saved blocks the restart is refused
+    bare = tmp_path / "bare"
+    bare.mkdir()
+    (tmp_path / "bare.ini").write_text(ini_txt.format(a3="0.5", out=bare) + "restart = 3\n")
+    r = subprocess.run([exe, str(tmp_path / "bare.ini")], capture_output=True, text=True, cwd=ROOT)
+    assert r.returncode == 1 and "restart" in r.stderr
