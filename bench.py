@@ -376,22 +376,36 @@ def run_ours(args, rank, world, local_rank):
         zs = zk_host[:cpu_sample_size(args, sim, threads)]
         cpu = cpu_leg(args, sysp, B, sim, threads, zs)
         accuracy = accuracy_check(sampler, args.method, sysp, B, sim, zs, cpu_leg.last, threads)
+    # each secondary leg runs on a handle of its own, released afterwards:
+    # buffers a handle holds from an earlier leg would otherwise count against
+    # the device memory a later call sizes itself by (checkpoint spacing and
+    # node-state caching of the gradient, batch groups)
+    sampler.close()
+    torch.cuda.empty_cache()
+
     def leg(skip, fn, *a):
         # a failing secondary leg is recorded in the line, not fatal to it
         if skip:
             return None
+        s = TraceSampler(local_rank)
+        s.set_krylov(args.method)
+        s.set_stream(stream.cuda_stream)
         try:
-            return fn(*a)
+            return fn(args, s, *a)
         except Exception as e:  # noqa: BLE001
             import traceback
             traceback.print_exc()
             return {"error": f"{type(e).__name__}: {e}"}
+        finally:
+            torch.cuda.synchronize()
+            s.close()
+            torch.cuda.empty_cache()
 
-    batched = leg(args.no_batch, batched_leg, args, sampler, local_rank)
-    adjoint = leg(args.no_adjoint, adjoint_leg, args, sampler, value / world)
-    batch_adjoint = leg(args.no_batch_adjoint, batched_adjoint_leg, args, sampler, local_rank)
-    symmetry = leg(args.no_symmetry, symmetry_leg, args, sampler)
-    small = leg(args.no_small, small_leg, args, sampler)
+    batched = leg(args.no_batch, batched_leg, local_rank)
+    adjoint = leg(args.no_adjoint, adjoint_leg, value / world)
+    batch_adjoint = leg(args.no_batch_adjoint, batched_adjoint_leg, local_rank)
+    symmetry = leg(args.no_symmetry, symmetry_leg)
+    small = leg(args.no_small, small_leg)
     fp64 = C.c_double()
     nat.check(nat.lib().spc_fp64_peak(local_rank, C.byref(fp64)))
     return dict(ms=ms, value=value, e2e=e2e, batched=batched, adjoint=adjoint, batch_adjoint=batch_adjoint,

@@ -430,6 +430,40 @@ __device__ void smem_matmul(int m, const double2* A, const double2* B, double2* 
   }
 }
 
+// C = A B for A with lower/upper bandwidths (la, ua) (A_ik = 0 when i - k > la
+// or k - i > ua) and B with (lb, ub): only the k where both factors can be
+// nonzero, in smem_matmul's even/odd partial sums and order. The skipped
+// terms are exact zeros, so every element rounds as the full product does
+// (finite inputs; at most the sign of a zero entry differs).
+__device__ void smem_matmul_band(int m, const double2* A, int la, int ua, const double2* B, int lb, int ub,
+                                 double2* C, int tid, int nt) {
+  const int mm = m * m;
+  for (int idx = tid; idx < mm; idx += nt) {
+    const int i = idx % m, j = idx / m;
+    const int k1 = min(min(i + ua, j + lb), m - 1);
+    int k = max(max(i - la, j - ub), 0);
+    double2 a0 = cz(), a1 = cz();
+    if (k <= k1 && (k & 1)) {
+      a1 = cfma(A[i + k * m], B[k + j * m], a1);
+      ++k;
+    }
+    for (; k + 1 <= k1; k += 2) {
+      a0 = cfma(A[i + k * m], B[k + j * m], a0);
+      a1 = cfma(A[i + (k + 1) * m], B[(k + 1) + j * m], a1);
+    }
+    if (k <= k1) a0 = cfma(A[i + k * m], B[k + j * m], a0);
+    C[idx] = cadd(a0, a1);
+  }
+}
+
+// Padé(6,6) with scaling and squaring, evaluated on the bands of the input:
+// a Lanczos basis gives a tridiagonal matrix, MGS an upper Hessenberg one.
+// The powers, the Padé sums, the LU factors (while partial pivoting keeps
+// the diagonal, which the denominator's diagonal dominance at the scaled
+// norm < 1/2 makes the rule) and the triangular solves then only touch their
+// bands; each element is computed by the same operations in the same order
+// as the dense evaluation, so the result has the same bits. A pivot off the
+// diagonal restarts the factorisation dense.
 template <bool WARP>
 __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double2* __restrict__ out, double dt,
                          double2* sm, double* rowsum, int* piv, int* s_sh, int* p_sh, int tid, int nt,
@@ -440,16 +474,34 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
   double2* E = X + mm;
   double2* D = E + mm;
   double2* T = D + mm;
-  // (0,-1)*dt*A
-  for (int i = tid; i < mm; i += nt) {
-    double2 a = Ain[(i % m) + (size_t)(i / m) * mld];
-    A2[i] = make_double2(dt * a.y, -dt * a.x);
+  // (0,-1)*dt*A and its bandwidths (held in piv[0], piv[1] until the LU)
+  if (tid == 0) piv[0] = piv[1] = 0;
+  expm_sync<WARP>();
+  {
+    int bl = 0, bu = 0;
+    for (int i = tid; i < mm; i += nt) {
+      const double2 a = Ain[(i % m) + (size_t)(i / m) * mld];
+      const double2 v = make_double2(dt * a.y, -dt * a.x);
+      A2[i] = v;
+      if (v.x != 0.0 || v.y != 0.0) {
+        bl = max(bl, i % m - i / m);
+        bu = max(bu, i / m - i % m);
+      }
+    }
+    if (bl) atomicMax(&piv[0], bl);
+    if (bu) atomicMax(&piv[1], bu);
   }
   expm_sync<WARP>();
-  // L-infinity norm (mat_norm_linf :89-104)
+  const int l1 = piv[0], u1 = piv[1];
+  const int l2 = min(2 * l1, m - 1), u2 = min(2 * u1, m - 1);
+  const int l4 = min(2 * l2, m - 1), u4 = min(2 * u2, m - 1);
+  const int l6 = min(l4 + l2, m - 1), u6 = min(u4 + u2, m - 1);
+  const int lN = max(l6, min(l1 + l4, m - 1)), uN = max(u6, min(u1 + u4, m - 1));
+  // L-infinity norm (mat_norm_linf :89-104): the row's band in column order
+  // (the entries outside add exact zeros)
   for (int i = tid; i < m; i += nt) {
     double s = 0.0;
-    for (int j = 0; j < m; ++j) s += hypot(A2[i + j * m].x, A2[i + j * m].y);
+    for (int j = max(0, i - l1); j <= min(m - 1, i + u1); ++j) s += hypot(A2[i + j * m].x, A2[i + j * m].y);
     rowsum[i] = s;
   }
   expm_sync<WARP>();
@@ -478,11 +530,11 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
   ck[0] = 1.0;
   ck[1] = 0.5;
   for (int k = 2; k <= q; ++k) ck[k] = ck[k - 1] * (double)(q - k + 1) / (double)(k * (2 * q - k + 1));
-  smem_matmul(m, A2, A2, X, tid, nt);  // a^2
+  smem_matmul_band(m, A2, l1, u1, A2, l1, u1, X, tid, nt);  // a^2
   expm_sync<WARP>();
-  smem_matmul(m, X, X, T, tid, nt);    // a^4
+  smem_matmul_band(m, X, l2, u2, X, l2, u2, T, tid, nt);    // a^4
   expm_sync<WARP>();
-  smem_matmul(m, T, X, D, tid, nt);    // a^6
+  smem_matmul_band(m, T, l4, u4, X, l2, u2, D, tid, nt);    // a^6
   expm_sync<WARP>();
   for (int i = tid; i < mm; i += nt) {
     const double id = (i % (m + 1) == 0) ? 1.0 : 0.0;
@@ -491,16 +543,68 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
     D[i] = make_double2(id * ck[1] + ck[3] * x2.x + ck[5] * x4.x, ck[3] * x2.y + ck[5] * x4.y);
   }
   expm_sync<WARP>();
-  smem_matmul(m, A2, D, X, tid, nt);   // odd part
+  smem_matmul_band(m, A2, l1, u1, D, l4, u4, X, tid, nt);   // odd part
   expm_sync<WARP>();
   for (int i = tid; i < mm; i += nt) {
     const double2 ev = E[i], od = X[i];
     T[i] = cadd(ev, od);  // N
     D[i] = csub(ev, od);  // D
+    X[i] = D[i];          // kept for a dense restart of the LU
   }
   expm_sync<WARP>();
-  // LU of D with partial pivoting (|re|+|im| pivot, as izamax), in place
+  // LU of D with partial pivoting (|re|+|im| pivot, as izamax), in place, on
+  // the bands (lN, uN) while every pivot is the diagonal: then no row moves,
+  // the unit-lower factor keeps bandwidth lN and the upper one uN
+  bool swapped = false;
   for (int k = 0; k < m; ++k) {
+    const int ie = min(k + lN, m - 1);
+    if (tid < 32) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + tid; i <= ie; i += 32) {
+        const double v = fabs(D[i + k * m].x) + fabs(D[i + k * m].y);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (tid == 0) {
+        *p_sh = bi;
+        piv[k] = bi;
+        if (best == 0.0) atomicExch(err, 2);
+      }
+    }
+    expm_sync<WARP>();
+    if (*p_sh != k) {  // a row swap: the bands no longer hold
+      swapped = true;
+      break;
+    }
+    const double2 dkk = D[k + k * m];
+    for (int i = k + 1 + tid; i <= ie; i += nt) D[i + k * m] = cdiv(D[i + k * m], dkk);
+    expm_sync<WARP>();
+    const int ri = ie - k, rj = min(k + uN, m - 1) - k;
+    for (int idx = tid; idx < ri * rj; idx += nt) {
+      const int i = k + 1 + idx % ri, j = k + 1 + idx / ri;
+      D[i + j * m] = cfms(D[i + k * m], D[k + j * m], D[i + j * m]);
+    }
+    expm_sync<WARP>();
+  }
+  if (swapped) {
+    // dense restart from the saved denominator
+    for (int i = tid; i < mm; i += nt) D[i] = X[i];
+    expm_sync<WARP>();
+  }
+  const int lL = swapped ? m - 1 : lN, uU = swapped ? m - 1 : uN;
+  for (int k = 0; swapped && k < m; ++k) {
     if (tid < 32) {
       double best = -1.0;
       int bi = k;
@@ -560,8 +664,9 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
   expm_sync<WARP>();
   for (int idx = tid; idx < mm; idx += nt) E[idx] = T[perm[idx % m] + (idx / m) * m];
   expm_sync<WARP>();
+  // (the factors' entries outside their bands are exact zeros)
   for (int k = 0; k + 1 < m; ++k) {
-    const int rem = m - k - 1;
+    const int rem = min(lL, m - k - 1);
     for (int idx = tid; idx < rem * m; idx += nt) {
       const int i = k + 1 + idx % rem, j = idx / rem;
       E[i + j * m] = cfms(D[i + k * m], E[k + j * m], E[i + j * m]);
@@ -571,8 +676,9 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
   for (int k = m - 1; k >= 0; --k) {
     for (int j = tid; j < m; j += nt) E[k + j * m] = cdiv(E[k + j * m], D[k + k * m]);
     expm_sync<WARP>();
-    for (int idx = tid; idx < k * m; idx += nt) {
-      const int i = idx % k, j = idx / k;
+    const int i0 = max(0, k - uU), ri = k - i0;
+    for (int idx = tid; idx < ri * m; idx += nt) {
+      const int i = i0 + idx % ri, j = idx / ri;
       E[i + j * m] = cfms(D[i + k * m], E[k + j * m], E[i + j * m]);
     }
     expm_sync<WARP>();
