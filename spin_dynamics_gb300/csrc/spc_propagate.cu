@@ -456,14 +456,32 @@ __device__ void smem_matmul_band(int m, const double2* A, int la, int ua, const 
   }
 }
 
+// Padé(6,6) coefficient c_k by the reference's recurrence (:54-77),
+// c_0 = 1, c_1 = 1/2, c_k = c_{k-1} (q - k + 1) / (k (2q - k + 1)), folded at
+// compile time with the same IEEE double operations.
+constexpr double pade6_coef(int k) {
+  double c = 1.0;
+  for (int j = 1; j <= k; ++j) c = j == 1 ? 0.5 : c * (double)(6 - j + 1) / (double)(j * (2 * 6 - j + 1));
+  return c;
+}
+
+// Complex reciprocal 1/d = conj(d) / |d|^2, for the band path's pivots (the
+// diagonal of a diagonally dominant denominator, |d| of order one).
+__device__ __forceinline__ double2 crcp(double2 d) {
+  const double s = 1.0 / fma(d.x, d.x, d.y * d.y);
+  return make_double2(d.x * s, -d.y * s);
+}
+
 // Padé(6,6) with scaling and squaring, evaluated on the bands of the input:
 // a Lanczos basis gives a tridiagonal matrix, MGS an upper Hessenberg one.
-// The powers, the Padé sums, the LU factors (while partial pivoting keeps
-// the diagonal, which the denominator's diagonal dominance at the scaled
-// norm < 1/2 makes the rule) and the triangular solves then only touch their
-// bands; each element is computed by the same operations in the same order
-// as the dense evaluation, so the result has the same bits. A pivot off the
-// diagonal restarts the factorisation dense.
+// The powers and the Padé sums (each element by the dense evaluation's
+// operations in its order: the skipped terms are exact zeros), the LU
+// factors (while partial pivoting keeps the diagonal, which the
+// denominator's diagonal dominance at the scaled norm < 1/2 makes the rule)
+// and the triangular solves then only touch their bands. On that path the
+// multipliers and the upper solve use the pivots' reciprocals: a complex
+// division is three IEEE divides on the serial path of every step. A pivot
+// off the diagonal restarts the factorisation dense with Smith's division.
 template <bool WARP>
 __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double2* __restrict__ out, double dt,
                          double2* sm, double* rowsum, int* piv, int* s_sh, int* p_sh, int tid, int nt,
@@ -525,11 +543,8 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
   // with the reference's coefficient recurrence (:54-77), evaluated from the
   // even and odd parts (Paterson-Stockmeyer): a^2, a^4, a^6 and
   // a (c1 + c3 a^2 + c5 a^4), four products instead of five
-  const int q = 6;
-  double ck[q + 1];
-  ck[0] = 1.0;
-  ck[1] = 0.5;
-  for (int k = 2; k <= q; ++k) ck[k] = ck[k - 1] * (double)(q - k + 1) / (double)(k * (2 * q - k + 1));
+  constexpr double ck[7] = {pade6_coef(0), pade6_coef(1), pade6_coef(2), pade6_coef(3),
+                            pade6_coef(4), pade6_coef(5), pade6_coef(6)};
   smem_matmul_band(m, A2, l1, u1, A2, l1, u1, X, tid, nt);  // a^2
   expm_sync<WARP>();
   smem_matmul_band(m, X, l2, u2, X, l2, u2, T, tid, nt);    // a^4
@@ -554,15 +569,18 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
   expm_sync<WARP>();
   // LU of D with partial pivoting (|re|+|im| pivot, as izamax), in place, on
   // the bands (lN, uN) while every pivot is the diagonal: then no row moves,
-  // the unit-lower factor keeps bandwidth lN and the upper one uN
+  // the unit-lower factor keeps bandwidth lN and the upper one uN. The
+  // multipliers l_ik = D_ik / D_kk (formed with the pivot's reciprocal in the
+  // same pass as the trailing update) go to the spent A2.
   bool swapped = false;
   for (int k = 0; k < m; ++k) {
-    const int ie = min(k + lN, m - 1);
+    const int ie = min(k + lN, m - 1), je = min(k + uN, m - 1);
     if (tid < 32) {
-      double best = -1.0;
+      // non-negative doubles order as their bit patterns: integer compares
+      long long best = -1;
       int bi = k;
       for (int i = k + tid; i <= ie; i += 32) {
-        const double v = fabs(D[i + k * m].x) + fabs(D[i + k * m].y);
+        const long long v = __double_as_longlong(fabs(D[i + k * m].x) + fabs(D[i + k * m].y));
         if (v > best) {
           best = v;
           bi = i;
@@ -570,7 +588,7 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
         const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
         if (ob > best || (ob == best && oi < bi)) {
           best = ob;
@@ -580,7 +598,7 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
       if (tid == 0) {
         *p_sh = bi;
         piv[k] = bi;
-        if (best == 0.0) atomicExch(err, 2);
+        if (best == 0) atomicExch(err, 2);
       }
     }
     expm_sync<WARP>();
@@ -588,13 +606,14 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
       swapped = true;
       break;
     }
-    const double2 dkk = D[k + k * m];
-    for (int i = k + 1 + tid; i <= ie; i += nt) D[i + k * m] = cdiv(D[i + k * m], dkk);
-    expm_sync<WARP>();
-    const int ri = ie - k, rj = min(k + uN, m - 1) - k;
+    const int ri = ie - k, rj = je - k + 1;  // rows k+1..ie, columns k..je
     for (int idx = tid; idx < ri * rj; idx += nt) {
-      const int i = k + 1 + idx % ri, j = k + 1 + idx / ri;
-      D[i + j * m] = cfms(D[i + k * m], D[k + j * m], D[i + j * m]);
+      const int i = k + 1 + idx % ri, j = k + idx / ri;
+      const double2 l = cmul(D[i + k * m], crcp(D[k + k * m]));
+      if (j == k)
+        A2[i + k * m] = l;
+      else
+        D[i + j * m] = cfms(l, D[k + j * m], D[i + j * m]);
     }
     expm_sync<WARP>();
   }
@@ -664,17 +683,27 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
   expm_sync<WARP>();
   for (int idx = tid; idx < mm; idx += nt) E[idx] = T[perm[idx % m] + (idx / m) * m];
   expm_sync<WARP>();
-  // (the factors' entries outside their bands are exact zeros)
+  // (the factors' entries outside their bands are exact zeros; the band
+  // path's multipliers are in A2, whose diagonal then takes the pivots'
+  // reciprocals for the upper solve)
+  const double2* Lf = swapped ? D : A2;
   for (int k = 0; k + 1 < m; ++k) {
     const int rem = min(lL, m - k - 1);
     for (int idx = tid; idx < rem * m; idx += nt) {
       const int i = k + 1 + idx % rem, j = idx / rem;
-      E[i + j * m] = cfms(D[i + k * m], E[k + j * m], E[i + j * m]);
+      E[i + j * m] = cfms(Lf[i + k * m], E[k + j * m], E[i + j * m]);
     }
     expm_sync<WARP>();
   }
+  if (!swapped) {
+    for (int k = tid; k < m; k += nt) A2[k + k * m] = crcp(D[k + k * m]);
+    expm_sync<WARP>();
+  }
   for (int k = m - 1; k >= 0; --k) {
-    for (int j = tid; j < m; j += nt) E[k + j * m] = cdiv(E[k + j * m], D[k + k * m]);
+    if (swapped)
+      for (int j = tid; j < m; j += nt) E[k + j * m] = cdiv(E[k + j * m], D[k + k * m]);
+    else
+      for (int j = tid; j < m; j += nt) E[k + j * m] = cmul(E[k + j * m], A2[k + k * m]);
     expm_sync<WARP>();
     const int i0 = max(0, k - uU), ri = k - i0;
     for (int idx = tid; idx < ri * m; idx += nt) {

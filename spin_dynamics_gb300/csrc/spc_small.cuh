@@ -26,6 +26,7 @@
 #define SMALL_VS 17      // staging row stride (padded: rows of one chunk start in different banks)
 #define SMALL_MAXC 9     // projector combinations per thread: 4 * 32 * 33 / 2 <= 9 * 256
 #define SMALL_MAX_M 32
+#define SMALL_ROUNDS 5   // dt-loop pair rounds over 128 threads: 32 * 33 / 2 <= 5 * 128
 #define SMALL_NMAX 2048
 
 struct SmallJob {
@@ -47,6 +48,10 @@ __device__ __forceinline__ double2 warp_sum2(double2 v) {
   return v;
 }
 
+// Barrier of warps 0-3 (the dt loop's warps; the others wait at the next
+// __syncthreads).
+__device__ __forceinline__ void small_bar4() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
 // Sum over the CTA: warp trees, then warp 0 sums the warps' partials with the
 // same tree; every thread gets the total (red holds SMALL_WARPS + 1). Only
 // warp 0 spends FP64 adds on the second level. Called by all threads.
@@ -61,6 +66,35 @@ __device__ __forceinline__ double2 block_sum2(double2 v, double2* red) {
   }
   __syncthreads();
   return red[SMALL_WARPS];
+}
+
+// Real sum over the CTA: warp trees (5 adds), then warp 0 adds the 8 warp
+// sums in three shuffle levels. With norm, lane 0 of warp 0 also takes the
+// square root and its reciprocal (0 for a zero norm) once for the CTA:
+// every thread gets {sum or sqrt, reciprocal} (red holds SMALL_WARPS + 2).
+// Called by all threads.
+template <bool NORM>
+__device__ __forceinline__ double2 block_sum1(double v, double* red) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double x = threadIdx.x < SMALL_WARPS ? red[threadIdx.x] : 0.0;
+    x += __shfl_xor_sync(0xffffffffu, x, 4);
+    x += __shfl_xor_sync(0xffffffffu, x, 2);
+    x += __shfl_xor_sync(0xffffffffu, x, 1);
+    if (threadIdx.x == 0) {
+      if (NORM) {
+        const double b = sqrt(x);
+        red[SMALL_WARPS] = b;
+        red[SMALL_WARPS + 1] = b > 0.0 ? 1.0 / b : 0.0;
+      } else {
+        red[SMALL_WARPS] = x;
+      }
+    }
+  }
+  __syncthreads();
+  return make_double2(red[SMALL_WARPS], red[SMALL_WARPS + 1]);
 }
 
 // y = H x for the rows r = tid, tid + nt, ... (k_spmm's per-row order);
@@ -212,9 +246,13 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
   __shared__ int piv[SPC_MAX_M];
   __shared__ int s_sh, p_sh;
   __shared__ double2 red[SMALL_WARPS + 1];
+  double* redd = reinterpret_cast<double*>(red);  // block_sum1's SMALL_WARPS + 2 doubles
   __shared__ double2 part[SMALL_WARPS][32];
   __shared__ double terms[16];
   __shared__ double cstat[2];
+  __shared__ double loop_t;
+  __shared__ int loop_k, loop_done;
+  __shared__ long long loop_steps;
 
   const int s = blockIdx.x;
   const SmallJob J = jobs[sjob[s]];
@@ -248,14 +286,14 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
     for (int attempt = 0; attempt < 2; ++attempt) {
       for (int i = tid; i < (int)mm; i += SMALL_THREADS) A[i] = cz();
       // c = ||psi|| e_1, Q_0 = psi / ||psi|| (get_krylov :440-447)
-      double2 acc = cz();
+      double acc = 0.0;
       for (int r = tid; r < n; r += SMALL_THREADS) {
         const double2 x = psi[r];
-        acc.x = fma(x.x, x.x, acc.x);
-        acc.x = fma(x.y, x.y, acc.x);
+        acc = fma(x.x, x.x, acc);
+        acc = fma(x.y, x.y, acc);
       }
-      const double b0 = sqrt(block_sum2(acc, red).x);
-      const double rb0 = b0 > 0.0 ? 1.0 / b0 : 0.0;
+      const double2 bn0 = block_sum1<true>(acc, redd);
+      const double b0 = bn0.x, rb0 = bn0.y;
       for (int r = tid; r < n; r += SMALL_THREADS) {
         const double2 x = psi[r];
         Q[r] = make_double2(x.x * rb0, x.y * rb0);
@@ -269,7 +307,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
         __syncthreads();
         if (lz) {
           // p -= beta_{i-1} Q_{i-1}; alpha_i = Re <Q_i, p>
-          double2 a2 = cz();
+          double a2 = 0.0;
           for (int r = tid; r < n; r += SMALL_THREADS) {
             double2 pv = p[r];
             if (i > 0) {
@@ -279,28 +317,29 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
               p[r] = pv;
             }
             const double2 x = qi[r];
-            a2.x = fma(x.x, pv.x, a2.x);
-            a2.x = fma(x.y, pv.y, a2.x);
+            a2 = fma(x.x, pv.x, a2);
+            a2 = fma(x.y, pv.y, a2);
           }
-          const double alpha = block_sum2(a2, red).x;
+          const double alpha = block_sum1<false>(a2, redd).x;
           if (tid == 0) A[i + i * m] = make_double2(alpha, -kap);
           if (i < me - 1) {
-            double2 nr = cz();
+            double nr = 0.0;
             for (int r = tid; r < n; r += SMALL_THREADS) {
               const double2 q = qi[r];
               double2 pv = p[r];
               pv.x = fma(-alpha, q.x, pv.x);
               pv.y = fma(-alpha, q.y, pv.y);
               p[r] = pv;
-              nr.x = fma(pv.x, pv.x, nr.x);
-              nr.x = fma(pv.y, pv.y, nr.x);
+              nr = fma(pv.x, pv.x, nr);
+              nr = fma(pv.y, pv.y, nr);
             }
-            beta = sqrt(block_sum2(nr, red).x);
+            const double2 bn = block_sum1<true>(nr, redd);
+            beta = bn.x;
             if (tid == 0) {
               A[(i + 1) + i * m] = make_double2(beta, 0.0);
               A[i + (i + 1) * m] = make_double2(beta, 0.0);
             }
-            const double rb = beta > 0.0 ? 1.0 / beta : 0.0;
+            const double rb = bn.y;
             double2* qn = Q + (size_t)(i + 1) * n;
             for (int r = tid; r < n; r += SMALL_THREADS) {
               const double2 pv = p[r];
@@ -327,16 +366,16 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
             if (tid == 0) A[(j + 1) + i * m] = hc;
           }
           if (i < me - 1) {
-            double2 nr = cz();
+            double nr = 0.0;
             for (int r = tid; r < n; r += SMALL_THREADS) {
               const double2 pv = cfms(hc, qi[r], p[r]);
               p[r] = pv;
-              nr.x = fma(pv.x, pv.x, nr.x);
-              nr.x = fma(pv.y, pv.y, nr.x);
+              nr = fma(pv.x, pv.x, nr);
+              nr = fma(pv.y, pv.y, nr);
             }
-            const double b = sqrt(block_sum2(nr, red).x);
-            if (tid == 0) A[(i + 1) + i * m] = make_double2(b, 0.0);
-            const double rb = b > 0.0 ? 1.0 / b : 0.0;
+            const double2 bn = block_sum1<true>(nr, redd);
+            if (tid == 0) A[(i + 1) + i * m] = make_double2(bn.x, 0.0);
+            const double rb = bn.y;
             double2* qn = Q + (size_t)(i + 1) * n;
             for (int r = tid; r < n; r += SMALL_THREADS) {
               const double2 pv = p[r];
@@ -382,91 +421,127 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
     expm_one<false>(me, m, A, E, dt, X, rowsum, piv, &s_sh, &p_sh, tid, SMALL_THREADS, err);
     __syncthreads();
     // dt loop (:348-364): c <- E c; P_X(t) = Re(c^H P_X c); stop when the
-    // last Krylov coordinate grows past tol or the window ends
-    double2* c = cA;
-    double2* cn = cB;
-    double c2 = 1.0, cm2 = 0.0;
-    while (cm2 <= tol * c2 && t < t_end) {
-      if (k >= T) {  // output full (guard; every thread takes it)
-        if (tid == 0) atomicExch(err, 1);
-        done = true;
-        break;
+    // last Krylov coordinate grows past tol or the window ends. It runs on
+    // warps 0-3, one per scheduler: GB300's FP64 pipe sits in each scheduler
+    // and a warp instruction holds it for the same time whatever its active
+    // lanes, so the step is laid out to issue few FP64 warp instructions:
+    //  * c' = E c with lane = row and warp w over the columns j = w mod 4 (c_j
+    //    by shuffle); every warp adds the four partials in warp order, so
+    //    each holds c' in its lanes and no further barrier is needed;
+    //  * the four forms over the pairs i <= j, with the Hermitian weights in
+    //    W = (s Re P_ij, -s Im P_ij) (s = 1 on the diagonal, 2 above it) and
+    //    g_ij = conj(c_i) c_j shared by the types: 12 FP64 operations a pair;
+    //  * each warp's four sums by a reduce-scatter over its lanes (6 adds
+    //    instead of 20), then the warps' sums added in warp order.
+    // Warps 4-7 wait at the barrier after the loop.
+    const int npair = me * (me + 1) / 2;
+    double2* W = X;  // 4 x npair weights in the spent expm scratch
+    for (int idx = tid; idx < 4 * npair; idx += SMALL_THREADS) {
+      const int ty = idx / npair;
+      int rem = idx % npair, i = 0;
+      while (rem >= me - i) {
+        rem -= me - i;
+        ++i;
       }
-      // c' = E c: warp w sums columns j = w, w + 8, ...; lane = row
-      double2 a = cz();
-      if (lane < me)
-        for (int j = warp; j < me; j += SMALL_WARPS) a = cfma(E[lane + j * m], c[j], a);
-      part[warp][lane] = a;
-      __syncthreads();
-      if (tid < me) {
-        double2 v = part[0][tid];
-        for (int w = 1; w < SMALL_WARPS; ++w) v = cadd(v, part[w][tid]);
-        cn[tid] = v;
-      }
-      __syncthreads();
-      // Re(c'^H P_t c') for the 4 types on warps 0-3 (one per scheduler):
-      // each Hermitian form is its diagonal plus twice the real part of the
-      // upper triangle, and g_ij = conj(c_i) c_j is shared by the types:
-      // Re(conj(c_i) P_ij c_j) = Re(P_ij) Re(g_ij) - Im(P_ij) Im(g_ij).
-      // Warp 4 takes |c'|^2 and |c'_{m-1}|^2.
-      if (warp < 4) {
-        double f0 = 0.0, f1 = 0.0, f2 = 0.0, f3 = 0.0;
-        const int npair = me * (me + 1) / 2;
-        int i = 0, rem = tid;
-        while (i < me && rem >= me - i) {
-          rem -= me - i;
-          ++i;
-        }
-        for (int pidx = tid; pidx < npair; pidx += 128) {
-          const int j = i + rem;
-          const double2 ci = cn[i], cj = cn[j];
-          const double sc = (i == j) ? 1.0 : 2.0;
-          const double gx = sc * fma(ci.x, cj.x, ci.y * cj.y), gy = sc * fma(ci.x, cj.y, -ci.y * cj.x);
-          const size_t x = (size_t)i + (size_t)j * m;
-          f0 = fma(P[x].x, gx, fma(-P[x].y, gy, f0));
-          f1 = fma(P[mm + x].x, gx, fma(-P[mm + x].y, gy, f1));
-          f2 = fma(P[2 * mm + x].x, gx, fma(-P[2 * mm + x].y, gy, f2));
-          f3 = fma(P[3 * mm + x].x, gx, fma(-P[3 * mm + x].y, gy, f3));
-          rem += 128;
-          while (i < me && rem >= me - i) {
+      const double2 pv = P[ty * mm + i + (size_t)(i + rem) * m];
+      const double sw = rem == 0 ? 1.0 : 2.0;
+      W[idx] = make_double2(sw * pv.x, -sw * pv.y);
+    }
+    __syncthreads();
+    if (warp < 4) {
+      int pi[SMALL_ROUNDS], pj[SMALL_ROUNDS];
+#pragma unroll
+      for (int r = 0; r < SMALL_ROUNDS; ++r) {
+        pi[r] = -1;
+        pj[r] = 0;
+        int rem = r * 128 + tid;
+        if (rem < npair) {
+          int i = 0;
+          while (rem >= me - i) {
             rem -= me - i;
             ++i;
           }
-        }
-        f0 = warp_sum(f0);
-        f1 = warp_sum(f1);
-        f2 = warp_sum(f2);
-        f3 = warp_sum(f3);
-        if (lane == 0) {
-          terms[4 * warp + 0] = f0;
-          terms[4 * warp + 1] = f1;
-          terms[4 * warp + 2] = f2;
-          terms[4 * warp + 3] = f3;
-        }
-      } else if (warp == 4) {
-        double nn = 0.0;
-        if (lane < me) nn = fma(cn[lane].x, cn[lane].x, cn[lane].y * cn[lane].y);
-        nn = warp_sum(nn);
-        if (lane == 0) {
-          cstat[0] = nn;
-          const double2 cmv = cn[me - 1];
-          cstat[1] = cmv.x * cmv.x + cmv.y * cmv.y;
+          pi[r] = i;
+          pj[r] = i + rem;
         }
       }
-      __syncthreads();
-      if (tid < 4) {
-        const int slot = tid == 0 ? 2 : (tid == 1 ? 0 : (tid == 2 ? 1 : 3));  // proj type -> obs slot
-        o[slot * T + k] = ((terms[tid] + terms[4 + tid]) + terms[8 + tid]) + terms[12 + tid];
+      double2 c = lane < me ? cA[lane] : cz();
+      double c2 = 1.0, cm2 = 0.0;
+      while (cm2 <= tol * c2 && t < t_end) {
+        if (k >= T) {  // output full (guard; every thread takes it)
+          if (tid == 0) atomicExch(err, 1);
+          done = true;
+          break;
+        }
+        double2 a = cz();
+        for (int j = warp; j < me; j += 4) {
+          const double2 cj = make_double2(__shfl_sync(0xffffffffu, c.x, j), __shfl_sync(0xffffffffu, c.y, j));
+          if (lane < me) a = cfma(E[lane + j * m], cj, a);
+        }
+        part[warp][lane] = a;
+        small_bar4();
+        double2 cn = cz();
+        if (lane < me) cn = cadd(cadd(cadd(part[0][lane], part[1][lane]), part[2][lane]), part[3][lane]);
+        double f0 = 0.0, f1 = 0.0, f2 = 0.0, f3 = 0.0;
+#pragma unroll
+        for (int r = 0; r < SMALL_ROUNDS; ++r) {
+          if (r * 128 + warp * 32 >= npair) break;  // no pair of this warp left
+          const int i = max(pi[r], 0), j = pj[r];
+          const double cix = __shfl_sync(0xffffffffu, cn.x, i), ciy = __shfl_sync(0xffffffffu, cn.y, i);
+          const double cjx = __shfl_sync(0xffffffffu, cn.x, j), cjy = __shfl_sync(0xffffffffu, cn.y, j);
+          if (pi[r] >= 0) {
+            const double gx = fma(cix, cjx, ciy * cjy), gy = fma(cix, cjy, -ciy * cjx);
+            const int pp = r * 128 + tid;
+            const double2 w0 = W[pp], w1 = W[npair + pp], w2 = W[2 * npair + pp], w3 = W[3 * npair + pp];
+            f0 = fma(w0.x, gx, fma(w0.y, gy, f0));
+            f1 = fma(w1.x, gx, fma(w1.y, gy, f1));
+            f2 = fma(w2.x, gx, fma(w2.y, gy, f2));
+            f3 = fma(w3.x, gx, fma(w3.y, gy, f3));
+          }
+        }
+        // reduce-scatter: lanes 8t..8t+7 end with the warp's sum of form t
+        const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+        double ka = h16 ? f2 : f0, kb = h16 ? f3 : f1;
+        ka += __shfl_xor_sync(0xffffffffu, h16 ? f0 : f2, 16);
+        kb += __shfl_xor_sync(0xffffffffu, h16 ? f1 : f3, 16);
+        double v = h8 ? kb : ka;
+        v += __shfl_xor_sync(0xffffffffu, h8 ? ka : kb, 8);
+        v += __shfl_xor_sync(0xffffffffu, v, 4);
+        v += __shfl_xor_sync(0xffffffffu, v, 2);
+        v += __shfl_xor_sync(0xffffffffu, v, 1);
+        if ((lane & 7) == 0) terms[4 * warp + (lane >> 3)] = v;
+        if (warp == 3) {  // the warp with the fewest pairs: |c'|^2, |c'_{m-1}|^2
+          double nn = lane < me ? fma(cn.x, cn.x, cn.y * cn.y) : 0.0;
+          nn = warp_sum(nn);
+          if (lane == 0) cstat[0] = nn;
+          if (lane == me - 1) cstat[1] = cn.x * cn.x + cn.y * cn.y;
+        }
+        small_bar4();
+        if (tid < 4) {
+          const int slot = tid == 0 ? 2 : (tid == 1 ? 0 : (tid == 2 ? 1 : 3));  // proj type -> obs slot
+          o[slot * T + k] = ((terms[tid] + terms[4 + tid]) + terms[8 + tid]) + terms[12 + tid];
+        }
+        c2 = cstat[0];
+        cm2 = cstat[1];
+        c = cn;
+        t = t + dt;
+        k = k + 1;
+        steps++;
       }
-      c2 = cstat[0];
-      cm2 = cstat[1];
-      double2* tmp = c;
-      c = cn;
-      cn = tmp;
-      t = t + dt;
-      k = k + 1;
-      steps++;
+      if (warp == 0 && lane < me) cA[lane] = c;  // for psi = Q c
+      if (tid == 0) {
+        loop_t = t;
+        loop_k = k;
+        loop_steps = steps;
+        loop_done = done ? 1 : 0;
+      }
     }
+    __syncthreads();
+    t = loop_t;
+    k = loop_k;
+    steps = loop_steps;
+    done = loop_done != 0;
+    const double2* c = cA;
     if (!done) done = !(t < t_end);
     if (!done) {
       // psi = Q c (:365)
@@ -476,7 +551,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
         psi[r] = acc3;
       }
     }
-    // c lives in cA or cB; the next build rewrites cA after a barrier
+    // c lives in cA; the next build rewrites it after a barrier
     __syncthreads();
   }
   if (tid == 0) {
