@@ -135,7 +135,8 @@ int spc_set_h(spc_handle* h, const spc_csr* H);
  * device array of about 5.3 MB that every GPU loading the library holds until
  * exit; systems above 2^20 rows, 64 nuclei or 65536 entry-table elements are
  * rejected with SPC_ERR_ARG. The first call under a device's context looks up
- * that array's device address (again after cudaDeviceReset). The size comes
+ * that array's device address (again after cudaDeviceReset); make that first
+ * call before any stream capture begins on the device. The size comes
  * from the closed-form nonzero count: *n_out and *nnz_out are set, and a
  * cap_nnz that is too small returns SPC_ERR_ARG before anything is launched
  * or written. The call waits for `stream` twice (after the count and after
