@@ -140,7 +140,10 @@ __device__ __forceinline__ void small_spmm(const SmallJob& J, const double2* __r
 // The four projector Grams (k_proj + k_proj_reduce): P_t = V_t^H V_t over
 // the Z nuclear rows, V_0 = Q_|aa>, V_1 = Q_|ab> - Q_|ba> (S, halved),
 // V_2 = Q_|ab> + Q_|ba> (T0, halved), V_3 = Q_|bb>; staged SMALL_NC rows at
-// a time in V (4 m SMALL_VS complex). MAXC = ceil(combinations / threads)
+// a time in V (4 m SMALL_VS complex) with Re - Im (Vd) and Re + Im (Vs) of
+// every element beside it, so that each conj(a) b takes three products as in
+// k_proj: t1 += a_r b_r, t2 += a_i b_i, t3 += (a_r - a_i)(b_r + b_i),
+// conj(a) b = (t1 + t2, t3 - t1 + t2). MAXC = ceil(combinations / threads)
 // exactly: a combination slot that no thread needs still issues its
 // (predicated-off) DFMAs. Ends with a barrier.
 template <int MAXC>
@@ -148,16 +151,18 @@ __device__ void small_projectors(int m, int me, int n, int Z, const double2* __r
   const int tid = threadIdx.x;
   const size_t mm = (size_t)m * m;
   const int nc4 = me * (me + 1) / 2, ncombo = 4 * nc4;
+  double* Vd = reinterpret_cast<double*>(V + 4 * m * SMALL_VS);
+  double* Vs = Vd + 4 * m * SMALL_VS;
   // ceil(ncombo / MAXC) threads hold the combinations: the warps past them
   // skip the accumulation instead of issuing predicated-off FMAs
   const int nth = (ncombo + MAXC - 1) / MAXC;
   const bool on = tid < nth;
-  double2 acc[MAXC];
-  int oi[MAXC], oj[MAXC], tq[MAXC], iq[MAXC], jq[MAXC];
+  double t1[MAXC], t2[MAXC], t3[MAXC];
+  int oi[MAXC], oj[MAXC];
 #pragma unroll
   for (int q = 0; q < MAXC; ++q) {
-    acc[q] = cz();
-    oi[q] = oj[q] = tq[q] = iq[q] = jq[q] = 0;
+    t1[q] = t2[q] = t3[q] = 0.0;
+    oi[q] = oj[q] = 0;
     const int cid = tid + q * nth;
     if (on && cid < ncombo) {
       const int t = cid / nc4;
@@ -166,12 +171,8 @@ __device__ void small_projectors(int m, int me, int n, int Z, const double2* __r
         rem -= me - i;
         ++i;
       }
-      const int j = i + rem;
-      tq[q] = t;
-      iq[q] = i;
-      jq[q] = j;
       oi[q] = (t * m + i) * SMALL_VS;
-      oj[q] = (t * m + j) * SMALL_VS;
+      oj[q] = (t * m + i + rem) * SMALL_VS;
     }
   }
   for (int c0 = 0; c0 < Z; c0 += SMALL_NC) {
@@ -186,26 +187,43 @@ __device__ void small_projectors(int m, int me, int n, int Z, const double2* __r
         q3 = base[2 * Z];
         q4 = base[3 * Z];
       }
-      V[(0 * m + j) * SMALL_VS + nn] = q1;
-      V[(1 * m + j) * SMALL_VS + nn] = csub(q2, q3);
-      V[(2 * m + j) * SMALL_VS + nn] = cadd(q2, q3);
-      V[(3 * m + j) * SMALL_VS + nn] = q4;
+      const double2 v[4] = {q1, csub(q2, q3), cadd(q2, q3), q4};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int o = (t * m + j) * SMALL_VS + nn;
+        V[o] = v[t];
+        Vd[o] = v[t].x - v[t].y;
+        Vs[o] = v[t].x + v[t].y;
+      }
     }
     __syncthreads();
     if (on)
       for (int nn = 0; nn < len; ++nn) {
 #pragma unroll
         for (int q = 0; q < MAXC; ++q)
-          if (tid + q * nth < ncombo) acc[q] = cjfma(V[oi[q] + nn], V[oj[q] + nn], acc[q]);
+          if (tid + q * nth < ncombo) {
+            const double2 a = V[oi[q] + nn], b = V[oj[q] + nn];
+            t1[q] = fma(a.x, b.x, t1[q]);
+            t2[q] = fma(a.y, b.y, t2[q]);
+            t3[q] = fma(Vd[oi[q] + nn], Vs[oj[q] + nn], t3[q]);
+          }
       }
     __syncthreads();
   }
 #pragma unroll
   for (int q = 0; q < MAXC; ++q) {
-    if (on && tid + q * nth < ncombo) {
-      const int t = tq[q], i = iq[q], j = jq[q];
-      double2 s = acc[q];
+    const int cid = tid + q * nth;
+    if (on && cid < ncombo) {
+      const int t = cid / nc4;
+      int rem = cid % nc4, i = 0;
+      while (rem >= me - i) {
+        rem -= me - i;
+        ++i;
+      }
+      const int j = i + rem;
+      double2 s = make_double2(t1[q] + t2[q], t3[q] - t1[q] + t2[q]);
       if (t == 1 || t == 2) s = make_double2(0.5 * s.x, 0.5 * s.y);
+      if (i == j) s.y = 0.0;  // a Gram's diagonal is real; the three-product form leaves rounding there
       double2* Pt = P + t * mm;
       Pt[i + j * m] = s;
       if (i != j) Pt[j + i * m] = make_double2(s.x, -s.y);
@@ -234,7 +252,7 @@ __device__ void small_projectors_any(int m, int me, int n, int Z, const double2*
 // with vec_smem they live in shared memory instead (every job's (m+2) n
 // complex fits there), which cuts the latency of the row sweeps.
 // Dynamic shared memory: A, E (m^2 each), P (4 m^2), c and c' (m each),
-// max(5 m^2, 4 m SMALL_VS) of expm / projector scratch, all complex, then
+// max(5 m^2, 8 m SMALL_VS) of expm / projector scratch, all complex, then
 // the vectors when vec_smem.
 __global__ void __launch_bounds__(SMALL_THREADS, 2)
     k_small_prop(const SmallJob* __restrict__ jobs, const int* __restrict__ sjob, const int* __restrict__ scol,
@@ -265,7 +283,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
   double2* cA = P + 4 * mm;
   double2* cB = cA + m;
   double2* X = cB + m;
-  double2* Q = vec_smem ? X + std::max<size_t>(5 * mm, 4 * (size_t)m * SMALL_VS) : work + soff[s];
+  double2* Q = vec_smem ? X + std::max<size_t>(5 * mm, 8 * (size_t)m * SMALL_VS) : work + soff[s];
   double2* p = Q + (size_t)m * n;
   double2* psi = p + n;
   const bool herm = J.kappa != nullptr;
@@ -565,7 +583,7 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
 // without the vectors.
 static size_t small_smem_bytes(int m) {
   const size_t mm = (size_t)m * m;
-  return sizeof(double2) * (6 * mm + 2 * (size_t)m + std::max<size_t>(5 * mm, 4 * (size_t)m * SMALL_VS));
+  return sizeof(double2) * (6 * mm + 2 * (size_t)m + std::max<size_t>(5 * mm, 8 * (size_t)m * SMALL_VS));
 }
 
 // Whether a call runs on k_small_prop (sets smem). Rows, m, shared memory
