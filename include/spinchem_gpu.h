@@ -307,11 +307,16 @@ int spc_mem_info(int device, int64_t* free_bytes, int64_t* total_bytes);
  * launch: SPC_SAMPLE_AUTO (default) when every job has at most 2048 rows,
  * m <= 32, a build of about 2.5e6 FP64 FMAs or less and the samples fill at
  * most two waves of CTAs; SPC_SAMPLE_OFF never; SPC_SAMPLE_ON whenever the
- * call fits it (rows, m, shared and device memory). The tiled path serves
- * every other call. Results agree with the tiled path to rounding. */
+ * call fits it (rows, m, shared and device memory). When the samples fill at
+ * most half the SMs, each sample takes a cluster of two CTAs (the second
+ * forms the projectors and the populations of every dt step beside the
+ * first's serial path); SPC_SAMPLE_SINGLE is SPC_SAMPLE_ON with one CTA per
+ * sample always. The tiled path serves every other call. Results agree with
+ * the tiled path to rounding. */
 #define SPC_SAMPLE_AUTO 0
 #define SPC_SAMPLE_OFF 1
 #define SPC_SAMPLE_ON 2
+#define SPC_SAMPLE_SINGLE 3
 int spc_set_sample_path(spc_handle* h, int mode);
 
 /* Cap on the device memory one propagation call on this handle may hold

@@ -99,7 +99,7 @@ SIGNATURES = {
     "spc_fp64_peak": (_I, [_I, C.POINTER(_D)]),
 }
 SPC_KERNEL_KINDS = 14
-SPC_SAMPLE_AUTO, SPC_SAMPLE_OFF, SPC_SAMPLE_ON = 0, 1, 2
+SPC_SAMPLE_AUTO, SPC_SAMPLE_OFF, SPC_SAMPLE_ON, SPC_SAMPLE_SINGLE = 0, 1, 2, 3
 
 _LIB: C.CDLL | None = None
 

@@ -434,7 +434,7 @@ int spc_set_graphs(spc_handle* h, int enable) {
 
 int spc_set_sample_path(spc_handle* h, int mode) {
   if (!h) return spc::set_error(SPC_ERR_ARG, "null handle");
-  if (mode < SPC_SAMPLE_AUTO || mode > SPC_SAMPLE_ON) return spc::set_error(SPC_ERR_ARG, "unknown sample-path mode %d", mode);
+  if (mode < SPC_SAMPLE_AUTO || mode > SPC_SAMPLE_SINGLE) return spc::set_error(SPC_ERR_ARG, "unknown sample-path mode %d", mode);
   h->h.sample_path = mode;
   return SPC_OK;
 }

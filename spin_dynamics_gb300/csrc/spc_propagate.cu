@@ -37,6 +37,8 @@
 #include <set>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "spc_common.cuh"
 #include "spc_internal.h"
 

@@ -247,6 +247,154 @@ __device__ void small_projectors_any(int m, int me, int n, int Z, const double2*
   }
 }
 
+// One Krylov basis of psi (get_krylov, src/qm_dynamics.f90:432-467): A (m x m,
+// zeroed first) gets the tridiagonal (lz: Lanczos on the Hermitian part, real
+// coefficients, alpha - i*kappa on the diagonal) or the Hessenberg (MGS),
+// Q_0..Q_{me-1} the basis, cA = ||psi|| e_1; p is the work vector. Called by
+// all SMALL_THREADS threads of the CTA; thread 0 writes A's last entries after
+// the last barrier, so the caller synchronises before reading A.
+__device__ __forceinline__ void small_krylov(const SmallJob& J, bool lz, bool herm, double kap, int m, double2* A,
+                                             double2* cA, double2* Q, double2* p, const double2* psi,
+                                             double2* red, double* redd) {
+  const int n = J.n, me = J.me, tid = threadIdx.x;
+  const size_t mm = (size_t)m * m;
+  for (int i = tid; i < (int)mm; i += SMALL_THREADS) A[i] = cz();
+  // c = ||psi|| e_1, Q_0 = psi / ||psi|| (get_krylov :440-447)
+  double acc = 0.0;
+  for (int r = tid; r < n; r += SMALL_THREADS) {
+    const double2 x = psi[r];
+    acc = fma(x.x, x.x, acc);
+    acc = fma(x.y, x.y, acc);
+  }
+  const double2 bn0 = block_sum1<true>(acc, redd);
+  const double b0 = bn0.x, rb0 = bn0.y;
+  for (int r = tid; r < n; r += SMALL_THREADS) {
+    const double2 x = psi[r];
+    Q[r] = make_double2(x.x * rb0, x.y * rb0);
+  }
+  if (tid < m) cA[tid] = tid == 0 ? make_double2(b0, 0.0) : cz();
+  __syncthreads();
+  double beta = 0.0;
+  for (int i = 0; i < me; ++i) {
+    const double2* qi = Q + (size_t)i * n;
+    small_spmm(J, qi, p, !lz && herm, kap);
+    __syncthreads();
+    if (lz) {
+      // p -= beta_{i-1} Q_{i-1}; alpha_i = Re <Q_i, p>
+      double a2 = 0.0;
+      for (int r = tid; r < n; r += SMALL_THREADS) {
+        double2 pv = p[r];
+        if (i > 0) {
+          const double2 q = qi[r - n];
+          pv.x = fma(-beta, q.x, pv.x);
+          pv.y = fma(-beta, q.y, pv.y);
+          p[r] = pv;
+        }
+        const double2 x = qi[r];
+        a2 = fma(x.x, pv.x, a2);
+        a2 = fma(x.y, pv.y, a2);
+      }
+      const double alpha = block_sum1<false>(a2, redd).x;
+      if (tid == 0) A[i + i * m] = make_double2(alpha, -kap);
+      if (i < me - 1) {
+        double nr = 0.0;
+        for (int r = tid; r < n; r += SMALL_THREADS) {
+          const double2 q = qi[r];
+          double2 pv = p[r];
+          pv.x = fma(-alpha, q.x, pv.x);
+          pv.y = fma(-alpha, q.y, pv.y);
+          p[r] = pv;
+          nr = fma(pv.x, pv.x, nr);
+          nr = fma(pv.y, pv.y, nr);
+        }
+        const double2 bn = block_sum1<true>(nr, redd);
+        beta = bn.x;
+        if (tid == 0) {
+          A[(i + 1) + i * m] = make_double2(beta, 0.0);
+          A[i + (i + 1) * m] = make_double2(beta, 0.0);
+        }
+        const double rb = bn.y;
+        double2* qn = Q + (size_t)(i + 1) * n;
+        for (int r = tid; r < n; r += SMALL_THREADS) {
+          const double2 pv = p[r];
+          qn[r] = make_double2(pv.x * rb, pv.y * rb);
+        }
+        __syncthreads();
+      }
+    } else {
+      // MGS (get_krylov :453-456): h_0 = <Q_0, p>; then p -= h_j Q_j
+      // fused with h_{j+1} = <Q_{j+1}, p>
+      double2 a2 = cz();
+      for (int r = tid; r < n; r += SMALL_THREADS) a2 = cjfma(Q[r], p[r], a2);
+      double2 hc = block_sum2(a2, red);
+      if (tid == 0) A[0 + i * m] = hc;
+      for (int j = 0; j < i; ++j) {
+        const double2* qj = Q + (size_t)j * n;
+        a2 = cz();
+        for (int r = tid; r < n; r += SMALL_THREADS) {
+          const double2 pv = cfms(hc, qj[r], p[r]);
+          p[r] = pv;
+          a2 = cjfma(qj[r + n], pv, a2);
+        }
+        hc = block_sum2(a2, red);
+        if (tid == 0) A[(j + 1) + i * m] = hc;
+      }
+      if (i < me - 1) {
+        double nr = 0.0;
+        for (int r = tid; r < n; r += SMALL_THREADS) {
+          const double2 pv = cfms(hc, qi[r], p[r]);
+          p[r] = pv;
+          nr = fma(pv.x, pv.x, nr);
+          nr = fma(pv.y, pv.y, nr);
+        }
+        const double2 bn = block_sum1<true>(nr, redd);
+        if (tid == 0) A[(i + 1) + i * m] = make_double2(bn.x, 0.0);
+        const double rb = bn.y;
+        double2* qn = Q + (size_t)(i + 1) * n;
+        for (int r = tid; r < n; r += SMALL_THREADS) {
+          const double2 pv = p[r];
+          qn[r] = make_double2(pv.x * rb, pv.y * rb);
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// max |sum_t P_t - I| over the me x me block of the four Grams (NaN wins):
+// the orthonormality of a Lanczos basis (the Grams sum to Q^H Q). Called by
+// all threads; every thread gets the maximum.
+__device__ __forceinline__ double small_ortho_err(int me, int m, const double2* P, double* terms, double* cstat) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const size_t mm = (size_t)m * m;
+  double mx = 0.0;
+  for (int id = tid; id < me * me; id += SMALL_THREADS) {
+    const int i = id % me, j = id / me;
+    const size_t x = (size_t)i + (size_t)j * m;
+    const double2 g = cadd(cadd(P[x], P[mm + x]), cadd(P[2 * mm + x], P[3 * mm + x]));
+    const double e = fmax(fabs(g.x - (i == j ? 1.0 : 0.0)), fabs(g.y));
+    mx = (e > mx || e != e) ? e : mx;
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    const double v = __shfl_xor_sync(0xffffffffu, mx, d);
+    mx = (v > mx || v != v) ? v : mx;
+  }
+  if (lane == 0) terms[warp] = mx;
+  __syncthreads();
+  if (warp == 0) {
+    double v = lane < SMALL_WARPS ? terms[lane] : 0.0;
+    for (int d = 16; d > 0; d >>= 1) {
+      const double u = __shfl_xor_sync(0xffffffffu, v, d);
+      v = (u > v || u != u) ? u : v;
+    }
+    if (lane == 0) cstat[0] = v;
+  }
+  __syncthreads();
+  const double mall = cstat[0];
+  __syncthreads();
+  return mall;
+}
+
 // Grid: one CTA of SMALL_THREADS per sample (global sample s = blockIdx.x).
 // work + soff[s]: the sample's basis (m x n), work vector (n) and state (n);
 // with vec_smem they live in shared memory instead (every job's (m+2) n
@@ -302,135 +450,11 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
   while (!done) {
     bool lz = lanczos != 0 && herm;
     for (int attempt = 0; attempt < 2; ++attempt) {
-      for (int i = tid; i < (int)mm; i += SMALL_THREADS) A[i] = cz();
-      // c = ||psi|| e_1, Q_0 = psi / ||psi|| (get_krylov :440-447)
-      double acc = 0.0;
-      for (int r = tid; r < n; r += SMALL_THREADS) {
-        const double2 x = psi[r];
-        acc = fma(x.x, x.x, acc);
-        acc = fma(x.y, x.y, acc);
-      }
-      const double2 bn0 = block_sum1<true>(acc, redd);
-      const double b0 = bn0.x, rb0 = bn0.y;
-      for (int r = tid; r < n; r += SMALL_THREADS) {
-        const double2 x = psi[r];
-        Q[r] = make_double2(x.x * rb0, x.y * rb0);
-      }
-      if (tid < m) cA[tid] = tid == 0 ? make_double2(b0, 0.0) : cz();
-      __syncthreads();
-      double beta = 0.0;
-      for (int i = 0; i < me; ++i) {
-        const double2* qi = Q + (size_t)i * n;
-        small_spmm(J, qi, p, !lz && herm, kap);
-        __syncthreads();
-        if (lz) {
-          // p -= beta_{i-1} Q_{i-1}; alpha_i = Re <Q_i, p>
-          double a2 = 0.0;
-          for (int r = tid; r < n; r += SMALL_THREADS) {
-            double2 pv = p[r];
-            if (i > 0) {
-              const double2 q = qi[r - n];
-              pv.x = fma(-beta, q.x, pv.x);
-              pv.y = fma(-beta, q.y, pv.y);
-              p[r] = pv;
-            }
-            const double2 x = qi[r];
-            a2 = fma(x.x, pv.x, a2);
-            a2 = fma(x.y, pv.y, a2);
-          }
-          const double alpha = block_sum1<false>(a2, redd).x;
-          if (tid == 0) A[i + i * m] = make_double2(alpha, -kap);
-          if (i < me - 1) {
-            double nr = 0.0;
-            for (int r = tid; r < n; r += SMALL_THREADS) {
-              const double2 q = qi[r];
-              double2 pv = p[r];
-              pv.x = fma(-alpha, q.x, pv.x);
-              pv.y = fma(-alpha, q.y, pv.y);
-              p[r] = pv;
-              nr = fma(pv.x, pv.x, nr);
-              nr = fma(pv.y, pv.y, nr);
-            }
-            const double2 bn = block_sum1<true>(nr, redd);
-            beta = bn.x;
-            if (tid == 0) {
-              A[(i + 1) + i * m] = make_double2(beta, 0.0);
-              A[i + (i + 1) * m] = make_double2(beta, 0.0);
-            }
-            const double rb = bn.y;
-            double2* qn = Q + (size_t)(i + 1) * n;
-            for (int r = tid; r < n; r += SMALL_THREADS) {
-              const double2 pv = p[r];
-              qn[r] = make_double2(pv.x * rb, pv.y * rb);
-            }
-            __syncthreads();
-          }
-        } else {
-          // MGS (get_krylov :453-456): h_0 = <Q_0, p>; then p -= h_j Q_j
-          // fused with h_{j+1} = <Q_{j+1}, p>
-          double2 a2 = cz();
-          for (int r = tid; r < n; r += SMALL_THREADS) a2 = cjfma(Q[r], p[r], a2);
-          double2 hc = block_sum2(a2, red);
-          if (tid == 0) A[0 + i * m] = hc;
-          for (int j = 0; j < i; ++j) {
-            const double2* qj = Q + (size_t)j * n;
-            a2 = cz();
-            for (int r = tid; r < n; r += SMALL_THREADS) {
-              const double2 pv = cfms(hc, qj[r], p[r]);
-              p[r] = pv;
-              a2 = cjfma(qj[r + n], pv, a2);
-            }
-            hc = block_sum2(a2, red);
-            if (tid == 0) A[(j + 1) + i * m] = hc;
-          }
-          if (i < me - 1) {
-            double nr = 0.0;
-            for (int r = tid; r < n; r += SMALL_THREADS) {
-              const double2 pv = cfms(hc, qi[r], p[r]);
-              p[r] = pv;
-              nr = fma(pv.x, pv.x, nr);
-              nr = fma(pv.y, pv.y, nr);
-            }
-            const double2 bn = block_sum1<true>(nr, redd);
-            if (tid == 0) A[(i + 1) + i * m] = make_double2(bn.x, 0.0);
-            const double rb = bn.y;
-            double2* qn = Q + (size_t)(i + 1) * n;
-            for (int r = tid; r < n; r += SMALL_THREADS) {
-              const double2 pv = p[r];
-              qn[r] = make_double2(pv.x * rb, pv.y * rb);
-            }
-            __syncthreads();
-          }
-        }
-      }
+      small_krylov(J, lz, herm, kap, m, A, cA, Q, p, psi, red, redd);
       small_projectors_any(m, me, n, Z, Q, P, X);
       if (!lz) break;
       // a Lanczos basis must be orthonormal: max |sum_t P_t - I| <= ORTHO_TOL
-      double mx = 0.0;
-      for (int id = tid; id < me * me; id += SMALL_THREADS) {
-        const int i = id % me, j = id / me;
-        const size_t x = (size_t)i + (size_t)j * m;
-        const double2 g = cadd(cadd(P[x], P[mm + x]), cadd(P[2 * mm + x], P[3 * mm + x]));
-        const double e = fmax(fabs(g.x - (i == j ? 1.0 : 0.0)), fabs(g.y));
-        mx = (e > mx || e != e) ? e : mx;
-      }
-      for (int d = 16; d > 0; d >>= 1) {
-        const double v = __shfl_xor_sync(0xffffffffu, mx, d);
-        mx = (v > mx || v != v) ? v : mx;
-      }
-      if (lane == 0) terms[warp] = mx;
-      __syncthreads();
-      if (warp == 0) {
-        double v = lane < SMALL_WARPS ? terms[lane] : 0.0;
-        for (int d = 16; d > 0; d >>= 1) {
-          const double u = __shfl_xor_sync(0xffffffffu, v, d);
-          v = (u > v || u != u) ? u : v;
-        }
-        if (lane == 0) cstat[0] = v;
-      }
-      __syncthreads();
-      const double mall = cstat[0];
-      __syncthreads();
+      const double mall = small_ortho_err(me, m, P, terms, cstat);
       if (mall <= ORTHO_TOL) break;
       nf++;
       lz = false;  // rebuild this basis with full MGS
@@ -579,6 +603,277 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Pair form: a cluster of two CTAs per sample, for calls with at most half as
+// many samples as SMs (the dim-288 workload runs 64 samples on 152 SMs, so
+// one CTA per sample leaves 88 SMs idle). The main CTA (cluster rank 0) keeps
+// the sample's serial path: the Krylov builds, the expm, the recurrence
+// c <- E c of the dt loop with its stop test, and psi = Q c. The helper CTA
+// (rank 1) takes the work off that path:
+//  * the four projector Grams, staged from the main CTA's basis through
+//    distributed shared memory, and the Lanczos orthonormality check, while
+//    the main CTA runs the expm of the same basis;
+//  * the populations Re(c^H P_X c) of every dt step, from the coordinates c
+//    that the main CTA's dt loop stores into the helper's shared memory in
+//    segments of at most hmax steps (two buffers): the helper evaluates a
+//    segment while the main CTA runs the next one, psi = Q c and the next
+//    Krylov build.
+// The main CTA's dt step is then c' = E c on four warps (one barrier) and the
+// stop test, which each of the four warps evaluates on its own copy of c'.
+// Control flow is uniform across the cluster: a flag that ends a loop is
+// written to both CTAs' shared memory before a cluster barrier and read after
+// it, and every thread of both CTAs reaches every cluster barrier. The
+// arithmetic is k_small_prop's except for the order in which the populations
+// add their pair terms (each lane's pairs in order, then a shuffle tree), so
+// populations agree with it to rounding and the rebuild schedule is the same.
+struct PairCtrl {
+  int ok;       // the basis passed the orthonormality check (written by the helper)
+  int cnt[2];   // per history buffer (written by the main CTA): steps in the segment,
+  int k0[2];    // output index of its first step,
+  int more[2];  // whether the build continues past it,
+  int done[2];  // whether the sample's propagation has ended
+};
+
+// Populations of cnt consecutive dt steps from their Krylov coordinates
+// (hist[st * m + i]), with the build's Hermitian weights W (4 x npair) and
+// pair table: step st on warp st mod SMALL_WARPS, the lanes over the pairs
+// (each lane adds its pairs' terms in order), then k_small_prop's
+// reduce-scatter; lanes 0, 8, 16, 24 write the four populations of output
+// index k0 + st. Called by all threads of the helper CTA.
+__device__ __forceinline__ void small_pair_forms(int cnt, int k0, int m, int npair, const double2* hist,
+                                                 const double2* W, const int2* pij, double* o, int T) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int st = warp; st < cnt; st += SMALL_WARPS) {
+    const double2* cv = hist + (size_t)st * m;
+    double f0 = 0.0, f1 = 0.0, f2 = 0.0, f3 = 0.0;
+    for (int pp = lane; pp < npair; pp += 32) {
+      const int2 ij = pij[pp];
+      const double2 ci = cv[ij.x], cj = cv[ij.y];
+      const double gx = fma(ci.x, cj.x, ci.y * cj.y), gy = fma(ci.x, cj.y, -ci.y * cj.x);
+      const double2 w0 = W[pp], w1 = W[npair + pp], w2 = W[2 * npair + pp], w3 = W[3 * npair + pp];
+      f0 = fma(w0.x, gx, fma(w0.y, gy, f0));
+      f1 = fma(w1.x, gx, fma(w1.y, gy, f1));
+      f2 = fma(w2.x, gx, fma(w2.y, gy, f2));
+      f3 = fma(w3.x, gx, fma(w3.y, gy, f3));
+    }
+    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+    double ka = h16 ? f2 : f0, kb = h16 ? f3 : f1;
+    ka += __shfl_xor_sync(0xffffffffu, h16 ? f0 : f2, 16);
+    kb += __shfl_xor_sync(0xffffffffu, h16 ? f1 : f3, 16);
+    double v = h8 ? kb : ka;
+    v += __shfl_xor_sync(0xffffffffu, h8 ? ka : kb, 8);
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    if ((lane & 7) == 0) {
+      const int ty = lane >> 3;
+      const int slot = ty == 0 ? 2 : (ty == 1 ? 0 : (ty == 2 ? 1 : 3));  // proj type -> obs slot
+      o[(size_t)slot * T + k0 + st] = v;
+    }
+  }
+}
+
+// Dynamic shared memory of k_small_pair (complex elements). Main CTA: A, E
+// (m^2 each), c (m), expm scratch (5 m^2), then the vectors when vec_smem.
+// Helper CTA: P (4 m^2), projector staging (8 m SMALL_VS), weights
+// (4 m(m+1)/2), pair table (m(m+1)/2 int2), history (2 hmax m).
+__host__ __device__ __forceinline__ size_t pair_main_elems(int m, int n, bool vec_smem) {
+  const size_t mm = (size_t)m * m;
+  return 7 * mm + (size_t)m + (vec_smem ? (size_t)(m + 2) * n : 0);
+}
+__host__ __device__ __forceinline__ size_t pair_help_elems(int m, int hmax) {
+  const size_t mm = (size_t)m * m, np = (size_t)m * (m + 1) / 2;
+  return 4 * mm + 8 * (size_t)m * SMALL_VS + 4 * np + (np + 1) / 2 + 2 * (size_t)hmax * m;
+}
+
+// Grid: two CTAs per sample (global sample s = blockIdx.x / 2), clusters of
+// two; arguments as k_small_prop's, plus hmax (steps per history buffer).
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(SMALL_THREADS, 1)
+    k_small_pair(const SmallJob* __restrict__ jobs, const int* __restrict__ sjob, const int* __restrict__ scol,
+                 const int64_t* __restrict__ soff, double2* __restrict__ work, Theta th, int m, int T, double dt,
+                 double t_end, double tol, int lanczos, int vec_smem, int hmax, double* __restrict__ obs,
+                 long long* __restrict__ nsteps, unsigned long long* __restrict__ counts, int* __restrict__ err) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ double2 smem[];
+  __shared__ double rowsum[SPC_MAX_M];
+  __shared__ int piv[SPC_MAX_M];
+  __shared__ int s_sh, p_sh;
+  __shared__ double2 red[SMALL_WARPS + 1];
+  double* redd = reinterpret_cast<double*>(red);
+  __shared__ double2 part[2][4][32];
+  __shared__ double terms[16];
+  __shared__ double cstat[2];
+  __shared__ PairCtrl ctrl;
+
+  const int rank = (int)cluster.block_rank();
+  const int s = blockIdx.x >> 1;
+  const SmallJob J = jobs[sjob[s]];
+  const int n = J.n, Z = J.Z, me = J.me;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const size_t mm = (size_t)m * m;
+  const int npair = me * (me + 1) / 2;
+  // main CTA's layout
+  double2* A = smem;
+  double2* E = A + mm;
+  double2* cA = E + mm;
+  double2* X = cA + m;
+  double2* Q = vec_smem ? X + 5 * mm : work + soff[s];
+  double2* p = Q + (size_t)m * n;
+  double2* psi = p + n;
+  // helper CTA's layout
+  const size_t np_max = (size_t)m * (m + 1) / 2;
+  double2* P = smem;
+  double2* V = P + 4 * mm;
+  double2* W = V + 8 * (size_t)m * SMALL_VS;
+  int2* pij = reinterpret_cast<int2*>(W + 4 * np_max);
+  double2* H = W + 4 * np_max + (np_max + 1) / 2;
+  // the other CTA's shared memory
+  PairCtrl* ctrl_main = cluster.map_shared_rank(&ctrl, 0);
+  PairCtrl* ctrl_help = cluster.map_shared_rank(&ctrl, 1);
+  double2* H_help = cluster.map_shared_rank(H, 1);
+  const double2* Q_main = vec_smem ? cluster.map_shared_rank(Q, 0) : Q;
+  const bool herm = J.kappa != nullptr;
+  const double kap = herm ? *J.kappa : 0.0;
+  double* o = obs + (size_t)s * 4 * T;
+
+  if (rank == 0) {
+    // psi_0 = theta (x) z (kron_vector)
+    const double2* zk = J.zk + (size_t)scol[s] * Z;
+    for (int r = tid; r < n; r += SMALL_THREADS) psi[r] = cmul(th.v[r / Z], zk[r % Z]);
+  }
+  __syncthreads();
+  double t = 0.0;
+  int k = 1;  // outputs 0 hold the initial populations (k_obs_init)
+  long long steps = 0;
+  unsigned long long nb = 0, nf = 0;
+  bool done = !(0.0 < t_end);
+  while (!done) {
+    bool lz = lanczos != 0 && herm;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+      if (rank == 0) small_krylov(J, lz, herm, kap, m, A, cA, Q, p, psi, red, redd);
+      cluster.sync();  // basis, A and c complete
+      if (rank == 0) {
+        expm_one<false>(me, m, A, E, dt, X, rowsum, piv, &s_sh, &p_sh, tid, SMALL_THREADS, err);
+      } else {
+        small_projectors_any(m, me, n, Z, Q_main, P, V);
+        // a Lanczos basis must be orthonormal: max |sum_t P_t - I| <= ORTHO_TOL
+        const bool okv = !lz || small_ortho_err(me, m, P, terms, cstat) <= ORTHO_TOL;
+        if (tid == 0) {
+          ctrl.ok = okv ? 1 : 0;
+          ctrl_main->ok = okv ? 1 : 0;
+        }
+      }
+      cluster.sync();  // Grams, check and exponential complete
+      if (ctrl.ok) break;
+      nf++;
+      lz = false;  // rebuild this basis with full MGS
+    }
+    nb++;
+    if (rank == 1) {
+      // Hermitian weights W_t = (s Re P_t, -s Im P_t) of the pairs i <= j
+      // (s = 1 on the diagonal, 2 above it) and the pair table
+      for (int idx = tid; idx < 4 * npair; idx += SMALL_THREADS) {
+        const int ty = idx / npair;
+        int rem = idx % npair, i = 0;
+        while (rem >= me - i) {
+          rem -= me - i;
+          ++i;
+        }
+        const double2 pv = P[ty * mm + i + (size_t)(i + rem) * m];
+        const double sw = rem == 0 ? 1.0 : 2.0;
+        W[idx] = make_double2(sw * pv.x, -sw * pv.y);
+        if (ty == 0) pij[idx] = make_int2(i, i + rem);
+      }
+      __syncthreads();
+    }
+    // dt loop (:348-364) in segments of at most hmax steps. Main CTA, warps
+    // 0-3: c' = E c with lane = row and warp w over the columns j = w mod 4
+    // (c_j by shuffle), the four partials (double-buffered by step parity)
+    // added in warp order by every warp, |c'|^2 and |c'_{me-1}|^2 by every
+    // warp for the stop test; warp 0 stores c' into the helper's history.
+    double2 c = (rank == 0 && lane < me) ? cA[lane] : cz();
+    double c2 = 1.0, cm2 = 0.0;
+    int buf = 0;
+    for (;;) {
+      if (rank == 0) {
+        if (warp < 4) {
+          double2* hist = H_help + (size_t)buf * hmax * m;
+          const int k0 = k;
+          int cnt = 0;
+          bool overflow = false;
+          while (cnt < hmax && cm2 <= tol * c2 && t < t_end) {
+            if (k >= T) {  // output full (guard; every chain thread takes it)
+              overflow = true;
+              break;
+            }
+            double2 a = cz();
+            for (int j = warp; j < me; j += 4) {
+              const double2 cj = make_double2(__shfl_sync(0xffffffffu, c.x, j), __shfl_sync(0xffffffffu, c.y, j));
+              if (lane < me) a = cfma(E[lane + j * m], cj, a);
+            }
+            part[cnt & 1][warp][lane] = a;
+            small_bar4();
+            double2 cn = cz();
+            if (lane < me)
+              cn = cadd(cadd(cadd(part[cnt & 1][0][lane], part[cnt & 1][1][lane]), part[cnt & 1][2][lane]),
+                        part[cnt & 1][3][lane]);
+            const double nn = lane < me ? fma(cn.x, cn.x, cn.y * cn.y) : 0.0;
+            c2 = warp_sum(nn);
+            cm2 = __shfl_sync(0xffffffffu, cn.x * cn.x + cn.y * cn.y, me - 1);
+            if (warp == 0 && lane < me) hist[(size_t)cnt * m + lane] = cn;
+            c = cn;
+            t = t + dt;
+            k = k + 1;
+            steps++;
+            cnt++;
+          }
+          const bool more = !overflow && cnt == hmax && cm2 <= tol * c2 && t < t_end;
+          const bool dn = overflow || (!more && !(t < t_end));
+          if (tid == 0) {
+            if (overflow) atomicExch(err, 1);
+            ctrl.more[buf] = more ? 1 : 0;
+            ctrl.done[buf] = dn ? 1 : 0;
+            ctrl_help->cnt[buf] = cnt;
+            ctrl_help->k0[buf] = k0;
+            ctrl_help->more[buf] = more ? 1 : 0;
+            ctrl_help->done[buf] = dn ? 1 : 0;
+          }
+          if (!more && warp == 0 && lane < me) cA[lane] = c;  // for psi = Q c
+        }
+        __syncthreads();
+      }
+      // history segment and flags visible to the helper; the flags of buffer
+      // buf are next written two segments on, after a cluster barrier that
+      // every thread reaches only once it has read them here
+      cluster.sync();
+      const bool more = ctrl.more[buf] != 0;
+      done = ctrl.done[buf] != 0;
+      if (rank == 1)
+        small_pair_forms(ctrl.cnt[buf], ctrl.k0[buf], m, npair, H + (size_t)buf * hmax * m, W, pij, o, T);
+      if (!more) break;
+      buf ^= 1;
+    }
+    if (rank == 0 && !done) {
+      // psi = Q c (:365)
+      for (int r = tid; r < n; r += SMALL_THREADS) {
+        double2 acc3 = cz();
+        for (int j = 0; j < me; ++j) acc3 = cfma(Q[(size_t)j * n + r], cA[j], acc3);
+        psi[r] = acc3;
+      }
+    }
+    __syncthreads();
+  }
+  // keep the helper's shared memory alive until the main CTA's last remote
+  // access has completed
+  cluster.sync();
+  if (rank == 0 && tid == 0) {
+    atomicAdd((unsigned long long*)nsteps, (unsigned long long)steps);
+    atomicAdd(&counts[0], nb);
+    atomicAdd(&counts[1], nf);
+  }
+}
+
 // Dynamic shared memory of k_small_prop for Krylov dimension m (bytes),
 // without the vectors.
 static size_t small_smem_bytes(int m) {
@@ -615,7 +910,7 @@ static bool small_path_fits(Handle* h, const std::vector<JobSpec>& jobs, int m, 
   double budget = (double)free_b + held - (512.0 * (1 << 20) + 0.02 * (double)total_b);
   if (h->mem_limit) budget = std::min(budget, (double)h->mem_limit);
   if (bytes > budget) return false;
-  if (h->sample_path == SPC_SAMPLE_ON) return true;
+  if (h->sample_path == SPC_SAMPLE_ON || h->sample_path == SPC_SAMPLE_SINGLE) return true;
   if (cudaFuncSetAttribute(k_small_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return false;
   int b = 0;
@@ -682,19 +977,41 @@ static int propagate_small(Handle* h, const double* theta, const double* init_po
   // the vectors in shared memory when every job's fit beside the matrices
   int nmax = 0;
   for (const JobSpec& j : jobs) nmax = std::max(nmax, j.n);
-  const size_t vbytes = sizeof(double2) * (size_t)(m + 2) * nmax;
-  const bool vec_smem = smem + vbytes + 8192 <= h->smem_optin;
-  if (vec_smem) smem += vbytes;
-  CK(cudaFuncSetAttribute(k_small_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t budget = h->smem_optin > 8192 ? h->smem_optin - 8192 : 0;  // less the static shared memory
   int* d_err = (int*)h->err.p;
   long long* d_nsteps = (long long*)((char*)h->err.p + 8);
   unsigned long long* d_counts = (unsigned long long*)((char*)h->err.p + 16);
+  // pair form (two CTAs per sample) when the samples fill at most half the
+  // SMs and its shared memory fits: history buffers of up to 64 steps
+  bool pair = h->sample_path != SPC_SAMPLE_SINGLE && 2 * (int64_t)G <= h->sm_count;
+  int hmax = 64;
+  size_t psmem = 0;
+  bool pvec = false;
+  if (pair) {
+    while (hmax > 8 && sizeof(double2) * pair_help_elems(m, hmax) > budget) hmax /= 2;
+    const size_t help = sizeof(double2) * pair_help_elems(m, hmax);
+    pvec = sizeof(double2) * pair_main_elems(m, nmax, true) <= budget;
+    psmem = std::max(help, sizeof(double2) * pair_main_elems(m, nmax, pvec));
+    pair = psmem <= budget &&
+           cudaFuncSetAttribute(k_small_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem) == cudaSuccess;
+  }
   int pe = h->prof.begin(st);
-  k_small_prop<<<G, SMALL_THREADS, smem, st>>>((const SmallJob*)plan, (const int*)(plan + o_sjob),
-                                               (const int*)(plan + o_scol), (const int64_t*)(plan + o_soff),
-                                               (double2*)h->Q.p, th, m, T, dt, t_end, tol, lanczos ? 1 : 0,
-                                               vec_smem ? 1 : 0, d_obs,
-                                               d_nsteps, d_counts, d_err);
+  if (pair) {
+    k_small_pair<<<2 * G, SMALL_THREADS, psmem, st>>>((const SmallJob*)plan, (const int*)(plan + o_sjob),
+                                                      (const int*)(plan + o_scol), (const int64_t*)(plan + o_soff),
+                                                      (double2*)h->Q.p, th, m, T, dt, t_end, tol, lanczos ? 1 : 0,
+                                                      pvec ? 1 : 0, hmax, d_obs, d_nsteps, d_counts, d_err);
+  } else {
+    const size_t vbytes = sizeof(double2) * (size_t)(m + 2) * nmax;
+    const bool vec_smem = smem + vbytes + 8192 <= h->smem_optin;
+    if (vec_smem) smem += vbytes;
+    CK(cudaFuncSetAttribute(k_small_prop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_small_prop<<<G, SMALL_THREADS, smem, st>>>((const SmallJob*)plan, (const int*)(plan + o_sjob),
+                                                 (const int*)(plan + o_scol), (const int64_t*)(plan + o_soff),
+                                                 (double2*)h->Q.p, th, m, T, dt, t_end, tol, lanczos ? 1 : 0,
+                                                 vec_smem ? 1 : 0, d_obs,
+                                                 d_nsteps, d_counts, d_err);
+  }
   h->prof.end(st, pe, PK_SAMPLE, 0.0, 0.0);
   h->count_launch();
   for (int j0 = 0; j0 < nj; j0 += 65535) {

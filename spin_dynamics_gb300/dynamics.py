@@ -231,8 +231,11 @@ class TraceSampler:
 
     def set_sample_path(self, mode: str) -> None:
         """Small systems with one CTA per sample ('auto' when it pays, 'off',
-        'on' whenever the call fits it); results agree to rounding."""
-        code = {"auto": nat.SPC_SAMPLE_AUTO, "off": nat.SPC_SAMPLE_OFF, "on": nat.SPC_SAMPLE_ON}[mode]
+        'on' whenever the call fits it, with a cluster of two CTAs per sample
+        when the samples fill at most half the SMs; 'single': 'on' with one
+        CTA per sample always); results agree to rounding."""
+        code = {"auto": nat.SPC_SAMPLE_AUTO, "off": nat.SPC_SAMPLE_OFF, "on": nat.SPC_SAMPLE_ON,
+                "single": nat.SPC_SAMPLE_SINGLE}[mode]
         nat.check(nat.lib().spc_set_sample_path(self._h, code))
 
     def set_memory_limit(self, nbytes: int) -> None:

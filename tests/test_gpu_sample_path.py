@@ -1,6 +1,8 @@
-"""The one-CTA-per-sample propagation of small systems (spc_set_sample_path)
-against the CPU oracle (1e-10 absolute, as every parity test) and against the
-tiled path (rounding-level agreement, the same Krylov rebuild schedule)."""
+"""The per-sample propagation of small systems (spc_set_sample_path) against
+the CPU oracle (1e-10 absolute, as every parity test) and against the tiled
+path (rounding-level agreement, the same Krylov rebuild schedule), in both
+of its forms: 'on' runs these calls (at most half as many samples as SMs) on
+a cluster of two CTAs per sample, 'single' on one CTA per sample."""
 import numpy as np
 import pytest
 
@@ -22,13 +24,16 @@ def _diff(a, b):
     return max(np.max(np.abs(getattr(a, k) - getattr(b, k))) for k in KEYS)
 
 
+MODES = ("on", "single", "off")
+
+
 def _both(sampler, run, method):
-    """run() on the per-sample path and on the tiled path; returns the two
-    results and their stats."""
+    """run() on the per-sample path (two CTAs per sample, then one) and on
+    the tiled path; returns the results and their stats by mode."""
     out = {}
     sampler.set_krylov(method)
     try:
-        for mode in ("on", "off"):
+        for mode in MODES:
             sampler.set_sample_path(mode)
             res = run()
             out[mode] = (res, sampler.stats())
@@ -62,11 +67,11 @@ def test_small_pair_reference_builder(sampler, oracle, method, m):
         return sampler.trace_sampling(zk, DT, t_end, m, 1e-6)
 
     r = _both(sampler, run, method)
-    assert _err(r["on"][0], ref) <= ABS_TOL
-    assert _err(r["off"][0], ref) <= ABS_TOL
-    assert _diff(r["on"][0], r["off"][0]) <= 1e-12
-    assert r["on"][1]["krylov_builds"] == r["off"][1]["krylov_builds"] == int(ref["n_builds"].sum())
-    assert r["on"][1]["sample_steps"] == r["off"][1]["sample_steps"]
+    for mode in MODES:
+        assert _err(r[mode][0], ref) <= ABS_TOL
+        assert _diff(r[mode][0], r["off"][0]) <= 1e-12
+        assert r[mode][1]["krylov_builds"] == int(ref["n_builds"].sum())
+        assert r[mode][1]["sample_steps"] == r["off"][1]["sample_steps"]
 
 
 @pytest.mark.parametrize("rates", [(1.0, 1.0), (3.0, 0.5)])
@@ -85,9 +90,9 @@ def test_anisotropic_tilted_field(sampler, oracle, rates):
         return sampler.trace_sampling(zk, DT, t_end, 16, 1e-5)
 
     r = _both(sampler, run, "auto")
-    assert _err(r["on"][0], ref) <= ABS_TOL
-    assert _err(r["off"][0], ref) <= ABS_TOL
-    assert _diff(r["on"][0], r["off"][0]) <= 1e-12
+    for mode in MODES:
+        assert _err(r[mode][0], ref) <= ABS_TOL
+        assert _diff(r[mode][0], r["off"][0]) <= 1e-12
 
 
 def test_uneven_batch(sampler, oracle):
@@ -106,11 +111,12 @@ def test_uneven_batch(sampler, oracle):
         return sampler.trace_sampling_batch(zks, DT, t_end, 14, 1e-6)
 
     r = _both(sampler, run, "auto")
-    for sy, f, zk, g_on, g_off in zip(systems, fields, zks, r["on"][0], r["off"][0]):
+    for i, (sy, f, zk) in enumerate(zip(systems, fields, zks)):
         rp, col, val = iso_csr(oracle, sy, f)
         ref = oracle.trace_sampling(rp, col, val, zk, DT, t_end, 14, 1e-6)
-        assert _err(g_on, ref) <= ABS_TOL
-        assert _diff(g_on, g_off) <= 1e-12
+        for mode in MODES:
+            assert _err(r[mode][0][i], ref) <= ABS_TOL
+            assert _diff(r[mode][0][i], r["off"][0][i]) <= 1e-12
 
 
 def test_exact_basis_and_lanczos_fallback(sampler, oracle):
@@ -129,17 +135,42 @@ def test_exact_basis_and_lanczos_fallback(sampler, oracle):
         return sampler.trace_sampling(zk, dt, t_end, 10, 1e-8)
 
     r = _both(sampler, run, "lanczos")
-    for mode in ("on", "off"):
+    for mode in MODES:
         assert _err(r[mode][0], ref) <= ABS_TOL
         assert r[mode][1]["krylov_builds"] == int(ref["n_builds"].sum())
         assert r[mode][1]["lanczos_fallbacks"] > 0
 
 
-def test_windows_shorter_than_dt_and_initial_states(sampler, oracle):
+@pytest.mark.parametrize("method", ["mgs", "lanczos"])
+def test_one_build_over_many_steps(sampler, oracle, method):
+    """tol = 1 never triggers a rebuild (|c_{m-1}|^2 <= |c|^2), so one Krylov
+    basis serves all 150 dt steps: the two-CTA form's dt loop then runs in
+    several history segments of at most 64 steps."""
+    s = W.small_pair()
+    rp, col, val = iso_csr(oracle, s, 0.05)
+    zk = W.random_phase_samples(s.Z, 20, seed=9)
+    t_end = 150 * DT
+    ref = oracle.trace_sampling(rp, col, val, zk, DT, t_end, 20, 1.0)
+    assert int(ref["n_builds"].sum()) == 20
+
+    def run():
+        sampler.set_h(rp, col, val)
+        return sampler.trace_sampling(zk, DT, t_end, 20, 1.0)
+
+    r = _both(sampler, run, method)
+    for mode in MODES:
+        assert _err(r[mode][0], ref) <= ABS_TOL
+        assert _diff(r[mode][0], r["off"][0]) <= 1e-12
+        assert r[mode][1]["krylov_builds"] == 20
+        assert r[mode][1]["sample_steps"] == r["off"][1]["sample_steps"]
+
+
+@pytest.mark.parametrize("mode", ["on", "single"])
+def test_windows_shorter_than_dt_and_initial_states(sampler, oracle, mode):
     s = W.small_pair()
     rp, col, val = iso_csr(oracle, s, 0.05)
     zk = W.random_phase_samples(s.Z, 3, seed=5)
-    sampler.set_sample_path("on")
+    sampler.set_sample_path(mode)
     try:
         sampler.set_h(rp, col, val)
         for t_end in (0.0, 0.05, DT):
@@ -189,7 +220,7 @@ def test_pair_without_nuclei(sampler, oracle, m, rates):
         return sampler.trace_sampling(zk, DT, 20 * DT, m, 1e-6)
 
     r = _both(sampler, run, "auto")
-    for mode in ("on", "off"):
+    for mode in MODES:
         assert _err(r[mode][0], ref) <= ABS_TOL
         assert r[mode][1]["krylov_builds"] == int(ref["n_builds"].sum())
 
