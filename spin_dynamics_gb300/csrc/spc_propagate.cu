@@ -525,16 +525,21 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
     rowsum[i] = s;
   }
   expm_sync<WARP>();
-  if (tid == 0) {
+  if (tid < 32) {
+    // the largest row sum by a warp maximum (exact: the same value in any order)
     double an = 0.0;
-    for (int i = 0; i < m; ++i) an = fmax(an, rowsum[i]);
-    int s = 0;
-    if (an > 0.0) {
-      const double l2 = log(an) / log(2.0);  // log_2 (:106-117)
-      const int ee = (int)l2 + 1;            // int() truncates toward zero
-      s = max(0, ee + 1);
+    for (int i = tid; i < m; i += 32) an = fmax(an, rowsum[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) an = fmax(an, __shfl_xor_sync(0xffffffffu, an, o));
+    if (tid == 0) {
+      int s = 0;
+      if (an > 0.0) {
+        const double l2 = log(an) / log(2.0);  // log_2 (:106-117)
+        const int ee = (int)l2 + 1;            // int() truncates toward zero
+        s = max(0, ee + 1);
+      }
+      *s_sh = s;
     }
-    *s_sh = s;
   }
   expm_sync<WARP>();
   const int s = *s_sh;
@@ -701,17 +706,33 @@ __device__ void expm_one(int m, int mld, const double2* __restrict__ Ain, double
     for (int k = tid; k < m; k += nt) A2[k + k * m] = crcp(D[k + k * m]);
     expm_sync<WARP>();
   }
-  for (int k = m - 1; k >= 0; --k) {
-    if (swapped)
+  if (swapped) {
+    for (int k = m - 1; k >= 0; --k) {
       for (int j = tid; j < m; j += nt) E[k + j * m] = cdiv(E[k + j * m], D[k + k * m]);
-    else
-      for (int j = tid; j < m; j += nt) E[k + j * m] = cmul(E[k + j * m], A2[k + k * m]);
-    expm_sync<WARP>();
-    const int i0 = max(0, k - uU), ri = k - i0;
-    for (int idx = tid; idx < ri * m; idx += nt) {
-      const int i = i0 + idx % ri, j = idx / ri;
-      E[i + j * m] = cfms(D[i + k * m], E[k + j * m], E[i + j * m]);
+      expm_sync<WARP>();
+      for (int idx = tid; idx < k * m; idx += nt) {
+        const int i = idx % k, j = idx / k;
+        E[i + j * m] = cfms(D[i + k * m], E[k + j * m], E[i + j * m]);
+      }
+      expm_sync<WARP>();
     }
+  } else {
+    // one sync per step: row k's solution, E_kj times the pivot's
+    // reciprocal, goes to T (N is spent), and every thread that updates a
+    // row above forms the same product itself
+    for (int k = m - 1; k >= 0; --k) {
+      const int i0 = max(0, k - uU), ri = k - i0 + 1;  // rows i0..k
+      for (int idx = tid; idx < ri * m; idx += nt) {
+        const int i = i0 + idx % ri, j = idx / ri;
+        const double2 ek = cmul(E[k + j * m], A2[k + k * m]);
+        if (i == k)
+          T[k + j * m] = ek;
+        else
+          E[i + j * m] = cfms(D[i + k * m], ek, E[i + j * m]);
+      }
+      expm_sync<WARP>();
+    }
+    for (int i = tid; i < mm; i += nt) E[i] = T[i];
     expm_sync<WARP>();
   }
   // s squarings

@@ -277,8 +277,8 @@ __device__ __forceinline__ void small_krylov(const SmallJob& J, bool lz, bool he
   double beta = 0.0;
   for (int i = 0; i < me; ++i) {
     const double2* qi = Q + (size_t)i * n;
+    // no barrier: the pass below reads only the rows this thread just wrote
     small_spmm(J, qi, p, !lz && herm, kap);
-    __syncthreads();
     if (lz) {
       // p -= beta_{i-1} Q_{i-1}; alpha_i = Re <Q_i, p>
       double a2 = 0.0;
