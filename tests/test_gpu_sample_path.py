@@ -102,7 +102,7 @@ def test_uneven_batch(sampler, oracle):
     fields = [0.2, 0.05, 0.3]
     for sy in systems:
         sy.kS = sy.kT = 1.0 / GAMMA_E
-    Ms = [5, 40, 33]
+    Ms = [5, 30, 33]  # 68 samples: the two-CTA form on a 152-SM part
     zks = [W.random_phase_samples(sy.Z, M, seed=20 + i) for i, (sy, M) in enumerate(zip(systems, Ms))]
     t_end = 60 * DT
 
