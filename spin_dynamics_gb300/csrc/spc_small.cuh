@@ -984,6 +984,7 @@ static int propagate_small(Handle* h, const double* theta, const double* init_po
   // pair form (two CTAs per sample) when the samples fill at most half the
   // SMs and its shared memory fits: history buffers of up to 64 steps
   bool pair = h->sample_path != SPC_SAMPLE_SINGLE && 2 * (int64_t)G <= h->sm_count;
+  CK(cudaGetLastError());  // a failed query below is cleared, not an earlier error
   int hmax = 64;
   size_t psmem = 0;
   bool pvec = false;
@@ -994,6 +995,18 @@ static int propagate_small(Handle* h, const double* theta, const double* init_po
     psmem = std::max(help, sizeof(double2) * pair_main_elems(m, nmax, pvec));
     pair = psmem <= budget &&
            cudaFuncSetAttribute(k_small_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem) == cudaSuccess;
+    if (pair) {
+      // every cluster resident at once (SMs pair up within a GPC, so this can
+      // be fewer than half the SMs)
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * G);
+      cfg.blockDim = dim3(SMALL_THREADS);
+      cfg.dynamicSmemBytes = psmem;
+      cfg.stream = st;
+      int ncl = 0;
+      pair = cudaOccupancyMaxActiveClusters(&ncl, k_small_pair, &cfg) == cudaSuccess && ncl >= G;
+    }
+    if (!pair) (void)cudaGetLastError();  // fall back to one CTA per sample
   }
   int pe = h->prof.begin(st);
   if (pair) {
