@@ -40,10 +40,10 @@ from spin_dynamics_gb300 import workloads as W  # noqa: E402
 METRIC = "sample-steps/s at dim 55296: batched+adjoint vs plain on GB300 at |\u0394\u03a6S|\u22641e-10"
 
 # DRAM traffic per k_spmm launch (dram__bytes_read.sum + dram__bytes_write.sum)
-# from one ncu capture at 64 sample columns (392 MB = 33 MB of Hamiltonian +
-# 359 MB that scales with the columns), scaled to the launch's column count.
+# from one ncu capture at 64 sample columns (409 MB = 33 MB of Hamiltonian +
+# 376 MB that scales with the columns), scaled to the launch's column count.
 SPMM_TRAFFIC_H = 33.2e6
-SPMM_TRAFFIC_PER_COLUMN = (392.2e6 - 33.2e6) / 64
+SPMM_TRAFFIC_PER_COLUMN = (409.1e6 - 33.2e6) / 64
 
 
 def parse():
