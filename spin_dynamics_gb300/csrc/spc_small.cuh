@@ -11,6 +11,9 @@
 // most SMALL_NMAX rows, m <= 32, a small estimated build and the samples fill
 // at most two waves of CTAs (small_path_fits).
 //
+// Calls with few samples give each sample a cluster of two CTAs instead
+// (k_small_pair, below).
+//
 // Per sample the arithmetic is the tiled path's: the SpMM row loop of k_spmm,
 // real-coefficient Lanczos on the Hermitian part (orthonormality checked from
 // the projector Grams, MGS rebuild when it fails) or MGS, expm_one, the four
@@ -604,9 +607,10 @@ __global__ void __launch_bounds__(SMALL_THREADS, 2)
 }
 
 // ---------------------------------------------------------------------------
-// Pair form: a cluster of two CTAs per sample, for calls with at most half as
-// many samples as SMs (the dim-288 workload runs 64 samples on 152 SMs, so
-// one CTA per sample leaves 88 SMs idle). The main CTA (cluster rank 0) keeps
+// Pair form: a cluster of two CTAs per sample, for calls whose clusters are
+// all resident at once (at most half as many samples as SMs: the dim-288
+// workload runs 64 samples on 152 SMs, so one CTA per sample leaves 88 SMs
+// idle). The main CTA (cluster rank 0) keeps
 // the sample's serial path: the Krylov builds, the expm, the recurrence
 // c <- E c of the dt loop with its stop test, and psi = Q c. The helper CTA
 // (rank 1) takes the work off that path:
