@@ -28,6 +28,18 @@ def test_header_declares_expected_entry_points():
         assert n in names
 
 
+def test_header_constants_match_the_binding():
+    """Every #define SPC_* of the header has the same value in _native."""
+    defs = dict(re.findall(r"^#define (SPC_\w+) (\d+)", open(HEADER).read(), flags=re.M))
+    assert "SPC_SAMPLE_SINGLE" in defs
+    for name, value in defs.items():
+        if hasattr(nat, name):
+            assert getattr(nat, name) == int(value), name
+    for name in ("SPC_SAMPLE_AUTO", "SPC_SAMPLE_OFF", "SPC_SAMPLE_ON", "SPC_SAMPLE_SINGLE",
+                 "SPC_KRYLOV_MGS", "SPC_KRYLOV_LANCZOS", "SPC_KRYLOV_AUTO"):
+        assert getattr(nat, name) == int(defs[name]), name
+
+
 def test_library_exports_every_declared_symbol():
     L = nat.lib()
     for name in declared_functions():
